@@ -1,0 +1,438 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the multi-pass PIV path on one GB300.
+
+Workload: 1024x1024 uint8 synthetic particle-image pairs (0.03 particles/px,
+sinusoidal shear u = 6 sin(2 pi y/256), v = 2 cos(2 pi x/512)), three passes
+64 -> 32 -> 16 px at 50% overlap (n_fft = 2, so 128/64/32-point DFTs),
+bilinear deformation on pass 2 and cubic B-spline on pass 3 (deforming_order
+1, 3, 3), Gaussian subpixel fit, median validation (tol 2, 3x3) with two
+revalidated spring replacements, smoothn with GCV between passes, float32.
+
+A step is one run of the whole pipeline over a batch of pairs resident in
+HBM (captured once as a CUDA graph and replayed). ``value`` is pairs/s over
+the timed steps; ``e2e`` is the same through the public Python API with the
+frames copied from pinned host memory and the fields copied back every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--pairs B] [--impl gpu|reference]
+
+Under torchrun each rank processes its own batch on its own GPU (replicas,
+no collective on the data path); rank 0 prints one JSON line.
+"""
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "openpiv-python-gpu_gb300")
+for p in (PKG, ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "frame pairs/s (1024x1024, 64->32->16 px three-pass PIV) on 1 GB300"
+WORKLOAD = ("1024x1024 uint8 pairs, 0.03 ppp, shear 6/2 px; 64->32->16 px @50%, n_fft=2; deforming_order (1,3,3); "
+            "median validation tol 2 + 2 revalidated spring replacements; smoothn GCV; float32")
+FRAME = (1024, 1024)
+DISTINCT = 16
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--pairs", type=int, default=128, help="pairs per step per GPU")
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--dft", choices=["fft", "tensor"], default="fft", help="correlation engine of the chosen form")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    return ap.parse_args()
+
+
+def piv_settings():
+    from openpiv_gpu import synthetic
+
+    kw = dict(synthetic.CONFIGS[2]["piv"])
+    mss = kw.pop("min_search_size")
+    return mss, kw
+
+
+def _make_pair(k):
+    sys.path.insert(0, PKG)
+    from openpiv_gpu import synthetic
+
+    a, b, _, _ = synthetic.config_case(2, k)
+    return a, b
+
+
+def generate_pairs(n):
+    """n distinct seeded pairs (seed 2000 + k), rendered in a spawn pool."""
+    import multiprocessing as mp
+
+    workers = max(1, min(n, os.cpu_count() or 1))
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_make_pair, range(n))
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (the reference algorithm restated in NumPy/SciPy).
+# ---------------------------------------------------------------------------
+def _oracle_pair(args):
+    k, dtype_f = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, ROOT)
+    from oracle.piv_oracle import OraclePIV
+    from openpiv_gpu import synthetic
+
+    a, b, _, piv = synthetic.config_case(2, k)
+    piv = dict(piv)
+    piv["dtype_f"] = dtype_f
+    mss = piv.pop("min_search_size")
+    t = time.perf_counter()
+    u, v = OraclePIV(a.shape, mss, **piv)(a, b)
+    return time.perf_counter() - t, u, v
+
+
+def cpu_pool(workers):
+    import multiprocessing as mp
+
+    return mp.get_context("spawn").Pool(workers)
+
+
+def cpu_throughput(pool, workers, steps, warmup, dtype_f="float32"):
+    """Times `steps` rounds of one oracle pair per worker; returns pairs/s."""
+    for _ in range(warmup):
+        pool.map(_oracle_pair, [(k % DISTINCT, dtype_f) for k in range(workers)])
+    t0 = time.perf_counter()
+    for s in range(steps):
+        pool.map(_oracle_pair, [((s * workers + k) % DISTINCT, dtype_f) for k in range(workers)])
+    dt = time.perf_counter() - t0
+    return steps * workers / dt, dt
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region.
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1].split()[0]), float(parts[2].split()[0]), parts[5:9]))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, s in enumerate(r) if s.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# Roofline helpers.
+# ---------------------------------------------------------------------------
+def corr_flops(ss, N):
+    """Algorithmic FLOPs of one window-pair correlation: two real-to-complex and
+    one complex-to-real 2-D FFT at 2.5 N^2 log2(N^2) each, the conjugate
+    product and the mean removal."""
+    return 3 * 2.5 * N * N * math.log2(N * N) + 6 * N * (N // 2 + 1) + 4 * ss * ss
+
+
+def sgemm_tflops(torch):
+    """FP32 SIMT reference throughput: cuBLAS SGEMM with TF32 disabled."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# Arms.
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    pool = cpu_pool(workers)
+    value, dt = cpu_throughput(pool, workers, args.steps, args.warmup)
+    pool.close()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded particle images)",
+        "config": {"workload": WORKLOAD, "pairs_per_step": workers, "frame": list(FRAME)},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": workers, "kind": "port",
+                         "sample": f"{workers} pairs per step, one per worker process, NumPy/SciPy restatement "
+                                   "of the reference algorithm in float32"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+
+    # CPU pool first (spawn), before heavy CUDA work.
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_pool(os.cpu_count() or 1)
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from openpiv_gpu import _lib
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    lib = _lib.load()
+    B = args.pairs
+    pairs = generate_pairs(DISTINCT)
+    idx = [(rank * B + k) % DISTINCT for k in range(B)]
+    host_a = np.stack([pairs[i][0] for i in idx])
+    host_b = np.stack([pairs[i][1] for i in idx])
+    fa = torch.as_tensor(host_a).cuda()
+    fb = torch.as_tensor(host_b).cuda()
+    mss, kw = piv_settings()
+    stream = torch.cuda.Stream()
+
+    def make(dft):
+        proc = PIVGPU(FRAME, mss, **kw, dft=dft)
+        with torch.cuda.stream(stream):
+            for _ in range(max(1, args.warmup)):
+                proc.run_batch(fa, fb)
+        stream.synchronize()
+        return proc
+
+    def graph_time(proc):
+        plan = proc.plan_handle(fa, B)
+        m, n = proc.piv_fields[-1].field_shape
+        u = torch.empty((B, m, n), dtype=torch.float64, device="cuda")
+        v = torch.empty_like(u)
+        val = torch.empty((B, m, n), dtype=torch.uint8, device="cuda")
+        out = torch.empty_like(val)
+        nk = ctypes.c_int(0)
+        s = stream.cuda_stream
+        _lib.check(lib.piv_plan_graph_capture(plan, B, fa.data_ptr(), fb.data_ptr(), u.data_ptr(), v.data_ptr(),
+                                              val.data_ptr(), out.data_ptr(), ctypes.byref(nk), s))
+        for _ in range(args.warmup):
+            _lib.check(lib.piv_plan_graph_launch(plan, s))
+        stream.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            _lib.check(lib.piv_plan_graph_launch(plan, s))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        return ms, nk.value, (u, v)
+
+    proc = make(args.dft)
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, kernels, (u_dev, v_dev) = graph_time(proc)
+    clocks = sampler.stop()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = B * world / (ms_step * 1e-3)
+    windows_per_pair = sum(f.n_wins for f in proc.piv_fields)
+
+    # Stage breakdown (CUDA events inside the run, same stream).
+    plan = proc.plan_handle(fa, B)
+    _lib.check(lib.piv_plan_set_timing(plan, 1))
+    n_stage_runs = 3
+    with torch.cuda.stream(stream):
+        for _ in range(n_stage_runs):
+            proc.run_batch(fa, fb)
+    stream.synchronize()
+    n_it = len(proc.piv_fields)
+    cap = n_it * 6 + 2
+    buf = (ctypes.c_float * cap)()
+    runs = ctypes.c_int(0)
+    _lib.check(lib.piv_plan_stage_times(plan, buf, cap, ctypes.byref(runs)))
+    _lib.check(lib.piv_plan_set_timing(plan, 0))
+    stage_ms = {}
+    for k in range(n_it):
+        for s, name in enumerate(_lib.STAGES):
+            t = buf[k * 6 + s] / max(1, runs.value)
+            if t > 0:
+                stage_ms[f"it{k}.{name}"] = round(t, 4)
+
+    # Dominant kernel roofline: the correlation stage with the largest time.
+    corr = {k: v for k, v in stage_ms.items() if k.endswith("correlate")}
+    dom = max(corr, key=corr.get)
+    kdom = int(dom[2:dom.index(".")])
+    f = proc.piv_fields[kdom]
+    N = proc._iterations[kdom].fft_size
+    flops = B * f.n_wins * corr_flops(f.search_size, N)
+    achieved = flops / (corr[dom] * 1e-3) / 1e12
+    peaks = measured_peaks()
+    traffic = ncu_traffic().get(f"correlate_N{N}")
+    if args.dft == "tensor":
+        peak, unit, bound, src = peaks.get("bf16_tflops", 1900.0), "TFLOP/s", "tensor", "MEASURED_PEAKS.json bf16"
+    else:
+        peak, unit, bound, src = sgemm_tflops(torch), "TFLOP/s", "fp32", "cuBLAS SGEMM (TF32 off) measured here"
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                "traffic": traffic * B * f.n_wins / max(1, B * f.n_wins) if traffic else None,
+                "kernel": f"correlate pass {kdom + 1} (ss={f.search_size}, N={N}, {B * f.n_wins} windows/launch)",
+                "peak_source": src, "launch_ms": corr[dom]}
+
+    # End to end through the public API: pinned host frames in, fields out.
+    pin_a = torch.as_tensor(host_a).pin_memory()
+    pin_b = torch.as_tensor(host_b).pin_memory()
+    na, nb = pin_a.numpy(), pin_b.numpy()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            proc.run_batch(na, nb, host_out=True)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            res_u, res_v = proc.run_batch(na, nb, host_out=True)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    m, n = proc.piv_fields[-1].field_shape
+    e2e = {"value": B * world * args.steps / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": int(2 * B * FRAME[0] * FRAME[1]),
+           "d2h_bytes_per_step": int(B * m * n * (8 + 8 + 1 + 1))}
+
+    # Accuracy of pair 0 against the float64 oracle (and the float32 parity oracle).
+    accuracy = None
+    if rank == 0 and not args.no_accuracy and cpu is not None:
+        (_, u64, v64), (_, u32, v32) = cpu.map(_oracle_pair, [(0, "float64"), (0, "float32")])
+        gu, gv = res_u[0].astype(np.float64), res_v[0].astype(np.float64)
+        rms = lambda a, b, c, d: float(np.sqrt(np.mean((a - b) ** 2 + (c - d) ** 2)))
+        accuracy = {"rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64), "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
+                    "max_px_vs_fp32_oracle": float(max(np.abs(gu - u32).max(), np.abs(gv - v32).max()))}
+
+    cpu_baseline = None
+    if cpu is not None:
+        workers = os.cpu_count() or 1
+        cval, cdt = cpu_throughput(cpu, workers, 1, 0)
+        cpu.close()
+        cpu_baseline = {"value": cval, "unit": "pairs/s", "cores": workers, "kind": "port",
+                        "sample": f"{workers} pairs, one per worker process (NumPy/SciPy restatement of the "
+                                  f"reference algorithm, float32), {cdt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded particle images)",
+            "config": {"workload": WORKLOAD, "pairs_per_step": B, "distinct_pairs": DISTINCT, "frame": list(FRAME),
+                       "form": args.dft, "graph": True,
+                       "l2": "inputs larger than L2 (B x 2 MiB frames + 8 MiB float frames per pair per pass)"},
+            "windows_per_s": value * windows_per_pair, "windows_per_pair": windows_per_pair,
+            "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
+            "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
+            "stage_ms": stage_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,833 @@
+// C ABI and the multi-pass plan executor.
+//
+// piv_plan_run restates PIVGPU.__call__ (gpu_process.py:564-647) for a batch
+// of equally sized frame pairs, as a fixed sequence of kernel launches on one
+// stream with no host synchronisation between them:
+//   for each iteration k:
+//     k > 0: predictor onto the grid (regrid when the window size changes,
+//            gpu_process.py:730-742), frame deformation (gpu_process.py:1149-1192)
+//     correlation + peak + subpixel (+ S2N)        (gpu_process.py:1021-1097)
+//     u = u_corr (+ up)                            (gpu_process.py:631-632)
+//     validation, replacement loop                 (gpu_process.py:744-834)
+//     smoothn unless last                          (gpu_process.py:637-639, 836-845)
+//   scaling                                        (gpu_process.py:641-643)
+// Data-dependent branches of the reference (no outliers, singular spring
+// system, GCV search) are decided on the device, so a run can be captured in a
+// CUDA graph.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "piv_common.cuh"
+#include "piv_internal.h"
+
+namespace piv {
+
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int set_cuda_error(cudaError_t e, const char* what) {
+  const int code = (e == cudaErrorMemoryAllocation) ? PIV_E_OOM : PIV_E_CUDA;
+  return set_error(code, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int sm_count() {
+  static std::mutex mu;
+  static int counts[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (counts[dev] == 0) {
+    int c = 0;
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    counts[dev] = c > 0 ? c : 1;
+  }
+  return counts[dev];
+}
+
+static size_t pixel_bytes(int pixel_type) {
+  switch (pixel_type) {
+    case PIV_PIXEL_U8: return 1;
+    case PIV_PIXEL_U16: return 2;
+    case PIV_PIXEL_F32: return 4;
+    case PIV_PIXEL_F64: return 8;
+    default: return 0;
+  }
+}
+
+int field_geometry(int height, int width, int window_size, int search_size, double overlap_ratio, int center,
+                   piv_geometry* g) {
+  if (height <= 0 || width <= 0 || search_size <= 0 || window_size <= 0 || window_size > search_size)
+    return set_error(PIV_E_ARG, "invalid geometry (frame %dx%d, window %d, search %d)", height, width, window_size,
+                     search_size);
+  if (!(overlap_ratio >= 0 && overlap_ratio < 1)) return set_error(PIV_E_ARG, "overlap_ratio must be in [0, 1)");
+  const int overlap = (int)(overlap_ratio * search_size);  // int(overlap_ratio * search_size)
+  const int spacing = search_size - overlap;
+  if (height < search_size || width < search_size)
+    return set_error(PIV_E_ARG, "frame %dx%d smaller than search size %d", height, width, search_size);
+  g->height = height;
+  g->width = width;
+  g->search_size = search_size;
+  g->window_size = window_size;
+  g->spacing = spacing;
+  // Python floor division of non-negative operands.
+  g->m = (height - search_size) / spacing + 1;
+  g->n = (width - search_size) / spacing + 1;
+  if (center) {
+    const int xr = width - (spacing * (g->n - 1) + search_size);
+    const int yr = height - (spacing * (g->m - 1) + search_size);
+    g->x_offset = xr / 2 + search_size % 2;
+    g->y_offset = yr / 2 + search_size % 2;
+  } else {
+    g->x_offset = g->y_offset = 0;
+  }
+  return PIV_OK;
+}
+
+}  // namespace piv
+
+using namespace piv;
+
+struct IterState {
+  piv_iteration it;
+  piv_geometry g;
+  int fp32;
+  size_t mn;
+  void* u_corr = nullptr;
+  void* v_corr = nullptr;
+  double* up = nullptr;
+  double* vp = nullptr;
+  double* u_rep = nullptr;
+  double* v_rep = nullptr;
+  double* u_out = nullptr;
+  double* v_out = nullptr;
+  uint8_t* val0 = nullptr;
+  uint8_t* val = nullptr;
+  double* smooth_p = nullptr;
+  int* peak_i = nullptr;
+  int* peak_j = nullptr;
+  void* s2n = nullptr;
+  uint8_t* field_mask = nullptr;
+};
+
+struct piv_plan {
+  piv_config cfg;
+  std::vector<piv_iteration> iters;
+  std::vector<IterState> st;
+  int device = 0;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  void* stage_a = nullptr;
+  void* stage_b = nullptr;
+  void* def_a = nullptr;
+  void* def_b = nullptr;
+  float* coef = nullptr;
+  uint8_t* frame_mask = nullptr;
+  void* corr_scratch = nullptr;
+  size_t corr_scratch_bytes = 0;
+  void* rep_scratch = nullptr;
+  void* smooth_scratch = nullptr;
+  double* rms_stats = nullptr;
+  uint8_t* outliers = nullptr;
+  double* u_final = nullptr;
+  double* v_final = nullptr;
+  bool any_cubic = false;
+  std::vector<uint8_t> host_mask;
+  // Stage timing.
+  bool timing = false;
+  struct TimedRun {
+    cudaEvent_t start;
+    std::vector<int> ids;
+    std::vector<cudaEvent_t> ev;
+  };
+  std::vector<TimedRun> timed;
+  std::vector<cudaEvent_t> event_pool;
+  // CUDA graph of one run.
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
+static cudaEvent_t take_event(piv_plan* p) {
+  if (!p->event_pool.empty()) {
+    cudaEvent_t e = p->event_pool.back();
+    p->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+static int plan_alloc(piv_plan* p, void** ptr, size_t bytes) {
+  *ptr = nullptr;
+  if (bytes == 0) return PIV_OK;
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(PIV_E_OOM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  p->allocs.push_back(*ptr);
+  p->bytes += bytes;
+  return PIV_OK;
+}
+
+template <typename Ptr>
+static int plan_alloc_t(piv_plan* p, Ptr** ptr, size_t count) {
+  void* v = nullptr;
+  int rc = plan_alloc(p, &v, count * sizeof(Ptr));
+  *ptr = reinterpret_cast<Ptr*>(v);
+  return rc;
+}
+
+static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+extern "C" {
+
+int piv_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return PIV_E_ARG;
+  strncpy(buf, g_last_error, len - 1);
+  buf[len - 1] = 0;
+  return PIV_OK;
+}
+
+int piv_memcpy(void* dst, const void* src, size_t bytes, int kind, void* stream) {
+  if (bytes == 0) return PIV_OK;
+  if (!dst || !src) return set_error(PIV_E_ARG, "NULL argument");
+  const cudaMemcpyKind k = kind == 0 ? cudaMemcpyDeviceToHost : (kind == 1 ? cudaMemcpyHostToDevice
+                                                                            : cudaMemcpyDeviceToDevice);
+  cudaError_t e = stream ? cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream) : cudaMemcpy(dst, src, bytes, k);
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "piv_memcpy");
+}
+
+int piv_field_geometry(int height, int width, int window_size, int search_size, double overlap_ratio, int center,
+                       piv_geometry* geom) {
+  if (!geom) return set_error(PIV_E_ARG, "geom is NULL");
+  return field_geometry(height, width, window_size, search_size, overlap_ratio, center, geom);
+}
+
+void piv_plan_destroy(piv_plan* p) {
+  if (!p) return;
+  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  for (auto& r : p->timed) {
+    p->event_pool.push_back(r.start);
+    for (auto e : r.ev) p->event_pool.push_back(e);
+  }
+  for (auto e : p->event_pool) cudaEventDestroy(e);
+  for (void* a : p->allocs) cudaFree(a);
+  delete p;
+}
+
+int piv_plan_set_timing(piv_plan* p, int enable) {
+  if (!p) return set_error(PIV_E_ARG, "NULL plan");
+  p->timing = enable != 0;
+  return PIV_OK;
+}
+
+int piv_plan_stage_times(piv_plan* p, float* ms, int capacity, int* runs) {
+  if (!p || !ms) return set_error(PIV_E_ARG, "NULL argument");
+  const int need = (int)p->st.size() * PIV_STAGES + 2;
+  if (capacity < need) return set_error(PIV_E_ARG, "stage_times needs capacity %d", need);
+  for (int k = 0; k < need; ++k) ms[k] = 0.0f;
+  int n = 0;
+  for (auto& r : p->timed) {
+    if (!r.ev.empty()) cudaEventSynchronize(r.ev.back());
+    cudaEvent_t prev = r.start;
+    for (size_t k = 0; k < r.ev.size(); ++k) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, prev, r.ev[k]);
+      if (r.ids[k] >= 0 && r.ids[k] < need) ms[r.ids[k]] += t;
+      prev = r.ev[k];
+    }
+    p->event_pool.push_back(r.start);
+    for (auto e : r.ev) p->event_pool.push_back(e);
+    ++n;
+  }
+  p->timed.clear();
+  if (runs) *runs = n;
+  return cudaGetLastError() == cudaSuccess ? PIV_OK : set_error(PIV_E_CUDA, "stage timing failed");
+}
+
+int piv_plan_create(const piv_config* cfg, piv_plan** out) {
+  if (!cfg || !out) return set_error(PIV_E_ARG, "NULL argument");
+  *out = nullptr;
+  if (cfg->n_iters <= 0 || !cfg->iters) return set_error(PIV_E_ARG, "no iterations");
+  if (cfg->max_pairs <= 0) return set_error(PIV_E_ARG, "max_pairs must be positive");
+  if (pixel_bytes(cfg->pixel_type) == 0) return set_error(PIV_E_ARG, "unknown pixel_type %d", cfg->pixel_type);
+  if (cfg->dtype != PIV_DTYPE_F32 && cfg->dtype != PIV_DTYPE_F64) return set_error(PIV_E_ARG, "unknown dtype");
+  if (!(cfg->dt > 0) || !(cfg->scaling_par > 0)) return set_error(PIV_E_ARG, "dt and scaling_par must be > 0");
+  piv_plan* p = new piv_plan();
+  p->cfg = *cfg;
+  p->iters.assign(cfg->iters, cfg->iters + cfg->n_iters);
+  p->cfg.iters = p->iters.data();
+  cudaGetDevice(&p->device);
+  const int P = cfg->max_pairs, H = cfg->height, W = cfg->width;
+  const size_t hw = (size_t)H * W;
+  const size_t tsz = cfg->dtype == PIV_DTYPE_F64 ? 8 : 4;
+  int rc = PIV_OK;
+  if (cfg->mask) p->host_mask.assign(cfg->mask, cfg->mask + hw);
+  p->st.resize(cfg->n_iters);
+  size_t max_mn = 0;
+  for (int k = 0; k < cfg->n_iters && rc == PIV_OK; ++k) {
+    const piv_iteration& it = p->iters[k];
+    IterState& s = p->st[k];
+    s.it = it;
+    rc = field_geometry(H, W, it.window_size, it.search_size, it.overlap_ratio, cfg->center, &s.g);
+    if (rc) break;
+    if (!is_pow2(it.fft_size) || it.fft_size < it.search_size || it.fft_size > 256) {
+      rc = set_error(PIV_E_UNSUPPORTED, "fft_size %d (search size %d) is not supported", it.fft_size,
+                     it.search_size);
+      break;
+    }
+    if (it.deforming_order == 3) p->any_cubic = true;
+    s.fp32 = (cfg->dtype == PIV_DTYPE_F32 && k == 0) ? 1 : 0;
+    s.mn = (size_t)s.g.m * s.g.n;
+    if (s.mn > max_mn) max_mn = s.mn;
+    const size_t cnt = s.mn * P;
+    if ((rc = plan_alloc(p, &s.u_corr, cnt * tsz))) break;
+    if ((rc = plan_alloc(p, &s.v_corr, cnt * tsz))) break;
+    if (k > 0) {
+      if ((rc = plan_alloc_t(p, &s.up, cnt))) break;
+      if ((rc = plan_alloc_t(p, &s.vp, cnt))) break;
+    }
+    if ((rc = plan_alloc_t(p, &s.u_rep, cnt))) break;
+    if ((rc = plan_alloc_t(p, &s.v_rep, cnt))) break;
+    if (k < cfg->n_iters - 1) {
+      if ((rc = plan_alloc_t(p, &s.u_out, cnt))) break;
+      if ((rc = plan_alloc_t(p, &s.v_out, cnt))) break;
+    } else {
+      s.u_out = s.u_rep;
+      s.v_out = s.v_rep;
+    }
+    if ((rc = plan_alloc_t(p, &s.val0, cnt))) break;
+    if ((rc = plan_alloc_t(p, &s.val, cnt))) break;
+    if ((rc = plan_alloc_t(p, &s.smooth_p, (size_t)P))) break;
+    if ((rc = plan_alloc_t(p, &s.peak_i, cnt))) break;
+    if ((rc = plan_alloc_t(p, &s.peak_j, cnt))) break;
+    if (!isnan(it.s2n_tol) && (rc = plan_alloc(p, &s.s2n, cnt * tsz))) break;
+    if (cfg->mask) {
+      std::vector<uint8_t> fm(s.mn);
+      for (int i = 0; i < s.g.m; ++i)
+        for (int j = 0; j < s.g.n; ++j) {
+          // mask[y.astype(int), x.astype(int)] at the window centres (gpu_process.py:951)
+          const int y = (int)(float)((double)i * s.g.spacing + s.g.search_size / 2.0 + s.g.y_offset);
+          const int x = (int)(float)((double)j * s.g.spacing + s.g.search_size / 2.0 + s.g.x_offset);
+          fm[(size_t)i * s.g.n + j] = cfg->mask[(size_t)y * W + x] ? 1 : 0;
+        }
+      if ((rc = plan_alloc_t(p, &s.field_mask, s.mn))) break;
+      cudaMemcpy(s.field_mask, fm.data(), s.mn, cudaMemcpyHostToDevice);
+    }
+    const size_t cs = correlate_fft_scratch_bytes(it.fft_size, cfg->dtype);
+    if (cs > p->corr_scratch_bytes) p->corr_scratch_bytes = cs;
+  }
+  if (rc == PIV_OK) rc = plan_alloc(p, &p->stage_a, (size_t)P * hw * pixel_bytes(cfg->pixel_type));
+  if (rc == PIV_OK) rc = plan_alloc(p, &p->stage_b, (size_t)P * hw * pixel_bytes(cfg->pixel_type));
+  if (rc == PIV_OK && cfg->n_iters > 1) {
+    rc = plan_alloc(p, &p->def_a, (size_t)P * hw * tsz);
+    if (rc == PIV_OK) rc = plan_alloc(p, &p->def_b, (size_t)P * hw * tsz);
+  }
+  if (rc == PIV_OK && p->any_cubic) rc = plan_alloc_t(p, &p->coef, 2 * (size_t)P * hw);
+  if (rc == PIV_OK && cfg->mask) {
+    rc = plan_alloc_t(p, &p->frame_mask, hw);
+    if (rc == PIV_OK) cudaMemcpy(p->frame_mask, cfg->mask, hw, cudaMemcpyHostToDevice);
+  }
+  if (rc == PIV_OK) rc = plan_alloc(p, &p->corr_scratch, p->corr_scratch_bytes);
+  if (rc == PIV_OK) rc = plan_alloc(p, &p->rep_scratch, replace_scratch_bytes(1, (int)max_mn, P));
+  size_t sm_bytes = 0;
+  for (auto& s : p->st) {
+    const size_t b = smoothn_scratch_bytes(s.g.m, s.g.n, P);
+    if (b > sm_bytes) sm_bytes = b;
+  }
+  if (rc == PIV_OK) rc = plan_alloc(p, &p->smooth_scratch, sm_bytes);
+  if (rc == PIV_OK) rc = plan_alloc_t(p, &p->rms_stats, 4 * (size_t)P);
+  if (rc == PIV_OK) {
+    const size_t cnt = p->st.back().mn * P;
+    rc = plan_alloc_t(p, &p->outliers, cnt);
+    if (rc == PIV_OK) rc = plan_alloc_t(p, &p->u_final, cnt);
+    if (rc == PIV_OK) rc = plan_alloc_t(p, &p->v_final, cnt);
+  }
+  if (rc != PIV_OK) {
+    piv_plan_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return PIV_OK;
+}
+
+int piv_plan_field_shape(const piv_plan* p, int iter, int* m, int* n) {
+  if (!p || !m || !n) return set_error(PIV_E_ARG, "NULL argument");
+  if (iter < 0) iter += (int)p->st.size();
+  if (iter < 0 || iter >= (int)p->st.size()) return set_error(PIV_E_ARG, "iteration %d out of range", iter);
+  *m = p->st[iter].g.m;
+  *n = p->st[iter].g.n;
+  return PIV_OK;
+}
+
+int piv_plan_workspace_bytes(const piv_plan* p, size_t* bytes) {
+  if (!p || !bytes) return set_error(PIV_E_ARG, "NULL argument");
+  *bytes = p->bytes;
+  return PIV_OK;
+}
+
+int piv_plan_iteration_view(const piv_plan* p, int iter, piv_iteration_view* v) {
+  if (!p || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (iter < 0 || iter >= (int)p->st.size()) return set_error(PIV_E_ARG, "iteration %d out of range", iter);
+  const IterState& s = p->st[iter];
+  v->m = s.g.m;
+  v->n = s.g.n;
+  v->u_corr = s.u_corr;
+  v->v_corr = s.v_corr;
+  v->up = s.up;
+  v->vp = s.vp;
+  v->u_rep = s.u_rep;
+  v->v_rep = s.v_rep;
+  v->u_out = s.u_out;
+  v->v_out = s.v_out;
+  v->val0 = s.val0;
+  v->smooth_p = s.smooth_p;
+  v->peak_i = s.peak_i;
+  v->peak_j = s.peak_j;
+  v->s2n = s.s2n;
+  return PIV_OK;
+}
+
+#define PIV_TRY(expr)            \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != PIV_OK) return _rc; \
+  } while (0)
+
+static int cuda_ok(cudaError_t e, const char* what) { return e == cudaSuccess ? PIV_OK : set_cuda_error(e, what); }
+
+__global__ void k_mask_frames(long long npix, int n_pairs, int pixel_bytes, const uint8_t* mask, void* a, void* b) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npix * n_pairs) return;
+  if (!mask[t % npix]) return;
+  uint8_t* pa = (uint8_t*)a + t * pixel_bytes;
+  uint8_t* pb = (uint8_t*)b + t * pixel_bytes;
+  for (int k = 0; k < pixel_bytes; ++k) { pa[k] = 0; pb[k] = 0; }
+}
+
+int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host, double* u,
+                 double* v, uint8_t* val_locations, uint8_t* outliers, int outputs_on_host, void* stream_ptr) {
+  if (!p || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (n_pairs <= 0 || n_pairs > p->cfg.max_pairs)
+    return set_error(PIV_E_ARG, "n_pairs %d outside [1, max_pairs=%d]", n_pairs, p->cfg.max_pairs);
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  const piv_config& cfg = p->cfg;
+  const int H = cfg.height, W = cfg.width;
+  const size_t hw = (size_t)H * W;
+  const size_t pb = pixel_bytes(cfg.pixel_type);
+  const int n_stage_ids = (int)p->st.size() * PIV_STAGES;
+  piv_plan::TimedRun* tr = nullptr;
+  if (p->timing) {
+    p->timed.emplace_back();
+    tr = &p->timed.back();
+    tr->start = take_event(p);
+    cudaEventRecord(tr->start, s);
+  }
+  auto mark = [&](int id) {
+    if (!tr) return;
+    cudaEvent_t e = take_event(p);
+    cudaEventRecord(e, s);
+    tr->ids.push_back(id);
+    tr->ev.push_back(e);
+  };
+  const void* fa = frames_a;
+  const void* fb = frames_b;
+  if (frames_on_host || p->frame_mask) {
+    const cudaMemcpyKind kind = frames_on_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    PIV_TRY(cuda_ok(cudaMemcpyAsync(p->stage_a, frames_a, n_pairs * hw * pb, kind, s), "frame copy"));
+    PIV_TRY(cuda_ok(cudaMemcpyAsync(p->stage_b, frames_b, n_pairs * hw * pb, kind, s), "frame copy"));
+    fa = p->stage_a;
+    fb = p->stage_b;
+    if (p->frame_mask) {
+      // mask_frames (gpu_process.py:682-688)
+      const long long tot = (long long)hw * n_pairs;
+      k_mask_frames<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>((long long)hw, n_pairs, (int)pb, p->frame_mask,
+                                                                    p->stage_a, p->stage_b);
+      PIV_TRY(cuda_ok(cudaGetLastError(), "k_mask_frames"));
+    }
+  }
+  mark(n_stage_ids);
+  bool coef_ready = false;
+  const int n_it = (int)p->st.size();
+  for (int k = 0; k < n_it; ++k) {
+    IterState& st = p->st[k];
+    const piv_iteration& it = st.it;
+    const int cnt = (int)(st.mn * n_pairs);
+    const void* ca = fa;
+    const void* cb = fb;
+    int c_pixel = cfg.pixel_type;
+    if (k > 0) {
+      IterState& pr = p->st[k - 1];
+      if (pr.g.search_size != st.g.search_size) {
+        PIV_TRY(regrid(pr.g, st.g, n_pairs, pr.u_out, pr.v_out, st.up, st.vp, s));
+      } else {
+        PIV_TRY(cuda_ok(cudaMemcpyAsync(st.up, pr.u_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
+        PIV_TRY(cuda_ok(cudaMemcpyAsync(st.vp, pr.v_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
+      }
+      mark(k * PIV_STAGES + 0);
+      if (it.deforming_order == 3 && !coef_ready) {
+        PIV_TRY(spline_prefilter(H, W, n_pairs, fa, cfg.pixel_type, p->coef, s));
+        PIV_TRY(spline_prefilter(H, W, n_pairs, fb, cfg.pixel_type, p->coef + (size_t)cfg.max_pairs * hw, s));
+        coef_ready = true;
+      }
+      DeformArgs d;
+      d.geom = st.g;
+      d.n_pairs = n_pairs;
+      d.frames_a = fa;
+      d.frames_b = fb;
+      d.pixel_type = cfg.pixel_type;
+      d.up = st.up;
+      d.vp = st.vp;
+      d.deforming_par = it.deforming_par;
+      d.order = it.deforming_order == 3 ? 3 : 1;
+      d.coef_a = p->coef;
+      d.coef_b = p->coef ? p->coef + (size_t)cfg.max_pairs * hw : nullptr;
+      d.frame_mask = p->frame_mask;
+      d.dtype = cfg.dtype;
+      d.out_a = p->def_a;
+      d.out_b = p->def_b;
+      PIV_TRY(deform(d, s));
+      mark(k * PIV_STAGES + 1);
+      ca = p->def_a;
+      cb = p->def_b;
+      c_pixel = cfg.dtype == PIV_DTYPE_F64 ? PIV_PIXEL_F64 : PIV_PIXEL_F32;
+    }
+    CorrArgs c{};
+    c.frame_a = ca;
+    c.frame_b = cb;
+    c.pixel_type = c_pixel;
+    c.height = H;
+    c.width = W;
+    c.ss = st.g.search_size;
+    c.ws = st.g.window_size;
+    c.spacing = st.g.spacing;
+    c.m = st.g.m;
+    c.n = st.g.n;
+    c.x_offset = st.g.x_offset;
+    c.y_offset = st.g.y_offset;
+    c.n_pairs = n_pairs;
+    c.fft_size = it.fft_size;
+    c.normalize = it.normalize;
+    c.subpixel = it.subpixel_method;
+    c.dtype = cfg.dtype;
+    c.win_mask = st.field_mask;
+    c.u = st.u_corr;
+    c.v = st.v_corr;
+    c.peak_i = st.peak_i;
+    c.peak_j = st.peak_j;
+    c.s2n = st.s2n;
+    c.s2n_method = it.s2n_method;
+    c.s2n_size = it.s2n_size;
+    c.scratch = p->corr_scratch;
+    c.scratch_bytes = p->corr_scratch_bytes;
+    c.maps = nullptr;
+    if (cfg.dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
+      PIV_TRY(correlate_tensor(c, s));
+    } else {
+      PIV_TRY(correlate_fft(c, s));
+    }
+    mark(k * PIV_STAGES + 2);
+    PIV_TRY(combine_fields(cnt, st.u_corr, st.v_corr, cfg.dtype, st.up, st.vp, st.fp32, st.u_rep, st.v_rep, s));
+    ValArgs va;
+    va.m = st.g.m;
+    va.n = st.g.n;
+    va.n_pairs = n_pairs;
+    va.u = st.u_rep;
+    va.v = st.v_rep;
+    va.s2n = st.s2n;
+    va.s2n_dtype = cfg.dtype;
+    va.size = it.validation_size;
+    va.s2n_tol = it.s2n_tol;
+    va.median_tol = it.median_tol;
+    va.mad_tol = it.mad_tol;
+    va.mean_tol = it.mean_tol;
+    va.rms_tol = it.rms_tol;
+    va.field_mask = st.field_mask;
+    va.exclude = nullptr;
+    va.fp32 = st.fp32;
+    PIV_TRY(validate(va, st.val0, p->rms_stats, s));
+    PIV_TRY(cuda_ok(cudaMemcpyAsync(st.val, st.val0, cnt, cudaMemcpyDeviceToDevice, s), "val copy"));
+    mark(k * PIV_STAGES + 3);
+    RepArgs ra;
+    ra.val = va;
+    ra.u = st.u_rep;
+    ra.v = st.v_rep;
+    ra.val_mask = st.val;
+    ra.n_iters = it.num_replacing_iters;
+    ra.method = it.replacing_method;
+    ra.size = it.replacing_size;
+    ra.revalidate = it.revalidate;
+    ra.dtype = cfg.dtype;
+    ra.scratch = p->rep_scratch;
+    ra.status = nullptr;
+    PIV_TRY(replace(ra, s));
+    if (k == n_it - 1) {
+      va.u = st.u_rep;
+      va.v = st.v_rep;
+      PIV_TRY(validate(va, p->outliers, p->rms_stats, s));
+    }
+    mark(k * PIV_STAGES + 4);
+    if (k != n_it - 1) {
+      PIV_TRY(smoothn(st.g.m, st.g.n, n_pairs, st.u_rep, st.v_rep, st.u_out, st.v_out, st.field_mask,
+                      it.smoothing_par, st.smooth_p, p->smooth_scratch, s));
+      mark(k * PIV_STAGES + 5);
+    }
+  }
+  IterState& last = p->st.back();
+  const int cnt = (int)(last.mn * n_pairs);
+  const double* ru = last.u_rep;
+  const double* rv = last.v_rep;
+  if (cfg.dt != 1 || cfg.scaling_par != 1) {
+    PIV_TRY(scale_fields(cnt, last.u_rep, last.v_rep, cfg.scaling_par, cfg.dt, last.fp32, p->u_final, p->v_final, s));
+    ru = p->u_final;
+    rv = p->v_final;
+  }
+  const cudaMemcpyKind ok = outputs_on_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  PIV_TRY(cuda_ok(cudaMemcpyAsync(u, ru, cnt * 8, ok, s), "result copy"));
+  PIV_TRY(cuda_ok(cudaMemcpyAsync(v, rv, cnt * 8, ok, s), "result copy"));
+  if (val_locations) PIV_TRY(cuda_ok(cudaMemcpyAsync(val_locations, last.val0, cnt, ok, s), "result copy"));
+  if (outliers) PIV_TRY(cuda_ok(cudaMemcpyAsync(outliers, p->outliers, cnt, ok, s), "result copy"));
+  mark(n_stage_ids + 1);
+  if (outputs_on_host) PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
+  return cuda_ok(cudaGetLastError(), "piv_plan_run");
+}
+
+int piv_plan_graph_capture(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, double* u,
+                           double* v, uint8_t* val_locations, uint8_t* outliers, int* kernel_nodes,
+                           void* stream_ptr) {
+  if (!p) return set_error(PIV_E_ARG, "NULL plan");
+  if (!stream_ptr) return set_error(PIV_E_ARG, "graph capture needs a non-default stream");
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  if (p->graph_exec) {
+    cudaGraphExecDestroy(p->graph_exec);
+    p->graph_exec = nullptr;
+  }
+  const bool saved = p->timing;
+  p->timing = false;
+  PIV_TRY(cuda_ok(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture"));
+  int rc = piv_plan_run(p, n_pairs, frames_a, frames_b, 0, u, v, val_locations, outliers, 0, stream_ptr);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  p->timing = saved;
+  if (rc != PIV_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_cuda_error(e, "cudaStreamEndCapture");
+  if (kernel_nodes) {
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(graph, nodes.data(), &n);
+    int k = 0;
+    for (size_t i = 0; i < n; ++i) {
+      cudaGraphNodeType t;
+      cudaGraphNodeGetType(nodes[i], &t);
+      if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    *kernel_nodes = k;
+  }
+  e = cudaGraphInstantiate(&p->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  return cuda_ok(e, "cudaGraphInstantiate");
+}
+
+int piv_plan_graph_launch(piv_plan* p, void* stream) {
+  if (!p || !p->graph_exec) return set_error(PIV_E_ARG, "no captured graph");
+  return cuda_ok(cudaGraphLaunch(p->graph_exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+// ---------------------------------------------------------------------------
+// Stage entry points.
+// ---------------------------------------------------------------------------
+int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, const void* frames_b, int pixel_type,
+                  int dtype, int fft_size, int normalize, int subpixel_method, const uint8_t* win_mask, void* u,
+                  void* v, int* peak_i, int* peak_j, int s2n_method, int s2n_size, void* s2n, int dft_mode,
+                  void* stream) {
+  if (!g || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (!is_pow2(fft_size) || fft_size < g->search_size || fft_size > 256)
+    return set_error(PIV_E_UNSUPPORTED, "fft_size %d is not supported", fft_size);
+  CorrArgs c{};
+  c.frame_a = frames_a;
+  c.frame_b = frames_b;
+  c.pixel_type = pixel_type;
+  c.height = g->height;
+  c.width = g->width;
+  c.ss = g->search_size;
+  c.ws = g->window_size;
+  c.spacing = g->spacing;
+  c.m = g->m;
+  c.n = g->n;
+  c.x_offset = g->x_offset;
+  c.y_offset = g->y_offset;
+  c.n_pairs = n_pairs;
+  c.fft_size = fft_size;
+  c.normalize = normalize;
+  c.subpixel = subpixel_method;
+  c.dtype = dtype;
+  c.win_mask = win_mask;
+  c.u = u;
+  c.v = v;
+  c.peak_i = peak_i;
+  c.peak_j = peak_j;
+  c.s2n = s2n;
+  c.s2n_method = s2n_method;
+  c.s2n_size = s2n_size;
+  c.scratch = nullptr;
+  c.scratch_bytes = 0;
+  c.maps = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t need = correlate_fft_scratch_bytes(fft_size, dtype);
+  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) return correlate_tensor(c, s);
+  if (need) {
+    PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
+    c.scratch_bytes = need;
+  }
+  int rc = correlate_fft(c, s);
+  if (c.scratch) cudaFreeAsync(c.scratch, s);
+  return rc;
+}
+
+int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a, const void* frames_b,
+                       int pixel_type, int dtype, int fft_size, int normalize, const uint8_t* win_mask, void* maps,
+                       void* stream) {
+  if (!g || !frames_a || !frames_b || !maps) return set_error(PIV_E_ARG, "NULL argument");
+  if (!is_pow2(fft_size) || fft_size < g->search_size || fft_size > 256)
+    return set_error(PIV_E_UNSUPPORTED, "fft_size %d is not supported", fft_size);
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t cnt = (size_t)n_pairs * g->m * g->n;
+  const size_t tsz = dtype == PIV_DTYPE_F64 ? 8 : 4;
+  void* u = nullptr;
+  PIV_TRY(cuda_ok(cudaMallocAsync(&u, 2 * cnt * tsz, s), "cudaMallocAsync"));
+  CorrArgs c{};
+  c.frame_a = frames_a;
+  c.frame_b = frames_b;
+  c.pixel_type = pixel_type;
+  c.height = g->height;
+  c.width = g->width;
+  c.ss = g->search_size;
+  c.ws = g->window_size;
+  c.spacing = g->spacing;
+  c.m = g->m;
+  c.n = g->n;
+  c.x_offset = g->x_offset;
+  c.y_offset = g->y_offset;
+  c.n_pairs = n_pairs;
+  c.fft_size = fft_size;
+  c.normalize = normalize;
+  c.subpixel = PIV_SUBPIXEL_GAUSSIAN;
+  c.dtype = dtype;
+  c.win_mask = win_mask;
+  c.u = u;
+  c.v = (char*)u + cnt * tsz;
+  c.maps = maps;
+  const size_t need = correlate_fft_scratch_bytes(fft_size, dtype);
+  if (need) {
+    PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
+    c.scratch_bytes = need;
+  }
+  int rc = correlate_fft(c, s);
+  if (c.scratch) cudaFreeAsync(c.scratch, s);
+  cudaFreeAsync(u, s);
+  return rc;
+}
+
+int piv_regrid(const piv_geometry* src, const piv_geometry* dst, int n_pairs, const double* u_src,
+               const double* v_src, double* u_dst, double* v_dst, void* stream) {
+  if (!src || !dst || !u_src || !v_src || !u_dst || !v_dst) return set_error(PIV_E_ARG, "NULL argument");
+  return regrid(*src, *dst, n_pairs, u_src, v_src, u_dst, v_dst, (cudaStream_t)stream);
+}
+
+int piv_deform(const piv_geometry* g, int n_pairs, const void* frames_a, const void* frames_b, int pixel_type,
+               const double* up, const double* vp, double deforming_par, int deforming_order, const float* coef_a,
+               const float* coef_b, const uint8_t* frame_mask, int dtype, void* out_a, void* out_b, void* stream) {
+  if (!g || !frames_a || !frames_b || !up || !vp || !out_a || !out_b) return set_error(PIV_E_ARG, "NULL argument");
+  DeformArgs d;
+  d.geom = *g;
+  d.n_pairs = n_pairs;
+  d.frames_a = frames_a;
+  d.frames_b = frames_b;
+  d.pixel_type = pixel_type;
+  d.up = up;
+  d.vp = vp;
+  d.deforming_par = deforming_par;
+  d.order = deforming_order == 3 ? 3 : 1;
+  d.coef_a = coef_a;
+  d.coef_b = coef_b;
+  d.frame_mask = frame_mask;
+  d.dtype = dtype;
+  d.out_a = out_a;
+  d.out_b = out_b;
+  return deform(d, (cudaStream_t)stream);
+}
+
+int piv_spline_prefilter(int height, int width, int n_frames, const void* frames, int pixel_type, float* coef,
+                         void* stream) {
+  if (!frames || !coef) return set_error(PIV_E_ARG, "NULL argument");
+  return spline_prefilter(height, width, n_frames, frames, pixel_type, coef, (cudaStream_t)stream);
+}
+
+int piv_validate(int m, int n, int n_pairs, const double* u, const double* v, const void* s2n, int s2n_dtype,
+                 int size, double s2n_tol, double median_tol, double mad_tol, double mean_tol, double rms_tol,
+                 const uint8_t* field_mask, const uint8_t* exclude, int fp32, uint8_t* val, void* stream) {
+  if (!u || !v || !val) return set_error(PIV_E_ARG, "NULL argument");
+  ValArgs a{m, n, n_pairs, u, v, s2n, s2n_dtype, size, s2n_tol, median_tol, mad_tol, mean_tol, rms_tol,
+            field_mask, exclude, fp32};
+  cudaStream_t s = (cudaStream_t)stream;
+  double* stats = nullptr;
+  if (!isnan(rms_tol)) PIV_TRY(cuda_ok(cudaMallocAsync((void**)&stats, 4 * 8 * (size_t)n_pairs, s), "cudaMallocAsync"));
+  int rc = validate(a, val, stats, s);
+  if (stats) cudaFreeAsync(stats, s);
+  return rc;
+}
+
+int piv_replace(int m, int n, int n_pairs, double* u, double* v, uint8_t* val, const uint8_t* field_mask, int n_iters,
+                int method, int size, int revalidate, const void* s2n, int s2n_dtype, int val_size, double s2n_tol,
+                double median_tol, double mad_tol, double mean_tol, double rms_tol, int fp32, int dtype,
+                void* stream) {
+  if (!u || !v || !val) return set_error(PIV_E_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  RepArgs a;
+  a.val = ValArgs{m, n, n_pairs, u, v, s2n, s2n_dtype, val_size, s2n_tol, median_tol, mad_tol, mean_tol, rms_tol,
+                  field_mask, nullptr, fp32};
+  a.u = u;
+  a.v = v;
+  a.val_mask = val;
+  a.n_iters = n_iters;
+  a.method = method;
+  a.size = size;
+  a.revalidate = revalidate;
+  a.dtype = dtype;
+  a.status = nullptr;
+  const size_t need = replace_scratch_bytes(m, n, n_pairs);
+  PIV_TRY(cuda_ok(cudaMallocAsync(&a.scratch, need, s), "cudaMallocAsync"));
+  int rc = replace(a, s);
+  cudaFreeAsync(a.scratch, s);
+  return rc;
+}
+
+int piv_smoothn(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double sp, double* p_out,
+                void* stream) {
+  if (!u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  PIV_TRY(cuda_ok(cudaMallocAsync(&scratch, smoothn_scratch_bytes(m, n, n_pairs), s), "cudaMallocAsync"));
+  int rc = smoothn(m, n, n_pairs, u, v, u, v, field_mask, sp, p_out, scratch, s);
+  cudaFreeAsync(scratch, s);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// Shared types and helpers for the PIV kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/piv_gb300.h"
+
+#define PIV_HD __host__ __device__ __forceinline__
+#define PIV_D __device__ __forceinline__
+
+namespace piv {
+
+template <typename T> struct Cplx;
+template <> struct __align__(8) Cplx<float> { float x, y; };
+template <> struct __align__(16) Cplx<double> { double x, y; };
+
+template <typename T> PIV_D Cplx<T> cmake(T a, T b) { Cplx<T> r; r.x = a; r.y = b; return r; }
+template <typename T> PIV_D Cplx<T> cadd(Cplx<T> a, Cplx<T> b) { return cmake<T>(a.x + b.x, a.y + b.y); }
+template <typename T> PIV_D Cplx<T> csub(Cplx<T> a, Cplx<T> b) { return cmake<T>(a.x - b.x, a.y - b.y); }
+template <typename T> PIV_D Cplx<T> cmul(Cplx<T> a, Cplx<T> b) {
+  return cmake<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename T> PIV_D Cplx<T> cmulconj(Cplx<T> a, Cplx<T> b) {
+  return cmake<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename T> PIV_D Cplx<T> cconj(Cplx<T> a) { return cmake<T>(a.x, -a.y); }
+
+// Round-to-nearest arithmetic without FMA contraction, used where the host
+// oracle evaluates an expression as separate IEEE operations.
+PIV_D float add_rn(float a, float b) { return __fadd_rn(a, b); }
+PIV_D float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+PIV_D float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+PIV_D float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+PIV_D double add_rn(double a, double b) { return __dadd_rn(a, b); }
+PIV_D double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+PIV_D double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+PIV_D double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+PIV_D bool is_nan(float v) { return isnan(v); }
+PIV_D bool is_nan(double v) { return isnan(v); }
+
+// Loads pixel `idx` of a frame of the given pixel type as T.
+template <typename T> PIV_D T load_pixel(const void* base, int pixel_type, long long idx) {
+  switch (pixel_type) {
+    case PIV_PIXEL_U8: return (T)__ldg(((const uint8_t*)base) + idx);
+    case PIV_PIXEL_U16: return (T)__ldg(((const uint16_t*)base) + idx);
+    case PIV_PIXEL_F32: return (T)__ldg(((const float*)base) + idx);
+    default: return (T)__ldg(((const double*)base) + idx);
+  }
+}
+
+PIV_HD int div_up(int a, int b) { return (a + b - 1) / b; }
+
+// Number of SMs of the current device (cached per process).
+int sm_count();
+
+}  // namespace piv

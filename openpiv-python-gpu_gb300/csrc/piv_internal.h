@@ -1,0 +1,111 @@
+// Internal interfaces between the kernel files and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/piv_gb300.h"
+
+namespace piv {
+
+// Records an error message for piv_last_error() and returns `code`.
+int set_error(int code, const char* fmt, ...);
+int set_cuda_error(cudaError_t e, const char* what);
+
+// Arguments of one correlation pass over n_pairs frame pairs.
+struct CorrArgs {
+  const void* frame_a;
+  const void* frame_b;
+  int pixel_type;
+  int height, width;
+  int ss, ws, spacing, m, n, x_offset, y_offset;
+  int n_pairs;
+  int fft_size;
+  int normalize;
+  int subpixel;
+  int dtype;
+  const uint8_t* win_mask;
+  void* u;
+  void* v;
+  int* peak_i;
+  int* peak_j;
+  void* s2n;
+  int s2n_method;
+  int s2n_size;
+  void* scratch;        // device scratch for transforms that do not fit in shared memory
+  size_t scratch_bytes;
+  void* maps;           // optional [windows][N][N] output of the shifted correlation maps
+};
+
+int correlate_fft(const CorrArgs& a, cudaStream_t stream);
+size_t correlate_fft_scratch_bytes(int fft_size, int dtype);
+int correlate_tensor(const CorrArgs& a, cudaStream_t stream);
+bool correlate_tensor_supported(const CorrArgs& a);
+
+// Deformation.
+struct DeformArgs {
+  piv_geometry geom;
+  int n_pairs;
+  const void* frames_a;
+  const void* frames_b;
+  int pixel_type;
+  const double* up;
+  const double* vp;
+  double deforming_par;
+  int order;
+  const float* coef_a;
+  const float* coef_b;
+  const uint8_t* frame_mask;
+  int dtype;
+  void* out_a;
+  void* out_b;
+};
+int deform(const DeformArgs& a, cudaStream_t stream);
+int regrid(const piv_geometry& src, const piv_geometry& dst, int n_pairs, const double* u_src, const double* v_src,
+           double* u_dst, double* v_dst, cudaStream_t stream);
+int spline_prefilter(int height, int width, int n_frames, const void* frames, int pixel_type, float* coef,
+                     cudaStream_t stream);
+
+// Validation and replacement.
+struct ValArgs {
+  int m, n, n_pairs;
+  const double* u;
+  const double* v;
+  const void* s2n;
+  int s2n_dtype;
+  int size;
+  double s2n_tol, median_tol, mad_tol, mean_tol, rms_tol;
+  const uint8_t* field_mask;  // [m][n] or NULL
+  const uint8_t* exclude;     // [pairs][m][n] or NULL
+  int fp32;
+};
+int validate(const ValArgs& a, uint8_t* val, double* rms_stats, cudaStream_t stream);
+
+struct RepArgs {
+  ValArgs val;                // revalidation settings (u/v/exclude ignored)
+  double* u;
+  double* v;
+  uint8_t* val_mask;
+  int n_iters, method, size, revalidate;
+  int dtype;                  // dtype_f of the pipeline (float32 coefficient rounding)
+  void* scratch;              // replace_scratch_bytes(m, n, n_pairs)
+  int* status;                // device word set to PIV_E_TIMEOUT when a solve hits its cap; may be NULL
+};
+size_t replace_scratch_bytes(int m, int n, int n_pairs);
+int replace(const RepArgs& a, cudaStream_t stream);
+
+// Field combination before validation: u = u_corr (+ up), in float32 when fp32.
+int combine_fields(int count, const void* u_corr, const void* v_corr, int corr_dtype, const double* up,
+                   const double* vp, int fp32, double* u, double* v, cudaStream_t stream);
+
+// smoothn.
+size_t smoothn_scratch_bytes(int m, int n, int n_pairs);
+int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out, double* v_out,
+            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream);
+
+// Final scaling u * scaling_par / dt (gpu_process.py:847-849).
+int scale_fields(int count, const double* u, const double* v, double scaling, double dt, int fp32, double* uo,
+                 double* vo, cudaStream_t stream);
+
+}  // namespace piv

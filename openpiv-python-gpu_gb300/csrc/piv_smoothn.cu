@@ -1,0 +1,300 @@
+// smoothn for the two displacement fields of each pair, as PIVGPU uses it
+// (SmoothnGPU(f_shape, mask, s)(u, v), gpu_smoothn.py:123-231: non-robust,
+// order 2, equal weights): z = IDCT2(gamma * DCT2(f)), gamma = 1/(1 + s lambda^2),
+// lambda = 2 (2 - cos(pi i/m) - cos(pi j/n)) (gpu_smoothn.py:340-351), one s
+// shared by u and v. With s unset, p = log10(s) minimises the GCV score
+// (gpu_smoothn.py:353-372) over [p_min, p_max] (gpu_smoothn.py:320-338): a
+// 10-point scan (gpu_smoothn.py:182-188) followed by a bounded local search
+// from the best scan point that keeps the scan point when its projected
+// finite-difference gradient is below 1e-5 (the stopping test of the
+// reference's L-BFGS-B call, gpu_smoothn.py:191-193).
+//
+// The orthonormal DCT-II/III pairs are float64 matrix products with cosine
+// matrices built on the device; the GCV search runs in one CTA per pair.
+#include <math.h>
+
+#include "piv_common.cuh"
+#include "piv_internal.h"
+
+namespace piv {
+
+struct SmoothScratch {
+  double* fd;    // [pairs][2][mn] DCT coefficients of u and v
+  double* tmp;   // [pairs][2][mn]
+  double* f2;    // [pairs][mn] fd_u^2 + fd_v^2
+  double* cm;    // [m][m]
+  double* cn;    // [n][n]
+  double* lam2;  // [mn]
+  double* p;     // [pairs]
+};
+
+static size_t align_up(size_t v) { return (v + 255) / 256 * 256; }
+
+size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
+  const size_t mn = (size_t)m * n;
+  return align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + align_up((size_t)m * m * 8) +
+         align_up((size_t)n * n * 8) + align_up(mn * 8) + align_up((size_t)n_pairs * 8);
+}
+
+static SmoothScratch carve(void* base, int m, int n, int n_pairs) {
+  const size_t mn = (size_t)m * n;
+  char* p = (char*)base;
+  SmoothScratch s;
+  s.fd = (double*)p; p += align_up(2 * mn * n_pairs * 8);
+  s.tmp = (double*)p; p += align_up(2 * mn * n_pairs * 8);
+  s.f2 = (double*)p; p += align_up(mn * n_pairs * 8);
+  s.cm = (double*)p; p += align_up((size_t)m * m * 8);
+  s.cn = (double*)p; p += align_up((size_t)n * n * 8);
+  s.lam2 = (double*)p; p += align_up(mn * 8);
+  s.p = (double*)p;
+  return s;
+}
+
+// Orthonormal DCT-II matrix C[k][i] = s_k cos(pi (2i+1) k / (2 len)).
+__global__ void k_dct_matrix(int len, double* c) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len * len) return;
+  const int k = t / len, i = t % len;
+  const double sk = k == 0 ? sqrt(1.0 / len) : sqrt(2.0 / len);
+  c[t] = sk * cospi((double)((2 * i + 1) * k) / (2.0 * len));
+}
+
+// lambda^2 with lambda = 2 (2 - (cos(pi i/m) + cos(pi j/n))).
+__global__ void k_lambda2(int m, int n, double* lam2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m * n) return;
+  const int i = t / n, j = t % n;
+  const double l = 2.0 * (2.0 - (cos(M_PI * i / m) + cos(M_PI * j / n)));
+  lam2[t] = l * l;
+}
+
+// out[b][i][l] = sum_j in[b][i][j] * c[l][j]       (transform along rows, mode 0)
+// out[b][i][l] = sum_j in[b][i][j] * c[j][l]       (inverse along rows, mode 1)
+// out[b][k][j] = sum_i c[k][i] * in[b][i][j]       (transform along columns, mode 2)
+// out[b][k][j] = sum_i c[i][k] * in[b][i][j]       (inverse along columns, mode 3)
+__global__ void k_dct_apply(int m, int n, int batch, int mode, const double* __restrict__ c,
+                            const double* __restrict__ in, double* __restrict__ out) {
+  const long long mn = (long long)m * n;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= mn * batch) return;
+  const int b = (int)(t / mn);
+  const int e = (int)(t % mn);
+  const int r = e / n, col = e % n;
+  const double* x = in + b * mn;
+  double acc = 0.0;
+  if (mode == 0) {
+    for (int j = 0; j < n; ++j) acc = fma(x[r * n + j], c[col * n + j], acc);
+  } else if (mode == 1) {
+    for (int j = 0; j < n; ++j) acc = fma(x[r * n + j], c[j * n + col], acc);
+  } else if (mode == 2) {
+    for (int i = 0; i < m; ++i) acc = fma(c[r * m + i], x[i * n + col], acc);
+  } else {
+    for (int i = 0; i < m; ++i) acc = fma(c[i * m + r], x[i * n + col], acc);
+  }
+  out[t] = acc;
+}
+
+__global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, double* __restrict__ f2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= mn * n_pairs) return;
+  const long long pair = t / mn, e = t % mn;
+  const double a = fd[(2 * pair) * mn + e], b = fd[(2 * pair + 1) * mn + e];
+  f2[t] = a * a + b * b;
+}
+
+static constexpr int kGcvThreads = 512;
+
+struct GcvEval {
+  const double* f2;
+  const double* lam2;
+  long long mn;
+  double n_finite;
+  int n_fields;
+};
+
+// GCV score at p (gpu_smoothn.py:353-372, w_mean > 0.9 branch). All threads call.
+PIV_D double gcv_score(const GcvEval& g, double p, double* red) {
+  const double s = pow(10.0, p);
+  double rss = 0.0, tr = 0.0;
+  for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
+    const double gm = 1.0 / (1.0 + s * g.lam2[e]);
+    const double d = gm - 1.0;
+    rss += g.f2[e] * d * d;
+    tr += gm;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rss += __shfl_xor_sync(~0u, rss, o);
+    tr += __shfl_xor_sync(~0u, tr, o);
+  }
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { red[w] = rss; red[32 + w] = tr; }
+  __syncthreads();
+  double trss = 0.0, ttr = 0.0;
+  for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
+  const double q = 1.0 - ttr / (double)g.mn;
+  return trss / g.n_finite / (q * q) / g.n_fields;
+}
+
+// Finite-difference gradient as the reference's L-BFGS-B call computes it
+// (absolute step 1e-8, backward at the upper bound).
+PIV_D double gcv_grad(const GcvEval& g, double p, double f0, double pmax, double* red) {
+  const double h = 1e-8;
+  if (p + h <= pmax) return (gcv_score(g, p + h, red) - f0) / h;
+  return (f0 - gcv_score(g, p - h, red)) / h;
+}
+
+__global__ void __launch_bounds__(kGcvThreads)
+k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2, double pmin,
+      double pmax, double* __restrict__ p_out) {
+  __shared__ double red[64];
+  const int pair = blockIdx.x;
+  const long long mn = (long long)m * n;
+  GcvEval g{f2 + pair * mn, lam2, mn, (double)mn, 2};
+  // 10-point scan.
+  double best_p = pmin, best_f = INFINITY;
+  for (int k = 0; k < 10; ++k) {
+    const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
+    const double fk = gcv_score(g, pk, red);
+    if (fk < best_f || (k == 0)) {
+      if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
+    }
+  }
+  double p = best_p;
+  const double f0 = best_f;
+  const double g0 = gcv_grad(g, p, f0, pmax, red);
+  const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
+  if (!(fabs(pg) <= 1e-5)) {
+    // Brent's bounded minimisation on the bracket around the scan point.
+    const double step = (pmax - pmin) / 9.0;
+    double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
+    const double cg = 0.3819660112501051;
+    double x = p, w = p, v = p, fx = f0, fw = f0, fv = f0, d = 0.0, e = 0.0;
+    for (int it = 0; it < 200; ++it) {
+      const double xm = 0.5 * (a + b);
+      const double tol1 = 1e-11 * fabs(x) + 1e-13, tol2 = 2.0 * tol1;
+      if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
+      bool golden = true;
+      if (fabs(e) > tol1) {
+        double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
+        q = 2.0 * (q - r);
+        if (q > 0) pp = -pp;
+        q = fabs(q);
+        const double etemp = e;
+        e = d;
+        if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
+          d = pp / q;
+          const double u = x + d;
+          if (u - a < tol2 || b - u < tol2) d = xm >= x ? tol1 : -tol1;
+          golden = false;
+        }
+      }
+      if (golden) {
+        e = (x >= xm) ? a - x : b - x;
+        d = cg * e;
+      }
+      const double u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
+      const double fu = gcv_score(g, u, red);
+      if (fu <= fx) {
+        if (u >= x) a = x; else b = x;
+        v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
+      } else {
+        if (u < x) a = u; else b = u;
+        if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
+        else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+      }
+    }
+    p = x;
+    // A minimum within the tolerance of a bound sits on the bound (a projected method lands there).
+    if (p - pmin < 1e-9) p = pmin;
+    if (pmax - p < 1e-9) p = pmax;
+  }
+  if (threadIdx.x == 0) p_out[pair] = p;
+}
+
+// fd *= gamma(p) for both fields of each pair.
+__global__ void k_apply_gamma(long long mn, int n_pairs, const double* __restrict__ lam2,
+                              const double* __restrict__ p, double fixed_p, double* __restrict__ fd) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * mn * n_pairs) return;
+  const long long pair = t / (2 * mn), e = t % mn;
+  const double pp = p ? p[pair] : fixed_p;
+  const double s = pow(10.0, pp);
+  fd[t] = (1.0 / (1.0 + s * lam2[e])) * fd[t];
+}
+
+__global__ void k_fill(int count, double value, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) out[t] = value;
+}
+
+static int check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, what);
+}
+
+int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out, double* v_out,
+            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream) {
+  const long long mn = (long long)m * n;
+  if (n_pairs == 0 || mn == 0) return PIV_OK;
+  if (field_mask) return set_error(PIV_E_UNSUPPORTED, "smoothn with a field mask (weighted smoothing) is not implemented");
+  if (mn < 2) {
+    cudaMemcpyAsync(u_out, u_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
+    cudaMemcpyAsync(v_out, v_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
+    return check("smoothn copy");
+  }
+  SmoothScratch sc = carve(scratch, m, n, n_pairs);
+  const int bs = 256;
+  k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, sc.cm);
+  k_dct_matrix<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n, sc.cn);
+  k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, sc.lam2);
+  // Gather u and v as [pair][field][mn] into tmp.
+  for (int f = 0; f < 2; ++f) {
+    cudaMemcpy2DAsync(sc.tmp + f * mn, 2 * mn * 8, f == 0 ? u_in : v_in, mn * 8, mn * 8, n_pairs,
+                      cudaMemcpyDeviceToDevice, stream);
+  }
+  const long long tot = 2 * mn * n_pairs;
+  const unsigned grid = (unsigned)((tot + bs - 1) / bs);
+  // Forward DCT-II: rows then columns.
+  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 0, sc.cn, sc.tmp, sc.fd);
+  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 2, sc.cm, sc.fd, sc.tmp);
+  int rc = check("smoothn forward dct");
+  if (rc) return rc;
+  // tmp now holds the DCT coefficients.
+  double* pvec = nullptr;
+  double fixed_p = 0.0;
+  const bool gcv = !(s > 0);
+  if (gcv) {
+    // p bounds for order 2 (gpu_smoothn.py:320-338), on the host.
+    const double h_min = 1e-3, h_max = 1.0 - h_min;
+    const int rank = (m != 1) + (n != 1);
+    const double a_max = pow(h_max, 2.0 / rank), a_min = pow(h_min, 2.0 / rank);
+    const double pmin = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_max)) / 4.0 / a_max, 2.0) - 1.0) / 16.0);
+    const double pmax = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_min)) / 4.0 / a_min, 2.0) - 1.0) / 16.0);
+    k_f2<<<(unsigned)((mn * n_pairs + bs - 1) / bs), bs, 0, stream>>>(mn, n_pairs, sc.tmp, sc.f2);
+    k_gcv<<<n_pairs, kGcvThreads, 0, stream>>>(m, n, n_pairs, sc.f2, sc.lam2, pmin, pmax, sc.p);
+    pvec = sc.p;
+    rc = check("k_gcv");
+    if (rc) return rc;
+  } else {
+    fixed_p = log10(s);
+  }
+  k_apply_gamma<<<grid, bs, 0, stream>>>(mn, n_pairs, sc.lam2, pvec, fixed_p, sc.tmp);
+  // Inverse DCT (DCT-III): rows then columns.
+  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 1, sc.cn, sc.tmp, sc.fd);
+  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 3, sc.cm, sc.fd, sc.tmp);
+  for (int f = 0; f < 2; ++f) {
+    cudaMemcpy2DAsync(f == 0 ? u_out : v_out, mn * 8, sc.tmp + f * mn, 2 * mn * 8, mn * 8, n_pairs,
+                      cudaMemcpyDeviceToDevice, stream);
+  }
+  if (p_out) {
+    if (gcv) {
+      cudaMemcpyAsync(p_out, sc.p, n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
+    } else {
+      k_fill<<<(n_pairs + 127) / 128, 128, 0, stream>>>(n_pairs, fixed_p, p_out);
+    }
+  }
+  return check("smoothn");
+}
+
+}  // namespace piv

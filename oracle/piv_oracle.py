@@ -247,6 +247,25 @@ def peak_gap(corr, i_peak, j_peak):
     return (top2[:, 0] - top2[:, 1]) / denom
 
 
+def fragile_windows(corr, i_peak, j_peak, method, search_size, tie_tol=1e-5):
+    """Windows whose integer peak or subpixel fit depends on floating-point
+    rounding noise: a near tie between the two largest map values, or (for the
+    Gaussian fit, which requires all five stencil values > 0) a stencil value
+    on a lag without window overlap (|lag| >= search size), whose exact value
+    is zero and whose computed value is rounding noise of either sign."""
+    n, N, _ = corr.shape
+    frag = peak_gap(corr, i_peak, j_peak) < tie_tol
+    if method == "gaussian":
+        lo = N // 2 - search_size  # shifted index of lag -ss
+        hi = N // 2 + search_size  # shifted index of lag +ss
+        for di, dj in ((0, 0), (-1, 0), (1, 0), (0, -1), (0, 1)):
+            ii, jj = i_peak + di, j_peak + dj
+            frag |= (ii <= lo) | (ii >= hi) | (jj <= lo) | (jj >= hi)
+        inside = (i_peak > 0) & (i_peak < N - 1) & (j_peak > 0) & (j_peak < N - 1)
+        frag &= inside | (peak_gap(corr, i_peak, j_peak) < tie_tol)
+    return frag
+
+
 def subpixel(corr, i_peak, j_peak, method, dtype_f):
     """Subpixel peak position (gpu_process.py:1256-1294)."""
     n, N, _ = corr.shape
@@ -704,6 +723,7 @@ class OraclePIV:
             i_sp, j_sp = subpixel(corr, i1, j1, it["subpixel_method"], ft)
             tr["i_peak"], tr["j_peak"] = i1, j1
             tr["peak_gap"] = peak_gap(corr, i1, j1)
+            tr["fragile"] = fragile_windows(corr, i1, j1, it["subpixel_method"], fld.search_size)
             uc_flat = j_sp - N // 2
             vc_flat = i_sp - N // 2
             if sel is not None:

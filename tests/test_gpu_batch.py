@@ -1,0 +1,65 @@
+"""A batch of pairs in one plan run gives each pair's single-pair result, and
+the CUDA-graph replay of a run gives the same fields as the direct run."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_equals_single_pairs():
+    import torch
+
+    from openpiv_gpu import _build, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    _build.build()
+    torch.cuda.set_device(0)
+    pairs = [synthetic.config_case(2, k, shape=(256, 256))[:2] for k in range(3)]
+    kw = dict(synthetic.CONFIGS[2]["piv"])
+    mss = kw.pop("min_search_size")
+    fa = np.stack([p[0] for p in pairs])
+    fb = np.stack([p[1] for p in pairs])
+    proc = PIVGPU((256, 256), mss, **kw)
+    ub, vb = proc.run_batch(fa, fb)
+    for k in range(3):
+        single = PIVGPU((256, 256), mss, **kw)
+        u, v = single(pairs[k][0], pairs[k][1])
+        np.testing.assert_array_equal(ub[k].cpu().numpy(), u.cpu().numpy())
+        np.testing.assert_array_equal(vb[k].cpu().numpy(), v.cpu().numpy())
+
+
+def test_graph_replay_equals_direct_run():
+    import torch
+
+    from openpiv_gpu import _build, _lib, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    _build.build()
+    lib = _lib.load()
+    pairs = [synthetic.config_case(2, k, shape=(256, 256))[:2] for k in range(2)]
+    kw = dict(synthetic.CONFIGS[2]["piv"])
+    mss = kw.pop("min_search_size")
+    fa = torch.as_tensor(np.stack([p[0] for p in pairs])).cuda()
+    fb = torch.as_tensor(np.stack([p[1] for p in pairs])).cuda()
+    proc = PIVGPU((256, 256), mss, **kw)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ud, vd = proc.run_batch(fa, fb)
+    s.synchronize()
+    plan = proc.plan_handle(fa, 2)
+    m, n = proc.piv_fields[-1].field_shape
+    u = torch.zeros((2, m, n), dtype=torch.float64, device="cuda")
+    v = torch.zeros_like(u)
+    val = torch.zeros((2, m, n), dtype=torch.uint8, device="cuda")
+    out = torch.zeros_like(val)
+    nk = ctypes.c_int(0)
+    _lib.check(lib.piv_plan_graph_capture(plan, 2, fa.data_ptr(), fb.data_ptr(), u.data_ptr(), v.data_ptr(),
+                                          val.data_ptr(), out.data_ptr(), ctypes.byref(nk), s.cuda_stream))
+    assert nk.value > 10
+    _lib.check(lib.piv_plan_graph_launch(plan, s.cuda_stream))
+    s.synchronize()
+    np.testing.assert_array_equal(u.cpu().numpy(), ud.cpu().numpy())
+    np.testing.assert_array_equal(v.cpu().numpy(), vd.cpu().numpy())
