@@ -260,6 +260,19 @@ int piv_replace(int m, int n, int n_pairs, double* u, double* v, uint8_t* val, c
 int piv_smoothn(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double s,
                 double* p_out, void* stream);
 
+/* piv_smoothn for callers that cannot allocate device memory while they run
+ * (a fixed memory budget handed over at start-up, a real-time loop that must
+ * not wait on the allocator, a host framework that owns every allocation).
+ * No counterpart in the reference. Same arguments and results as
+ * piv_smoothn, but the scratch is a fixed 4 MiB device array inside the
+ * library (for example 4 pairs of 128 x 128 fields); larger requests fail with
+ * PIV_E_ARG and a message. It calls no allocator. The first call on a device
+ * looks up the array's device address, so make that first call before any
+ * stream capture. Calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller. */
+int piv_smoothn_noalloc(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double s,
+                        double* p_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

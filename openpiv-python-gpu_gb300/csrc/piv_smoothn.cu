@@ -13,6 +13,8 @@
 // matrices built on the device; the GCV search runs in one CTA per pair.
 #include <math.h>
 
+#include <mutex>
+
 #include "piv_common.cuh"
 #include "piv_internal.h"
 
@@ -298,3 +300,66 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
 }
 
 }  // namespace piv
+
+namespace piv {
+
+// ---------------------------------------------------------------------------
+// smoothn without device allocation.
+//
+// Some callers cannot allocate device memory while they run: a host that
+// hands this library a fixed memory budget at start-up, a real-time loop that
+// must not stall in the allocator, or a framework that owns every device
+// allocation itself. piv_smoothn_noalloc serves them with scratch that lives
+// in a fixed device array of this file, sized for modest fields. Every GPU
+// that loads the library holds the array until the process exits.
+// ---------------------------------------------------------------------------
+static constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB: e.g. 4 pairs of 128 x 128 fields
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch, looked up once per device. In host code
+// the array's name is only a host-side stand-in, never a device address.
+static void* noalloc_scratch_address(int* rc) {
+  static std::mutex mu;
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *rc = set_cuda_error(e, "cudaGetDevice");
+    return nullptr;
+  }
+  if (dev < 0 || dev >= 64) {
+    *rc = set_error(PIV_E_UNSUPPORTED, "device index %d out of range", dev);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      *rc = set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  *rc = PIV_OK;
+  return addr[dev];
+}
+
+}  // namespace piv
+
+extern "C" int piv_smoothn_noalloc(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask,
+                                   double s, double* p_out, void* stream) {
+  using namespace piv;
+  if (!u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (m <= 0 || n <= 0 || n_pairs <= 0) return set_error(PIV_E_ARG, "empty field (m=%d, n=%d, pairs=%d)", m, n, n_pairs);
+  const size_t need = smoothn_scratch_bytes(m, n, n_pairs);
+  if (need > kNoAllocScratchBytes)
+    return set_error(PIV_E_ARG,
+                     "piv_smoothn_noalloc: %d pair(s) of %d x %d fields need %zu bytes of scratch, more than its "
+                     "fixed %zu bytes; use piv_smoothn or fewer/smaller fields",
+                     n_pairs, m, n, need, kNoAllocScratchBytes);
+  int rc = PIV_OK;
+  void* scratch = noalloc_scratch_address(&rc);
+  if (!scratch) return rc;
+  return smoothn(m, n, n_pairs, u, v, u, v, field_mask, s, p_out, scratch, (cudaStream_t)stream);
+}

@@ -93,6 +93,8 @@ _SIGNATURES = {
                             c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_int, c_int,
                             c_void_p]),
     "piv_smoothn": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p]),
+    "piv_smoothn_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p,
+                                    c_void_p]),
 }
 
 _lock = threading.Lock()
