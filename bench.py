@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--pairs", type=int, default=128, help="pairs per step per GPU")
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--dft", choices=["fft", "tensor"], default="fft", help="correlation engine of the chosen form")
+    ap.add_argument("--dft", choices=["fft", "tensor"], default="tensor", help="correlation engine of the chosen form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     return ap.parse_args()
@@ -171,6 +171,11 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # Roofline helpers.
 # ---------------------------------------------------------------------------
+def tc_executed_flops(ss, N):
+    """FLOPs the tensor engine executes per window pair (four dense DFT stages)."""
+    return 2 * (2 * ss * ss * 2 * N + 2 * N * 2 * ss * 2 * N + N * 2 * N * 2 * N + N * 2 * N * N)
+
+
 def corr_flops(ss, N):
     """Algorithmic FLOPs of one window-pair correlation: two real-to-complex and
     one complex-to-real 2-D FFT at 2.5 N^2 log2(N^2) each, the conjugate
@@ -327,6 +332,16 @@ def run_gpu(args):
     ms_step = ms / args.steps
     value = B * world / (ms_step * 1e-3)
     windows_per_pair = sum(f.n_wins for f in proc.piv_fields)
+    plain = None
+    if args.dft != "fft":
+        proc_plain = make("fft")
+        ms_p, _, _ = graph_time(proc_plain)
+        if dist:
+            t = torch.tensor([ms_p], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_p = float(t.item())
+        plain = {"pairs_per_s": B * world / (ms_p / args.steps * 1e-3), "ms_per_step": ms_p / args.steps}
+        plain["chosen_over_plain"] = value / plain["pairs_per_s"]
 
     # Stage breakdown (CUDA events inside the run, same stream).
     plan = proc.plan_handle(fa, B)
@@ -355,18 +370,29 @@ def run_gpu(args):
     kdom = int(dom[2:dom.index(".")])
     f = proc.piv_fields[kdom]
     N = proc._iterations[kdom].fft_size
-    flops = B * f.n_wins * corr_flops(f.search_size, N)
+    n_win = B * f.n_wins
+    flops = n_win * corr_flops(f.search_size, N)
     achieved = flops / (corr[dom] * 1e-3) / 1e12
     peaks = measured_peaks()
-    traffic = ncu_traffic().get(f"correlate_N{N}")
-    if args.dft == "tensor":
-        peak, unit, bound, src = peaks.get("bf16_tflops", 1900.0), "TFLOP/s", "tensor", "MEASURED_PEAKS.json bf16"
+    traffic_w = ncu_traffic()
+    on_tensor = args.dft == "tensor" and N == 2 * f.search_size and f.search_size in (16, 32)
+    if on_tensor:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        unit, bound = "TFLOP/s", "tensor"
+        src = "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in peaks else "fallback 1900 TFLOP/s"
+        key = f"correlate_tc_N{N}"
     else:
         peak, unit, bound, src = sgemm_tflops(torch), "TFLOP/s", "fp32", "cuBLAS SGEMM (TF32 off) measured here"
+        key = f"correlate_fft_N{N}"
+    per_window_traffic = traffic_w.get(key)
     roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-                "traffic": traffic * B * f.n_wins / max(1, B * f.n_wins) if traffic else None,
-                "kernel": f"correlate pass {kdom + 1} (ss={f.search_size}, N={N}, {B * f.n_wins} windows/launch)",
-                "peak_source": src, "launch_ms": corr[dom]}
+                "traffic": per_window_traffic * n_win if per_window_traffic else None,
+                "kernel": f"correlate pass {kdom + 1} (ss={f.search_size}, N={N}, {n_win} windows/launch, "
+                          f"{'tcgen05' if on_tensor else 'fft'})",
+                "peak_source": src, "launch_ms": corr[dom],
+                "algorithmic_flops_per_window": corr_flops(f.search_size, N)}
+    if on_tensor:
+        roofline["executed_tflops"] = n_win * tc_executed_flops(f.search_size, N) / (corr[dom] * 1e-3) / 1e12
 
     # End to end through the public API: pinned host frames in, fields out.
     pin_a = torch.as_tensor(host_a).pin_memory()
@@ -394,10 +420,15 @@ def run_gpu(args):
     accuracy = None
     if rank == 0 and not args.no_accuracy and cpu is not None:
         (_, u64, v64), (_, u32, v32) = cpu.map(_oracle_pair, [(0, "float64"), (0, "float32")])
-        gu, gv = res_u[0].astype(np.float64), res_v[0].astype(np.float64)
         rms = lambda a, b, c, d: float(np.sqrt(np.mean((a - b) ** 2 + (c - d) ** 2)))
-        accuracy = {"rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64), "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
+        gu, gv = res_u[0].astype(np.float64), res_v[0].astype(np.float64)
+        accuracy = {"form": args.dft, "rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64),
+                    "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
                     "max_px_vs_fp32_oracle": float(max(np.abs(gu - u32).max(), np.abs(gv - v32).max()))}
+        if args.dft != "fft":
+            pu, pv = proc_plain.run_batch(fa[:1], fb[:1])
+            pu, pv = pu[0].cpu().numpy(), pv[0].cpu().numpy()
+            accuracy["plain_rms_px_vs_fp64_oracle"] = rms(pu, u64, pv, v64)
 
     cpu_baseline = None
     if cpu is not None:
@@ -417,6 +448,7 @@ def run_gpu(args):
                        "form": args.dft, "graph": True,
                        "l2": "inputs larger than L2 (B x 2 MiB frames + 8 MiB float frames per pair per pass)"},
             "windows_per_s": value * windows_per_pair, "windows_per_pair": windows_per_pair,
+            "plain_form": plain,
             "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
             "stage_ms": stage_ms,

@@ -210,7 +210,7 @@ int piv_correlate(const piv_geometry* geom, int n_pairs, const void* frames_a, c
  * piv_correlate. */
 int piv_correlate_maps(const piv_geometry* geom, int n_pairs, const void* frames_a, const void* frames_b,
                        int pixel_type, int dtype, int fft_size, int normalize, const uint8_t* win_mask, void* maps,
-                       void* stream);
+                       int dft_mode, void* stream);
 
 /* Linear interpolation of a field from grid `src` to the coordinates of grid
  * `dst`, with linear extrapolation (interpolate_displacement,

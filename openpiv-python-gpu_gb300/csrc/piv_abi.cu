@@ -140,6 +140,7 @@ struct piv_plan {
   void* rep_scratch = nullptr;
   void* smooth_scratch = nullptr;
   double* rms_stats = nullptr;
+  int* status = nullptr;      // device status word of bounded device-side waits
   uint8_t* outliers = nullptr;
   double* u_final = nullptr;
   double* v_final = nullptr;
@@ -351,6 +352,10 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
   if (rc == PIV_OK) rc = plan_alloc(p, &p->smooth_scratch, sm_bytes);
   if (rc == PIV_OK) rc = plan_alloc_t(p, &p->rms_stats, 4 * (size_t)P);
   if (rc == PIV_OK) {
+    rc = plan_alloc_t(p, &p->status, 1);
+    if (rc == PIV_OK) cudaMemset(p->status, 0, sizeof(int));
+  }
+  if (rc == PIV_OK) {
     const size_t cnt = p->st.back().mn * P;
     rc = plan_alloc_t(p, &p->outliers, cnt);
     if (rc == PIV_OK) rc = plan_alloc_t(p, &p->u_final, cnt);
@@ -534,6 +539,7 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
     c.scratch = p->corr_scratch;
     c.scratch_bytes = p->corr_scratch_bytes;
     c.maps = nullptr;
+    c.status = p->status;
     if (cfg.dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
       PIV_TRY(correlate_tensor(c, s));
     } else {
@@ -572,7 +578,7 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
     ra.revalidate = it.revalidate;
     ra.dtype = cfg.dtype;
     ra.scratch = p->rep_scratch;
-    ra.status = nullptr;
+    ra.status = p->status;
     PIV_TRY(replace(ra, s));
     if (k == n_it - 1) {
       va.u = st.u_rep;
@@ -691,7 +697,17 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
   c.maps = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t need = correlate_fft_scratch_bytes(fft_size, dtype);
-  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) return correlate_tensor(c, s);
+  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
+    PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
+    cudaMemsetAsync(c.status, 0, sizeof(int), s);
+    int rc = correlate_tensor(c, s);
+    int st = 0;
+    cudaMemcpyAsync(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(c.status, s);
+    cudaStreamSynchronize(s);
+    if (rc == PIV_OK && st != 0) rc = set_error(st, "tensor correlation: a bounded wait gave up");
+    return rc;
+  }
   if (need) {
     PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
     c.scratch_bytes = need;
@@ -703,7 +719,7 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
 
 int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a, const void* frames_b,
                        int pixel_type, int dtype, int fft_size, int normalize, const uint8_t* win_mask, void* maps,
-                       void* stream) {
+                       int dft_mode, void* stream) {
   if (!g || !frames_a || !frames_b || !maps) return set_error(PIV_E_ARG, "NULL argument");
   if (!is_pow2(fft_size) || fft_size < g->search_size || fft_size > 256)
     return set_error(PIV_E_UNSUPPORTED, "fft_size %d is not supported", fft_size);
@@ -734,12 +750,21 @@ int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a,
   c.u = u;
   c.v = (char*)u + cnt * tsz;
   c.maps = maps;
+  int rc;
+  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
+    PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
+    cudaMemsetAsync(c.status, 0, sizeof(int), s);
+    rc = correlate_tensor(c, s);
+    cudaFreeAsync(c.status, s);
+    cudaFreeAsync(u, s);
+    return rc;
+  }
   const size_t need = correlate_fft_scratch_bytes(fft_size, dtype);
   if (need) {
     PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
     c.scratch_bytes = need;
   }
-  int rc = correlate_fft(c, s);
+  rc = correlate_fft(c, s);
   if (c.scratch) cudaFreeAsync(c.scratch, s);
   cudaFreeAsync(u, s);
   return rc;

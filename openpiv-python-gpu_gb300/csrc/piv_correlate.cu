@@ -46,7 +46,8 @@ struct FftLayout {
   static constexpr int NW = NT / 32;
   static constexpr size_t TW_BYTES = 256 * sizeof(Cplx<T>);
   static constexpr int PART = 2 * NW + WPC;            // per-warp / per-slot partial results
-  static constexpr size_t RED_BYTES = PART * (sizeof(T) + sizeof(int)) + 4 * WPC * sizeof(T) + 8 * WPC * sizeof(int);
+  static constexpr size_t RED_BYTES = WPC * sizeof(long long) + PART * (sizeof(T) + sizeof(int)) +
+                                      4 * WPC * sizeof(T) + 8 * WPC * sizeof(int);
   static constexpr size_t BUF_BYTES = (size_t)WPC * WIN * sizeof(Cplx<T>);
   static constexpr size_t SMEM_SMALL = TW_BYTES + ((RED_BYTES + 15) / 16) * 16;
   static constexpr bool GLOBAL_BUF = (SMEM_SMALL + BUF_BYTES) > 200 * 1024;
@@ -211,7 +212,8 @@ __global__ void __launch_bounds__(FftCfg<N, T>::NT) k_corr_fft(CorrArgs a, Cplx<
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cplx<T>* tw = reinterpret_cast<Cplx<T>*>(smem_raw);
   unsigned char* red = smem_raw + L::TW_BYTES;
-  T* part_v = reinterpret_cast<T*>(red);
+  long long* win_base = reinterpret_cast<long long*>(red);  // [WPC] element offset of each window's corner
+  T* part_v = reinterpret_cast<T*>(red + WPC * sizeof(long long));
   T* win_v = part_v + L::PART;         // 4 * WPC values
   int* part_i = reinterpret_cast<int*>(win_v + 4 * WPC);
   int* win_i = part_i + L::PART;       // 8 * WPC ints
@@ -250,62 +252,72 @@ __global__ void __launch_bounds__(FftCfg<N, T>::NT) k_corr_fft(CorrArgs a, Cplx<
     if (tid < WPC) {
       const long long g = g0 + tid;
       int ok = g < total;
-      if (ok && a.win_mask) ok = a.win_mask[(int)(g % n_wins)] == 0;
+      long long base = 0;
+      if (ok) {
+        const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
+        if (a.win_mask) ok = a.win_mask[k] == 0;
+        base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
+      }
       valid[tid] = ok;
+      win_base[tid] = base;
     }
     __syncthreads();
 
     // Window means (gpu_process.py:1201-1205); shrink: A over its inner window.
-    if (normalize) {
-      for (int w = 0; w < WPC; ++w) {
-        const long long g = g0 + w;
-        T sa = 0, sb = 0;
-        if (valid[w]) {
-          const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-          const long long base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width +
-                                 (k % nf) * sp + a.x_offset;
-          for (int e = tid; e < ss * ss; e += NT) {
-            const int r = e / ss, c = e % ss;
-            const long long idx = base + (long long)r * a.width + c;
-            if (r >= inner0 && r < inner1 && c >= inner0 && c < inner1)
-              sa += load_pixel<T>(a.frame_a, a.pixel_type, idx);
-            sb += load_pixel<T>(a.frame_b, a.pixel_type, idx);
+    // Pixel loads are specialised on the pixel type outside the loops.
+    auto fill = [&](auto tag) {
+      using P = decltype(tag);
+      const P* fa = reinterpret_cast<const P*>(a.frame_a);
+      const P* fb = reinterpret_cast<const P*>(a.frame_b);
+      if (normalize) {
+        for (int w = 0; w < WPC; ++w) {
+          T sa = 0, sb = 0;
+          if (valid[w]) {
+            const long long base = win_base[w];
+            for (int e = tid; e < ss * ss; e += NT) {
+              const int r = e / ss, c = e % ss;
+              const long long idx = base + (long long)r * a.width + c;
+              if (r >= inner0 && r < inner1 && c >= inner0 && c < inner1) sa += (T)__ldg(fa + idx);
+              sb += (T)__ldg(fb + idx);
+            }
           }
+          sa = warp_sum(sa);
+          sb = warp_sum(sb);
+          if ((tid & 31) == 0) { part_v[tid >> 5] = sa; part_v[NW + (tid >> 5)] = sb; }
+          __syncthreads();
+          if (tid == 0) {
+            T ta = 0, tb = 0;
+            for (int q = 0; q < NW; ++q) { ta += part_v[q]; tb += part_v[NW + q]; }
+            const int wa = inner1 - inner0;
+            means[2 * w] = ta / (T)(wa * wa);
+            means[2 * w + 1] = tb / (T)(ss * ss);
+          }
+          __syncthreads();
         }
-        sa = warp_sum(sa);
-        sb = warp_sum(sb);
-        if ((tid & 31) == 0) { part_v[tid >> 5] = sa; part_v[NW + (tid >> 5)] = sb; }
-        __syncthreads();
-        if (tid == 0) {
-          T ta = 0, tb = 0;
-          for (int q = 0; q < NW; ++q) { ta += part_v[q]; tb += part_v[NW + q]; }
-          const int wa = inner1 - inner0;
-          means[2 * w] = ta / (T)(wa * wa);
-          means[2 * w + 1] = tb / (T)(ss * ss);
-        }
-        __syncthreads();
       }
-    }
-
-    // Fill the N x N buffers: z = (a - mean_a) + i (b - mean_b) in the centre, 0 elsewhere.
-    for (int e = tid; e < WPC * N * N; e += NT) {
-      const int w = e / (N * N), rc = e % (N * N), r = rc / N - pad, c = rc % N - pad;
-      Cplx<T> z = cmake<T>(0, 0);
-      if (valid[w] && r >= 0 && r < ss && c >= 0 && c < ss) {
-        const long long g = g0 + w;
-        const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-        const long long idx = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset + r) * a.width +
-                              (k % nf) * sp + a.x_offset + c;
-        T va = 0;
-        if (r >= inner0 && r < inner1 && c >= inner0 && c < inner1) {
-          va = load_pixel<T>(a.frame_a, a.pixel_type, idx);
-          if (normalize) va = va - means[2 * w];
+      // Fill the N x N buffers: z = (a - mean_a) + i (b - mean_b) in the centre, 0 elsewhere.
+      for (int e = tid; e < WPC * N * N; e += NT) {
+        const int w = e / (N * N), rc = e % (N * N), r = rc / N - pad, c = rc % N - pad;
+        Cplx<T> z = cmake<T>(0, 0);
+        if (valid[w] && r >= 0 && r < ss && c >= 0 && c < ss) {
+          const long long idx = win_base[w] + (long long)r * a.width + c;
+          T va = 0;
+          if (r >= inner0 && r < inner1 && c >= inner0 && c < inner1) {
+            va = (T)__ldg(fa + idx);
+            if (normalize) va = va - means[2 * w];
+          }
+          T vb = (T)__ldg(fb + idx);
+          if (normalize) vb = vb - means[2 * w + 1];
+          z = cmake<T>(va, vb);
         }
-        T vb = load_pixel<T>(a.frame_b, a.pixel_type, idx);
-        if (normalize) vb = vb - means[2 * w + 1];
-        z = cmake<T>(va, vb);
+        buf[w * L::WIN + (rc / N) * LD + (rc % N)] = z;
       }
-      buf[w * L::WIN + (rc / N) * LD + (rc % N)] = z;
+    };
+    switch (a.pixel_type) {
+      case PIV_PIXEL_U8: fill(uint8_t{}); break;
+      case PIV_PIXEL_U16: fill(uint16_t{}); break;
+      case PIV_PIXEL_F32: fill(float{}); break;
+      default: fill(double{}); break;
     }
     __syncthreads();
 

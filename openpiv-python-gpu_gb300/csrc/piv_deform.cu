@@ -4,14 +4,17 @@
 //   gpu_process.py:730-742);
 // * deform: the predictor onto every pixel and the deformed frames
 //   (deform_frame + interpolate_frame, gpu_process.py:1149-1192, 1461-1547), with
-//   the reference's bilinear kernel or this project's cubic B-spline sampling;
+//   the reference's bilinear kernel or this project's cubic B-spline sampling.
+//   The per-pixel predictor is evaluated in float32 (the reference uses
+//   float64 and casts to float32; float64 throughput on this GPU is a small
+//   fraction of float32);
 // * spline_prefilter: cubic B-spline coefficients (mirror boundary) for the cubic path.
 //
 // Both interpolations of the predictor restate RegularGridInterpolator(...,
 // bounds_error=False, fill_value=None) on the reference's uniform grids:
 // interval index clamped to [0, n-2], weights from the unclamped normalised
-// distance, evaluated in float64 as separate IEEE operations in the order the
-// host oracle uses.
+// distance. The field-to-field regrid runs in float64 as separate IEEE
+// operations in the order the host oracle uses.
 #include <math.h>
 
 #include "piv_common.cuh"
@@ -115,12 +118,12 @@ PIV_D T sample_bilinear(const void* frame, int pixel_type, long long base, int W
   return r;
 }
 
+// Mirror index for taps in [-(n-1), 2(n-1)] (sample coordinates are clamped
+// into the frame, so taps stay within one reflection).
 PIV_D int mirror_index(int i, int n) {
   if (n == 1) return 0;
-  const int period = 2 * (n - 1);
-  i = i % period;
-  if (i < 0) i += period;
-  return i < n ? i : period - i;
+  i = i < 0 ? -i : i;
+  return i < n ? i : 2 * (n - 1) - i;
 }
 
 PIV_D void bspline3_weights(float t, float* w) {
@@ -155,17 +158,49 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
   return acc;
 }
 
+// Predictor weight of one axis at integer pixel coordinate q on the uniform
+// grid g_k = k*sp + ss/2 + off: interval index clamped to [0, len-2], weight
+// from the unclamped distance. Works in doubled integer coordinates so that
+// odd search sizes (half-integer grid points) stay exact.
+struct AxisWeight {
+  int i;
+  float t;
+};
+PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
+  const int d2 = 2 * q - (ss + 2 * off), sp2 = 2 * sp;
+  int i = d2 >= 0 ? d2 / sp2 : -((-d2 + sp2 - 1) / sp2);  // floor division
+  i = i < 0 ? 0 : (i > len - 2 ? len - 2 : i);
+  if (len < 2) i = 0;
+  const float t = len < 2 ? 0.0f : (float)(d2 - i * sp2) / (float)sp2;
+  return AxisWeight{i, t};
+}
+
+// Bilinear predictor value from four float64 field values, in float32.
+PIV_D float lerp2(const double* v, int n, const AxisWeight& wy, const AxisWeight& wx, int my, int nx) {
+  const int iy1 = my < 2 ? wy.i : wy.i + 1, ix1 = nx < 2 ? wx.i : wx.i + 1;
+  const float v00 = (float)__ldg(v + wy.i * n + wx.i), v01 = (float)__ldg(v + wy.i * n + ix1);
+  const float v10 = (float)__ldg(v + iy1 * n + wx.i), v11 = (float)__ldg(v + iy1 * n + ix1);
+  const float top = fmaf(wx.t, v01 - v00, v00);
+  const float bot = fmaf(wx.t, v11 - v10, v10);
+  return fmaf(wy.t, bot - top, top);
+}
+
+// One thread per pixel: predictor at the pixel (float32; the reference
+// evaluates it in float64 and casts to the frame type, a difference of one or
+// two float32 ulps), then frame A sampled at x + up*dta and frame B at
+// x + up*dtb.
+// Launch grid: x over the columns of a row, y over rows, z over pairs.
 template <typename T>
 __global__ void k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
   const piv_geometry& g = a.geom;
   const int H = g.height, W = g.width;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= W) return;
+  const int i = blockIdx.y, pair = blockIdx.z;
   const long long npix = (long long)H * W;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npix * a.n_pairs) return;
-  const int pair = (int)(t / npix);
-  const long long p = t % npix;
-  const int i = (int)(p / W), j = (int)(p % W);
+  const long long p = (long long)i * W + j;
   const long long base = (long long)pair * npix;
+  const long long t = base + p;
   T* out_a = reinterpret_cast<T*>(a.out_a);
   T* out_b = reinterpret_cast<T*>(a.out_b);
   if (a.frame_mask && a.frame_mask[p]) {
@@ -173,12 +208,12 @@ __global__ void k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
     out_b[t] = (T)0;
     return;
   }
-  // Predictor at the pixel, float64 then cast to the frame type (gpu_process.py:1159-1162).
-  const GridAxis ay = axis_y(g), ax = axis_x(g);
+  const AxisWeight wy = axis_weight(i, g.search_size, g.y_offset, g.spacing, g.m);
+  const AxisWeight wx = axis_weight(j, g.search_size, g.x_offset, g.spacing, g.n);
   const long long fo = (long long)pair * g.m * g.n;
   const T x = (T)j, y = (T)i;
-  const T up = (T)grid_interp(a.up + fo, g.n, ay, ax, (double)y, (double)x);
-  const T vp = (T)grid_interp(a.vp + fo, g.n, ay, ax, (double)y, (double)x);
+  const T up = (T)lerp2(a.up + fo, g.n, wy, wx, g.m, g.n);
+  const T vp = (T)lerp2(a.vp + fo, g.n, wy, wx, g.m, g.n);
   if (do_a) {
     const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
     out_a[t] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
@@ -206,8 +241,10 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   if (dp > 0 && dp < 1) { dta = dp - 1; dtb = dp; do_a = do_b = 1; }
   else if (dp == 1) { dtb = 1; do_b = 1; }
   else { dta = -1; do_a = 1; }
+  if (a.geom.height > 65535 || a.n_pairs > 65535)
+    return set_error(PIV_E_UNSUPPORTED, "deformation grid limit (height and pairs <= 65535)");
   const int bs = 256;
-  const unsigned grid = (unsigned)((total + bs - 1) / bs);
+  const dim3 grid((unsigned)((a.geom.width + bs - 1) / bs), (unsigned)a.geom.height, (unsigned)a.n_pairs);
   if (a.dtype == PIV_DTYPE_F64)
     k_deform<double><<<grid, bs, 0, stream>>>(a, dta, dtb, do_a, do_b);
   else

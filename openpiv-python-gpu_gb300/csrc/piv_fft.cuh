@@ -85,9 +85,12 @@ PIV_D Cplx<T> twiddle(const Cplx<T>* __restrict__ tw, int e) {
 // line l, es the element stride.
 template <int N, int R1, int R2, bool INV, typename T, class LineOff>
 PIV_D void fft_pass_a(Cplx<T>* buf, int n_lines, LineOff line_off, int es, const Cplx<T>* tw, int tid, int nt) {
+  // Line index fastest: a warp's lanes touch 32 lines at the same in-line
+  // position (row lines are N+1 elements apart, an odd count, so 8-byte
+  // accesses are bank-conflict free; column lines are adjacent).
   for (int it = tid; it < n_lines * R1; it += nt) {
-    const int n1 = it % R1;
-    const int l = it / R1;
+    const int l = it % n_lines;
+    const int n1 = it / n_lines;
     Cplx<T>* p = buf + line_off(l) + n1 * es;
     Cplx<T> x[R2];
 #pragma unroll
@@ -112,8 +115,8 @@ template <int N, int R1, int R2, bool INV, typename T, class LineOff>
 PIV_D void fft_pass_b(Cplx<T>* buf, int n_lines, LineOff line_off, int es, const Cplx<T>* tw, int tid, int nt) {
   if constexpr (R1 > 1) {
     for (int it = tid; it < n_lines * R2; it += nt) {
-      const int k2 = it % R2;
-      const int l = it / R2;
+      const int l = it % n_lines;
+      const int k2 = it / n_lines;
       Cplx<T>* p = buf + line_off(l) + R1 * k2 * es;
       Cplx<T> x[R1];
 #pragma unroll

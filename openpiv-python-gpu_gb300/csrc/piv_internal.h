@@ -36,6 +36,7 @@ struct CorrArgs {
   void* scratch;        // device scratch for transforms that do not fit in shared memory
   size_t scratch_bytes;
   void* maps;           // optional [windows][N][N] output of the shifted correlation maps
+  int* status;          // device word set to PIV_E_TIMEOUT when a bounded wait gives up (tensor engine)
 };
 
 int correlate_fft(const CorrArgs& a, cudaStream_t stream);

@@ -81,7 +81,7 @@ _SIGNATURES = {
                               c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_int,
                               c_void_p]),
     "piv_correlate_maps": (c_int, [POINTER(PivGeometry), c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
-                                   c_void_p, c_void_p, c_void_p]),
+                                   c_void_p, c_void_p, c_int, c_void_p]),
     "piv_regrid": (c_int, [POINTER(PivGeometry), POINTER(PivGeometry), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p]),
     "piv_deform": (c_int, [POINTER(PivGeometry), c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_double,
