@@ -2,28 +2,33 @@
 // correlation (gpu_process.py:1207-1246) as dense matrix products on the 5th
 // generation tensor cores, fp16 operands, fp32 accumulation in TMEM.
 //
-// A CTA of 256 threads owns a tile of W = 128/ss window pairs; threads t and
-// t + 128 share TMEM lane t and split every phase in two natural halves
-// (frame a / frame b, or row tile 0 / row tile 1). With N = 2 ss (the reference's default n_fft = 2, centred zero
-// pad of ss/2):
-//   stage 1  T = a G^T             rows (w, y),   K = x,             cols (Re|Im, f_c)
-//   stage 2  A = G T               rows (w, f_c), K = (Re|Im, y),    cols (Re|Im, f_r)
-//   product  P = s_w conj(A) B     in registers (fp32), s_w a power of two
-//   stage 3  U = P E / N           rows (w, f_c), K = (Re|Im, f_r),  cols (Re|Im, r)
-//   stage 4  c = Re(U E^T) / N     rows (w, r),   K = (Re|Im, f_c),  cols s
-// G = exp(-2 pi i f (x + ss/2)/N) folds the zero pad into the forward matrices,
-// E = exp(+2 pi i f r / N). Between stages a warp reads its accumulator lanes
-// (tcgen05.ld), converts to fp16 and writes the next stage's operand tile to
-// shared memory (K-major or MN-major, no swizzle). s_w = 2^(14 - ceil(log2(
-// sum|a| * sum|b|))) keeps |P| below 2^14, inside fp16 range, and the two 1/N
-// factors keep U and c there too; c is scaled back exactly. The map in TMEM
+// Real-input ("packed") DFTs. For a real sequence g of length ss placed at
+// offset ss/2 of a zero-padded length N = 2 ss (the reference's default
+// n_fft = 2, centred pad), the N real numbers
+//   R[0] = Re X(0), R[1] = Re X(N/2), R[2f] = Re X(f), R[2f+1] = Im X(f), 0 < f < N/2
+// hold the whole spectrum X (X(N-f) = conj X(f)); F is the N x ss matrix that
+// maps g to R. A CTA of 128 threads (one per TMEM lane) owns W = 128/ss
+// window pairs per tile:
+//   stage 1  T = a F^T   rows (w, y),          K = x,  cols packed f_c       (per frame)
+//   stage 2  X = T^T F^T rows (tile e|o, w, c), K = y,  cols packed f_r       (per frame)
+//            tile e holds the rows k = 2c of T^T (Re T, or the DC column),
+//            tile o the rows k = 2c + 1 (Im T, or the Nyquist column), so
+//            each thread finds both halves of its complex column in its own lane.
+//   product  Q(f_r, c) = 2^-10 conj(A) B for c = 1 .. N/2-1 and all f_r; row c = 0
+//            packs the two real-input columns: Q = conj(A0) B0 + i conj(AN) BN.
+//   stage 3  U = Q E / N rows (w, c),              K = (Re|Im, f_r), cols (Re|Im, r)
+//   stage 4  c = U E' / N rows (w, r),             K = (Re|Im, c),   cols s
+// where E is the inverse DFT along f_r and E' the real inverse along f_c
+// (U(r, N-c) = conj U(r, c)). Each frame's window is scaled by a power of two
+// 2^e with sum |2^e (a - mean)| <= 2^12, so every fp16 operand stays below
+// 2^15; the map is scaled back exactly by 2^(10 - e_a - e_b). The map in TMEM
 // (one row per lane) then goes through the same peak search and subpixel fit
 // as the FFT engine: first maximum in the fftshift-ed row-major order, lags
 // without window overlap read as exact zeros.
 #include <cuda_fp16.h>
 #include <math.h>
-#include <stdio.h>
-#include <stdlib.h>
+
+#include <algorithm>
 
 #include "piv_common.cuh"
 #include "piv_internal.h"
@@ -33,22 +38,22 @@ namespace piv {
 
 template <int SS>
 struct TcLayout {
-  static constexpr int N = 2 * SS;          // DFT size
-  static constexpr int W = 128 / SS;        // window pairs per tile
-  static constexpr int TCOLS = 8 * N;       // TMEM columns (stage 2 holds A and B of both row tiles)
-  // fp16 operand tiles (bytes).
-  static constexpr int B1 = 0;                             // [2N][SS]   K-major
-  static constexpr int B2 = B1 + 2 * N * SS * 2;           // [2N][2SS]  K-major
-  static constexpr int B3 = B2 + 2 * N * 2 * SS * 2;       // [2N][2N]   K-major
-  static constexpr int B4 = B3 + 2 * N * 2 * N * 2;        // [N][2N]    K-major
-  static constexpr int A1 = B4 + N * 2 * N * 2;            // 2 x [128][SS] K-major (frames a, b)
-  static constexpr int A2 = A1 + 2 * 128 * SS * 2;         // 2 frames x 2 row tiles x [128][2SS] MN-major; reused as A4
-  static constexpr int A3 = A2 + 2 * 2 * 128 * 2 * SS * 2; // 2 row tiles x [128][2N] K-major
-  static constexpr int END = A3 + 2 * 128 * 2 * N * 2;
-  static constexpr int A2_TILE = 128 * 2 * SS * 2;         // bytes of one A2 row tile
-  static constexpr int A4_TILE = 128 * 2 * N * 2;          // bytes of one A4 row tile (in the A2 region)
-  static constexpr int A3_TILE = 128 * 2 * N * 2;
-  static constexpr size_t SMEM = END + 1024;               // + alignment slack
+  static constexpr int N = 2 * SS;           // DFT size
+  static constexpr int HN = N / 2;
+  static constexpr int W = 128 / SS;         // window pairs per tile
+  static constexpr int TCOLS = 4 * N;        // TMEM columns (stage 2: two frames x two row tiles)
+  // fp16 operand tiles (byte offsets). X and Y are each reused by two stages.
+  static constexpr int B1 = 0;                          // F [N][SS] K-major (stages 1 and 2)
+  static constexpr int B3 = B1 + N * SS * 2;            // [2N][2N] K-major
+  static constexpr int B4 = B3 + 2 * N * 2 * N * 2;     // [N][N] K-major
+  static constexpr int XB = B4 + N * N * 2;             // A1: 2 x [128][SS] K-major;  A3: [128][2N] K-major
+  static constexpr int YB = XB + 1024 * SS;             // A2: 2 x 2 x [128][SS] MN-major;  A4: 2 x [128][N] MN-major
+  static constexpr int END = YB + 1024 * SS;
+  static constexpr int A1_BYTES = 128 * SS * 2;
+  static constexpr int A2_BYTES = 128 * SS * 2;
+  static constexpr int A4_BYTES = 128 * N * 2;
+  static constexpr size_t SMEM = END + 128;             // + alignment slack
+  static constexpr int MIN_BLOCKS = 512 / TCOLS;        // CTAs per SM that the TMEM allows
 };
 
 // Byte offset of element (r, k) in a no-swizzle K-major tile with K columns.
@@ -76,40 +81,53 @@ PIV_D void sth(unsigned char* base, uint32_t off, float v) {
   *reinterpret_cast<__half*>(base + off) = __float2half_rn(v);
 }
 
+// 2^e for |e| <= 126.
+PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
+
 static constexpr uint32_t kMaxPolls = 1u << 24;
 
-template <int SS>
-struct TcThreads {
-  static constexpr int NT = 256;                  // two threads per TMEM lane
-  static constexpr int MIN_BLOCKS = SS == 16 ? 2 : 1;
+// Product of one frequency pair: the outputs at f_r = g (q0) and f_r = N - g
+// (q1) from the spectra E (even row) and O (odd row) of frames a and b at f_r = g.
+struct PairQ {
+  float r0, i0, r1, i1;
 };
+PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, float bi, float pr, float pi,
+                         bool special) {
+  const float re1 = fmaf(ar, br, ai * bi), im1 = fmaf(ar, bi, -ai * br);     // conj(Ea) Eb
+  const float re2 = fmaf(orr, pr, oi * pi), im2 = fmaf(orr, pi, -oi * pr);   // conj(Oa) Ob
+  const float re3 = fmaf(ar, pr, ai * pi), im3 = fmaf(ar, pi, -ai * pr);     // conj(Ea) Ob
+  const float re4 = fmaf(orr, br, oi * bi), im4 = fmaf(orr, bi, -oi * br);   // conj(Oa) Eb
+  PairQ q;
+  q.r0 = special ? re1 - im2 : (re1 + re2) + (im4 - im3);
+  q.i0 = special ? im1 + re2 : (im1 + im2) + (re3 - re4);
+  q.r1 = special ? re1 + im2 : (re1 + re2) - (im4 - im3);
+  q.i1 = special ? re2 - im1 : (re3 - re4) - (im1 + im2);
+  return q;
+}
 
 template <int SS>
-__global__ void __launch_bounds__(256, TcThreads<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
+__global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
   using L = TcLayout<SS>;
-  constexpr int N = L::N, W = L::W, H = N / 2;
-  constexpr int NT = TcThreads<SS>::NT;
+  constexpr int N = L::N, HN = L::HN, W = L::W;
+  constexpr int NPART = N / 32;      // warps per window in the epilogue
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ float tw_re[N], tw_im[N];
-  __shared__ float l1[2][W];         // sum |a - mean| and sum |b - mean| per window
-  __shared__ float sc_exp[W];        // log2 of the product scale per window
+  __shared__ int sc_e[2][W];         // per frame and window: log2 of the operand scale
   __shared__ long long win_base[W];
   __shared__ int win_valid[W];
-  __shared__ float pk_val[W][2];     // per window: best value of each 32-row part
-  __shared__ int pk_idx[W][2];
-  __shared__ float nb[W][5];         // c, cd, cu, cl, cr
+  __shared__ float pk_val[W][NPART];
+  __shared__ int pk_idx[W][NPART];
+  __shared__ float nb[W][5];         // c, cd, cu, cl, cr (scaled)
 
   const int tid = threadIdx.x;
-  const int half = tid >> 7;         // frame (staging, stage 1 -> 2) or row tile (later phases)
-  const int t = tid & 127;           // TMEM lane of this thread
   const int warp = tid >> 5, lane = tid & 31;
-  const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
+  const uint32_t lane_sel = (uint32_t)(32 * warp) << 16;
 
   // Twiddles W_N^k = exp(-2 pi i k / N).
-  for (int k = tid; k < N; k += NT) {
+  for (int k = tid; k < N; k += 128) {
     float sn, cs;
     sincospif(2.0f * (float)k / (float)N, &sn, &cs);
     tw_re[k] = cs;
@@ -117,32 +135,32 @@ __global__ void __launch_bounds__(256, TcThreads<SS>::MIN_BLOCKS) k_corr_tc(Corr
   }
   if (tid == 0) tc::mbar_init(&bar, 1);
   __syncthreads();
-  // Constant DFT operands.
   const float inv_n = 1.0f / (float)N;
-  const int pad = SS / 2;
-  for (int e = tid; e < 2 * N * SS; e += NT) {  // B1[n][x]
-    const int n = e / SS, x = e % SS, f = n % N, q = (f * (x + pad)) % N;
-    sth(sm + L::B1, off_k(n, x, SS), n < N ? tw_re[q] : tw_im[q]);
+  const int p0 = SS / 2;
+  for (int e = tid; e < N * SS; e += 128) {  // F[k][x]
+    const int k = e / SS, x = e % SS, f = k >> 1, q = (f * (x + p0)) % N;
+    float v;
+    if (k == 0) v = 1.0f;
+    else if (k == 1) v = ((x + p0) & 1) ? -1.0f : 1.0f;
+    else v = (k & 1) ? tw_im[q] : tw_re[q];
+    sth(sm + L::B1, off_k(k, x, SS), v);
   }
-  for (int e = tid; e < 2 * N * 2 * SS; e += NT) {  // B2[n][k]
-    const int n = e / (2 * SS), k = e % (2 * SS), fr = n % N, y = k % SS, part = k / SS;
-    const int q = (fr * (y + pad)) % N;
-    const float gr = tw_re[q], gi = tw_im[q];
-    const float v = n < N ? (part == 0 ? gr : -gi) : (part == 0 ? gi : gr);
-    sth(sm + L::B2, off_k(n, k, 2 * SS), v);
-  }
-  for (int e = tid; e < 2 * N * 2 * N; e += NT) {  // B3[n][k], E = conj(W)/N
-    const int n = e / (2 * N), k = e % (2 * N), r = n % N, fr = k % N;
+  for (int e = tid; e < 4 * N * N; e += 128) {  // B3[n][kappa], kappa = (part, b, g)
+    const int n = e / (2 * N), kap = e % (2 * N);
+    const int part = kap / N, b = (kap % N) / HN, g = kap % HN;
+    const int fr = b == 0 ? g : (g == 0 ? HN : N - g), r = n % N;
     const int q = (fr * r) % N;
-    const float er = tw_re[q] * inv_n, ei = -tw_im[q] * inv_n;
-    const float v = n < N ? (k < N ? er : -ei) : (k < N ? ei : er);
-    sth(sm + L::B3, off_k(n, k, 2 * N), v);
+    const float cs = tw_re[q] * inv_n, sn = -tw_im[q] * inv_n;
+    const float v = n < N ? (part == 0 ? cs : -sn) : (part == 0 ? sn : cs);
+    sth(sm + L::B3, off_k(n, kap, 2 * N), v);
   }
-  for (int e = tid; e < N * 2 * N; e += NT) {  // B4[s][k]: Re(U e^{+i theta}) / N
-    const int sidx = e / (2 * N), k = e % (2 * N), fc = k % N;
-    const int q = (fc * sidx) % N;
-    const float v = k < N ? tw_re[q] * inv_n : tw_im[q] * inv_n;
-    sth(sm + L::B4, off_k(sidx, k, 2 * N), v);
+  for (int e = tid; e < N * N; e += 128) {  // B4[s][kappa], kappa = (part, c)
+    const int s = e / N, kap = e % N, part = kap / HN, c = kap % HN;
+    const int q = (c * s) % N;
+    float v;
+    if (c == 0) v = part == 0 ? inv_n : ((s & 1) ? -inv_n : inv_n);
+    else v = part == 0 ? 2.0f * tw_re[q] * inv_n : 2.0f * tw_im[q] * inv_n;
+    sth(sm + L::B4, off_k(s, kap, N), v);
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base_s, L::TCOLS);
   tc::fence_async_smem();
@@ -191,237 +209,271 @@ __global__ void __launch_bounds__(256, TcThreads<SS>::MIN_BLOCKS) k_corr_tc(Corr
     }
     __syncthreads();
 
-    // ---- Staging: thread (half, t): frame `half`, row t = (w, y) of the tile.
+    // ---- Staging: thread (w, y) gathers row y of window w of both frames.
     {
-      const int w = t / SS, y = t % SS;
+      const int w = tid / SS, y = tid % SS;
       const bool ok = win_valid[w] != 0;
-      const void* frame = half == 0 ? a.frame_a : a.frame_b;
-      float r[SS];
-      float sum = 0.f;
       const long long rowoff = win_base[w] + (long long)y * a.width;
 #pragma unroll
-      for (int x = 0; x < SS; ++x) {
-        r[x] = ok ? load_pixel<float>(frame, a.pixel_type, rowoff + x) : 0.f;
-        sum += r[x];
+      for (int f = 0; f < 2; ++f) {
+        const void* frame = f == 0 ? a.frame_a : a.frame_b;
+        float r[SS];
+        float sum = 0.f;
+#pragma unroll
+        for (int x = 0; x < SS; ++x) {
+          r[x] = ok ? load_pixel<float>(frame, a.pixel_type, rowoff + x) : 0.f;
+          sum += r[x];
+        }
+        // Window sums over its SS rows (a window's lanes are contiguous, SS | 32).
+#pragma unroll
+        for (int o = 1; o < SS; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        const float mean = sum / (float)(SS * SS);
+        float l = 0.f;
+#pragma unroll
+        for (int x = 0; x < SS; ++x) {
+          r[x] -= mean;
+          l += fabsf(r[x]);
+        }
+#pragma unroll
+        for (int o = 1; o < SS; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        int e = 0;
+        if (l > 0.f) e = min(120, max(-120, 11 - ilogbf(l)));
+        const float s = pow2i(e);
+#pragma unroll
+        for (int x = 0; x < SS; ++x) r[x] *= s;
+        if (y == 0) sc_e[f][w] = e;
+#pragma unroll
+        for (int x = 0; x < SS; x += 8) st8(sm + L::XB + f * L::A1_BYTES, off_k(tid, x, SS), r + x);
       }
-      // Window sum over its SS rows (a window's lanes are contiguous, SS | 32).
-#pragma unroll
-      for (int o = 1; o < SS && o < 32; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      const float mean = sum / (float)(SS * SS);
-      float l = 0.f;
-#pragma unroll
-      for (int x = 0; x < SS; ++x) {
-        r[x] -= mean;
-        l += fabsf(r[x]);
-      }
-#pragma unroll
-      for (int o = 1; o < SS && o < 32; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-      if (y == 0) l1[half][w] = l;
-#pragma unroll
-      for (int x = 0; x < SS; x += 8) st8(sm + L::A1 + half * 128 * SS * 2, off_k(t, x, SS), r + x);
     }
     sync_for_mma();
-    if (tid < W) {
-      const float prod = l1[0][tid] * l1[1][tid];
-      sc_exp[tid] = prod > 0.f ? (float)(14 - (int)ceilf(log2f(prod))) : 0.f;
-    }
 
-    // ---- Stage 1: T = a G^T for a and b -> TMEM cols [0, 2N) and [2N, 4N).
+    // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
     if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
+      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
-      for (int f = 0; f < 2; ++f) {
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
         for (int ks = 0; ks < SS / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::A1 + f * 128 * SS * 2 + ks * 256, 128, SS * 16);
+          const uint64_t ad = tc::sdesc(sbase + L::XB + f * L::A1_BYTES + ks * 256, 128, SS * 16);
           const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
-          tc::mma_f16(tmem + f * 2 * N, ad, bd, id, ks > 0);
+          tc::mma_f16(tmem + f * N, ad, bd, id, ks > 0);
         }
-      }
       tc::mma_commit(&bar);
     }
     if (!wait_mma()) break;
 
-    // ---- Stage 1 -> 2: frame `half`: T rows (w, y) become MN-major rows (w, f_c), K = (Re|Im, y).
+    // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
+    // (w, c) of tile e (k = 2c) and tile o (k = 2c + 1).
     {
-      const int w = t / SS, y = t % SS;
-      unsigned char* dst = sm + L::A2 + half * 2 * L::A2_TILE;
-      float v[2 * N];
+      const int w = tid / SS, y = tid % SS;
 #pragma unroll
-      for (int c0 = 0; c0 < 2 * N; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + half * 2 * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
+      for (int f = 0; f < 2; ++f) {
+        float v[N];
 #pragma unroll
-      for (int c0 = 0; c0 < 2 * N; c0 += 8) {
-        const int k = (c0 / N) * SS + y;   // Re rows then Im rows of K
-        const int m = w * N + (c0 % N);    // global operand row
-        st8(dst + (m >> 7) * L::A2_TILE, off_mn(m & 127, k, 128), v + c0);
+        for (int c0 = 0; c0 < N; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + f * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int rt = 0; rt < 2; ++rt) {
+          unsigned char* dst = sm + L::YB + (f * 2 + rt) * L::A2_BYTES;
+#pragma unroll
+          for (int c0 = 0; c0 < HN; c0 += 8) {
+            float v8[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
+            st8(dst, off_mn(w * HN + c0, y, 128), v8);
+          }
+        }
       }
     }
     sync_for_mma();
 
-    // ---- Stage 2: A = G T for a, b and both row tiles -> TMEM cols [f*4N + rt*2N, +2N).
+    // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
     if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, 2 * N, 1, 0);
-      for (int f = 0; f < 2; ++f)
-        for (int rt = 0; rt < 2; ++rt)
-          for (int ks = 0; ks < 2 * SS / 16; ++ks) {
-            const uint64_t ad = tc::sdesc(sbase + L::A2 + (f * 2 + rt) * L::A2_TILE + ks * 32 * 128, 128 * 16, 128);
-            const uint64_t bd = tc::sdesc(sbase + L::B2 + ks * 256, 128, 2 * SS * 16);
-            tc::mma_f16(tmem + f * 4 * N + rt * 2 * N, ad, bd, id, ks > 0);
+      const uint32_t id = tc::idesc_f16(128, N, 1, 0);
+#pragma unroll
+      for (int rt = 0; rt < 2; ++rt)
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+#pragma unroll
+          for (int ks = 0; ks < SS / 16; ++ks) {
+            const uint64_t ad =
+                tc::sdesc(sbase + L::YB + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
+            const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
+            tc::mma_f16(tmem + rt * 2 * N + f * N, ad, bd, id, ks > 0);
           }
       tc::mma_commit(&bar);
     }
     if (!wait_mma()) break;
 
-    // ---- Product (row tile `half`): P = s_w conj(A) B, K-major rows (w, f_c), K = (Re|Im, f_r).
+    // ---- Product: thread (w, c) forms row c of Q, K = (Re|Im, b, g) with
+    // f_r = g (b = 0) or N - g (b = 1; g = 0 pairs with f_r = N/2).
     {
-      const int rt = half, m = rt * 128 + t, w = m / N;
-      const float sc = exp2f(sc_exp[w]);
-      unsigned char* dst = sm + L::A3 + rt * L::A3_TILE;
+      const bool special = (tid % HN) == 0;
+      const float qs = 1.0f / 1024.0f;
+      unsigned char* dst = sm + L::XB;
 #pragma unroll
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float ar[16], ai[16], br[16], bi[16];
-        tc::tmem_ld16(tmem + lane_sel + rt * 2 * N + c0, ar);
-        tc::tmem_ld16(tmem + lane_sel + rt * 2 * N + N + c0, ai);
-        tc::tmem_ld16(tmem + lane_sel + 4 * N + rt * 2 * N + c0, br);
-        tc::tmem_ld16(tmem + lane_sel + 4 * N + rt * 2 * N + N + c0, bi);
+      for (int g0 = 0; g0 < HN; g0 += 8) {
+        float ea[16], eb[16], oa[16], ob[16];
+        tc::tmem_ld16(tmem + lane_sel + 0 * N + 2 * g0, ea);
+        tc::tmem_ld16(tmem + lane_sel + 1 * N + 2 * g0, eb);
+        tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
+        tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
-        float pr[16], pi[16];
+        float qr0[8], qi0[8], qr1[8], qi1[8];
 #pragma unroll
-        for (int h = 0; h < 16; ++h) {
-          pr[h] = (ar[h] * br[h] + ai[h] * bi[h]) * sc;
-          pi[h] = (ar[h] * bi[h] - ai[h] * br[h]) * sc;
+        for (int i = 0; i < 8; ++i) {
+          PairQ q;
+          if (g0 + i == 0) {
+            // f_r = 0 and f_r = N/2: real spectra R[0] and R[1].
+            const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
+            const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
+            q.r0 = q0.r0; q.i0 = q0.i0; q.r1 = q1.r0; q.i1 = q1.i0;
+          } else {
+            q = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                             ob[2 * i], ob[2 * i + 1], special);
+          }
+          qr0[i] = q.r0 * qs; qi0[i] = q.i0 * qs; qr1[i] = q.r1 * qs; qi1[i] = q.i1 * qs;
         }
-#pragma unroll
-        for (int h = 0; h < 16; h += 8) {
-          st8(dst, off_k(t, c0 + h, 2 * N), pr + h);
-          st8(dst, off_k(t, N + c0 + h, 2 * N), pi + h);
-        }
+        st8(dst, off_k(tid, 0 * N + 0 * HN + g0, 2 * N), qr0);
+        st8(dst, off_k(tid, 0 * N + 1 * HN + g0, 2 * N), qr1);
+        st8(dst, off_k(tid, 1 * N + 0 * HN + g0, 2 * N), qi0);
+        st8(dst, off_k(tid, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
     }
     sync_for_mma();
 
-    // ---- Stage 3: U = P E / N -> TMEM cols [rt*2N, +2N).
+    // ---- Stage 3: U = Q E / N -> TMEM cols [0, 2N).
     if (tid == 0) {
       const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
-      for (int rt = 0; rt < 2; ++rt)
-        for (int ks = 0; ks < 2 * N / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::A3 + rt * L::A3_TILE + ks * 256, 128, 2 * N * 16);
-          const uint64_t bd = tc::sdesc(sbase + L::B3 + ks * 256, 128, 2 * N * 16);
-          tc::mma_f16(tmem + rt * 2 * N, ad, bd, id, ks > 0);
-        }
+#pragma unroll
+      for (int ks = 0; ks < 2 * N / 16; ++ks) {
+        const uint64_t ad = tc::sdesc(sbase + L::XB + ks * 256, 128, 2 * N * 16);
+        const uint64_t bd = tc::sdesc(sbase + L::B3 + ks * 256, 128, 2 * N * 16);
+        tc::mma_f16(tmem, ad, bd, id, ks > 0);
+      }
       tc::mma_commit(&bar);
     }
     if (!wait_mma()) break;
 
-    // ---- Stage 3 -> 4 (row tile `half`): rows (w, f_c) of U become MN-major rows (w, r), K = (Re|Im, f_c).
+    // ---- Stage 3 -> 4: row (w, c) of U becomes columns (Re|Im, c) of the MN-major rows (w, r).
     {
-      const int rt = half, m = rt * 128 + t, w = m / N, fc = m % N;
-      unsigned char* dst = sm + L::A2;
-      float v[2 * N];
+      const int w = tid / HN, c = tid % HN;
 #pragma unroll
-      for (int c0 = 0; c0 < 2 * N; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + rt * 2 * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
+      for (int part = 0; part < 2; ++part) {
+        float v[N];
 #pragma unroll
-      for (int c0 = 0; c0 < 2 * N; c0 += 8) {
-        const int k = (c0 / N) * N + fc;
-        const int mo = w * N + (c0 % N);
-        st8(dst + (mo >> 7) * L::A4_TILE, off_mn(mo & 127, k, 128), v + c0);
+        for (int c0 = 0; c0 < N; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + part * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int r0 = 0; r0 < N; r0 += 8) {
+          const int m = w * N + r0;
+          st8(sm + L::YB + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
+        }
       }
     }
     sync_for_mma();
 
-    // ---- Stage 4: c = Re(U E^T) / N -> TMEM cols [rt*N, +N).
+    // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
     if (tid == 0) {
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
+#pragma unroll
       for (int rt = 0; rt < 2; ++rt)
-        for (int ks = 0; ks < 2 * N / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::A2 + rt * L::A4_TILE + ks * 32 * 128, 128 * 16, 128);
-          const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, 2 * N * 16);
+#pragma unroll
+        for (int ks = 0; ks < N / 16; ++ks) {
+          const uint64_t ad = tc::sdesc(sbase + L::YB + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
+          const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16);
           tc::mma_f16(tmem + rt * N, ad, bd, id, ks > 0);
         }
       tc::mma_commit(&bar);
     }
     if (!wait_mma()) break;
 
-    // ---- Epilogue (row tile `half`): this thread holds map row r of window w.
-    const int rt = half, m = rt * 128 + t, w = m / N, r = m % N, i = r ^ H;
-    float rowc[N];
-    {
-      const float unscale = exp2f(-sc_exp[w]);
+    // ---- Epilogue. Row rt*128 + tid of the tile is map row r of window w
+    // (scaled by 2^-(10 - e_a - e_b)); shifted row index i = r ^ N/2.
+#pragma unroll
+    for (int rt = 0; rt < 2; ++rt) {
+      const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
       float v[N];
 #pragma unroll
       for (int c0 = 0; c0 < N; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
+      // Shifted row: column j holds lag s = j ^ N/2; lags without overlap are 0.
+      float rowc[N];
 #pragma unroll
-      for (int sc = 0; sc < N; ++sc) {
-        const int j = sc ^ H;
-        const int di = i - H, dj = j - H;
-        const bool zero_lag = di <= -SS || di >= SS || dj <= -SS || dj >= SS;
-        rowc[j] = zero_lag ? 0.f : v[sc] * unscale;
-      }
-    }
-    {
-      // Row maximum (first in column order), then the window maximum (first in
-      // row-major order of the shifted map) over the window's rows.
-      float v = rowc[0];
+      for (int j = 0; j < N; ++j) rowc[j] = (i == 0 || j == 0) ? 0.f : v[j ^ HN];
+      float best = rowc[0];
       int bj = 0;
 #pragma unroll
       for (int j = 1; j < N; ++j)
-        if (rowc[j] > v) { v = rowc[j]; bj = j; }
+        if (rowc[j] > best) { best = rowc[j]; bj = j; }
       int idx = i * N + bj;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-        if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+        if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
       }
       if (lane == 0) {
-        const int part = r / 32;  // a window spans N / 32 warps
-        pk_val[w][part] = v;
-        pk_idx[w][part] = idx;
-        if (N == 32) { pk_val[w][1] = -INFINITY; pk_idx[w][1] = 0x7fffffff; }
+        pk_val[w][r / 32] = best;
+        pk_idx[w][r / 32] = idx;
+      }
+      if (a.maps && g0 + w < total) {
+        const int ue = 10 - sc_e[0][w] - sc_e[1][w];
+        float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
+#pragma unroll
+        for (int j = 0; j < N; ++j) mo[j] = ldexpf(rowc[j], ue);
       }
     }
     __syncthreads();
     if (tid < W) {
       float v = pk_val[tid][0];
       int idx = pk_idx[tid][0];
-      if (pk_val[tid][1] > v || (pk_val[tid][1] == v && pk_idx[tid][1] < idx)) idx = pk_idx[tid][1];
+#pragma unroll
+      for (int p = 1; p < NPART; ++p)
+        if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
+          v = pk_val[tid][p];
+          idx = pk_idx[tid][p];
+        }
       pk_idx[tid][0] = idx;
     }
     __syncthreads();
-    {
-      // Neighbours of the peak: rows i-1, i, i+1 at column j, and j-1, j+1 of row i.
-      const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
-      if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1) {
-        // Masked sums keep the row in registers (an indexed read would move it
-        // to local memory); exactly one term of each sum is non-zero.
-        float vc = 0.f, vl = 0.f, vr = 0.f;
+    // Neighbours of the peak: rows i-1, i, i+1 at column j, and j-1, j+1 of row i.
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-          const float x = rowc[j];
-          vc = fmaf(j == pj ? 1.f : 0.f, x, vc);
-          vl = fmaf(j == pj - 1 ? 1.f : 0.f, x, vl);
-          vr = fmaf(j == pj + 1 ? 1.f : 0.f, x, vr);
-        }
-        if (i == pi_) {
-          nb[w][0] = vc;
-          nb[w][3] = vl;
-          nb[w][4] = vr;
-        } else if (i == pi_ - 1) {
-          nb[w][1] = vc;
-        } else {
-          nb[w][2] = vc;
+    for (int rt = 0; rt < 2; ++rt) {
+      const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
+      const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
+      const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
+      if (__any_sync(0xffffffffu, mine)) {
+        float v[N];
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+        if (mine) {
+          // Masked sums keep the row in registers; exactly one term of each is non-zero.
+          float vc = 0.f, vl = 0.f, vr = 0.f;
+#pragma unroll
+          for (int j = 0; j < N; ++j) {
+            const float x = (i == 0 || j == 0) ? 0.f : v[j ^ HN];
+            vc = fmaf(j == pj ? 1.f : 0.f, x, vc);
+            vl = fmaf(j == pj - 1 ? 1.f : 0.f, x, vl);
+            vr = fmaf(j == pj + 1 ? 1.f : 0.f, x, vr);
+          }
+          if (i == pi_) {
+            nb[w][0] = vc;
+            nb[w][3] = vl;
+            nb[w][4] = vr;
+          } else if (i == pi_ - 1) {
+            nb[w][1] = vc;
+          } else {
+            nb[w][2] = vc;
+          }
         }
       }
-    }
-    if (a.maps && g0 + w < total) {
-      float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
-#pragma unroll
-      for (int j = 0; j < N; ++j) mo[j] = rowc[j];
     }
     __syncthreads();
     if (tid < W && g0 + tid < total) {
@@ -430,7 +482,9 @@ __global__ void __launch_bounds__(256, TcThreads<SS>::MIN_BLOCKS) k_corr_tc(Corr
       const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-        float c = nb[ww][0], cd = nb[ww][1], cu = nb[ww][2], cl = nb[ww][3], cr = nb[ww][4];
+        const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
+        float c = ldexpf(nb[ww][0], ue), cd = ldexpf(nb[ww][1], ue), cu = ldexpf(nb[ww][2], ue);
+        float cl = ldexpf(nb[ww][3], ue), cr = ldexpf(nb[ww][4], ue);
         const float eps = 1e-7f;
         if (a.subpixel == PIV_SUBPIXEL_GAUSSIAN) {
           if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
@@ -449,8 +503,8 @@ __global__ void __launch_bounds__(256, TcThreads<SS>::MIN_BLOCKS) k_corr_tc(Corr
       float* uo = reinterpret_cast<float*>(a.u);
       float* vo = reinterpret_cast<float*>(a.v);
       if (win_valid[ww]) {
-        uo[g] = sub_rn(jsp, (float)H);
-        vo[g] = sub_rn(isp, (float)H);
+        uo[g] = sub_rn(jsp, (float)HN);
+        vo[g] = sub_rn(isp, (float)HN);
       } else {
         uo[g] = NAN;
         vo[g] = NAN;
@@ -472,45 +526,67 @@ bool correlate_tensor_supported(const CorrArgs& a) {
          (a.ss == 16 || a.ss == 32);
 }
 
+// CTAs per SM and the dynamic shared memory that makes exactly that many fit:
+// the occupancy API does not know about TMEM, so the shared-memory request is
+// padded until no more CTAs than the TMEM holds can be resident on one SM.
+struct TcLaunch {
+  int per_sm = 0;
+  size_t smem = 0;
+};
+
+template <int SS>
+static int tc_launch_config(TcLaunch& out) {
+  using L = TcLayout<SS>;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_corr_tc<SS>);
+  if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncGetAttributes(k_corr_tc)");
+  int smem_sm = 0, smem_optin = 0, resv = 0, regs_sm = 0;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  const size_t per_cta = L::SMEM + fa.sharedSizeBytes + resv;
+  int per_sm = 512 / L::TCOLS;
+  const int by_smem = (int)(smem_sm / per_cta);
+  const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * 4;
+  const int by_regs = regs_cta > 0 ? regs_sm / regs_cta : per_sm;
+  per_sm = std::min(per_sm, std::min(by_smem, by_regs));
+  if (per_sm < 1) return set_error(PIV_E_UNSUPPORTED, "tensor correlation does not fit on an SM");
+  size_t smem = (size_t)smem_sm / per_sm - fa.sharedSizeBytes - resv;
+  smem = std::min(smem, (size_t)smem_optin - fa.sharedSizeBytes);
+  smem = std::max(smem, L::SMEM) & ~(size_t)127;
+  if (smem < L::SMEM) smem = L::SMEM;
+  e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc)");
+  out.per_sm = per_sm;
+  out.smem = smem;
+  return PIV_OK;
+}
+
 template <int SS>
 static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
   using L = TcLayout<SS>;
   const long long total = (long long)a.n_pairs * a.m * a.n;
   if (total == 0) return PIV_OK;
+  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
   const int n_tiles = (int)((total + L::W - 1) / L::W);
-  constexpr int NT = TcThreads<SS>::NT;
   static thread_local int configured_dev = -1;
+  static thread_local TcLaunch cfg;
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_dev != dev) {
-    cudaError_t e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc)");
+    const int rc = tc_launch_config<SS>(cfg);
+    if (rc != PIV_OK) return rc;
     configured_dev = dev;
   }
-  // At most 512 TMEM columns per SM in flight: CTAs per SM = min(occupancy, 512 / TCOLS).
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_corr_tc<SS>, NT, L::SMEM);
-  const int tmem_limit = 512 / L::TCOLS;
-  if (getenv("PIV_DEBUG_LAUNCH")) {
-    cudaFuncAttributes fa;
-    cudaFuncGetAttributes(&fa, k_corr_tc<SS>);
-    int smem_sm = 0, smem_blk = 0, regs_sm = 0;
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-    fprintf(stderr, "k_corr_tc<%d>: occupancy %d/SM, tmem limit %d, regs %d, static smem %zu, dyn smem %zu, "
-            "max dyn %d, smem/SM %d, smem/block %d, regs/SM %d\n", SS, per_sm, tmem_limit, fa.numRegs,
-            fa.sharedSizeBytes, (size_t)L::SMEM, fa.maxDynamicSharedSizeBytes, smem_sm, smem_blk, regs_sm);
-  }
-  if (per_sm > tmem_limit) per_sm = tmem_limit;
-  if (per_sm < 1) return set_error(PIV_E_UNSUPPORTED, "tensor correlation does not fit on an SM");
-  int grid = sm_count() * per_sm;
+  int grid = sm_count() * cfg.per_sm;
   if (grid > n_tiles) grid = n_tiles;
-  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
-  k_corr_tc<SS><<<grid, NT, L::SMEM, stream>>>(a, a.status);
+  k_corr_tc<SS><<<grid, 128, cfg.smem, stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
 }
