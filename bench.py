@@ -172,8 +172,11 @@ class ClockSampler:
 # Roofline helpers.
 # ---------------------------------------------------------------------------
 def tc_executed_flops(ss, N):
-    """FLOPs the tensor engine executes per window pair (four dense DFT stages)."""
-    return 2 * (2 * ss * ss * 2 * N + 2 * N * 2 * ss * 2 * N + N * 2 * N * 2 * N + N * 2 * N * N)
+    """FLOPs the tensor engine executes per window pair: packed real DFT along x
+    (both frames), along y (both frames), complex inverse along f_r over N/2
+    packed columns, real inverse along f_c."""
+    macs = 2 * ss * ss * N + 2 * N * ss * N + (N // 2) * (2 * N) * (2 * N) + N * N * N
+    return 2 * macs
 
 
 def corr_flops(ss, N):
@@ -375,7 +378,7 @@ def run_gpu(args):
     achieved = flops / (corr[dom] * 1e-3) / 1e12
     peaks = measured_peaks()
     traffic_w = ncu_traffic()
-    on_tensor = args.dft == "tensor" and N == 2 * f.search_size and f.search_size in (16, 32)
+    on_tensor = args.dft == "tensor" and N == 2 * f.search_size and f.search_size in (16, 32, 64)
     if on_tensor:
         peak = peaks.get("bf16_tflops", 1900.0)
         unit, bound = "TFLOP/s", "tensor"

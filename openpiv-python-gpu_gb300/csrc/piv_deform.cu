@@ -17,6 +17,8 @@
 // operations in the order the host oracle uses.
 #include <math.h>
 
+#include <algorithm>
+
 #include "piv_common.cuh"
 #include "piv_internal.h"
 
@@ -40,28 +42,6 @@ struct GridAxis {
   int spacing, len;
 };
 
-PIV_D double grid_interp(const double* v, int n, const GridAxis& ay, const GridAxis& ax, double yq, double xq) {
-  const int iy = grid_interval(yq, ay.g0, ay.spacing, ay.len);
-  const int ix = grid_interval(xq, ax.g0, ax.spacing, ax.len);
-  const double y0 = ay.g0 + (double)iy * ay.spacing, y1 = ay.g0 + (double)(iy + 1) * ay.spacing;
-  const double x0 = ax.g0 + (double)ix * ax.spacing, x1 = ax.g0 + (double)(ix + 1) * ax.spacing;
-  if (ay.len < 2 || ax.len < 2) {
-    // Degenerate one-point axis: constant along it.
-    const int jy = ay.len < 2 ? 0 : iy, jx = ax.len < 2 ? 0 : ix;
-    return v[jy * n + jx];
-  }
-  const double ty = __ddiv_rn(__dsub_rn(yq, y0), __dsub_rn(y1, y0));
-  const double tx = __ddiv_rn(__dsub_rn(xq, x0), __dsub_rn(x1, x0));
-  const double v00 = v[iy * n + ix], v01 = v[iy * n + ix + 1];
-  const double v10 = v[(iy + 1) * n + ix], v11 = v[(iy + 1) * n + ix + 1];
-  const double oy = __dsub_rn(1.0, ty), ox = __dsub_rn(1.0, tx);
-  const double t1 = __dmul_rn(__dmul_rn(v00, oy), ox);
-  const double t2 = __dmul_rn(__dmul_rn(v01, oy), tx);
-  const double t3 = __dmul_rn(__dmul_rn(v10, ty), ox);
-  const double t4 = __dmul_rn(__dmul_rn(v11, ty), tx);
-  return __dadd_rn(__dadd_rn(__dadd_rn(t1, t2), t3), t4);
-}
-
 PIV_HD GridAxis axis_x(const piv_geometry& g) {
   return GridAxis{(double)g.search_size * 0.5 + g.x_offset, g.spacing, g.n};
 }
@@ -69,28 +49,72 @@ PIV_HD GridAxis axis_y(const piv_geometry& g) {
   return GridAxis{(double)g.search_size * 0.5 + g.y_offset, g.spacing, g.m};
 }
 
-__global__ void k_regrid(piv_geometry src, piv_geometry dst, int n_pairs, const double* __restrict__ u_src,
-                         const double* __restrict__ v_src, double* __restrict__ u_dst, double* __restrict__ v_dst) {
-  const long long npts = (long long)dst.m * dst.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npts * n_pairs) return;
-  const int pair = (int)(t / npts);
-  const int k = (int)(t % npts);
-  const int i = k / dst.n, j = k % dst.n;
-  const double yq = grid_coord(i, dst.spacing, dst.search_size, dst.y_offset);
-  const double xq = grid_coord(j, dst.spacing, dst.search_size, dst.x_offset);
+// RegularGridInterpolator's linear rule in float64, one separate IEEE
+// operation at a time in the host oracle's order. One CTA per (destination
+// row, group of pairs): the column weights of the row are computed once into
+// shared memory and reused for every pair, so the per-point work is four
+// loads and the bilinear sum.
+static constexpr int kRegridPairGroups = 8;
+static constexpr int kRegridMaxCols = 4096;
+
+__global__ void __launch_bounds__(128) k_regrid(piv_geometry src, piv_geometry dst, int n_pairs,
+                                                const double* __restrict__ u_src, const double* __restrict__ v_src,
+                                                double* __restrict__ u_dst, double* __restrict__ v_dst) {
+  __shared__ int s_ix[kRegridMaxCols];
+  __shared__ double s_tx[kRegridMaxCols];
+  const int i = blockIdx.x;
   const GridAxis ay = axis_y(src), ax = axis_x(src);
-  const long long so = (long long)pair * src.m * src.n;
-  u_dst[t] = grid_interp(u_src + so, src.n, ay, ax, yq, xq);
-  v_dst[t] = grid_interp(v_src + so, src.n, ay, ax, yq, xq);
+  for (int j = threadIdx.x; j < dst.n; j += blockDim.x) {
+    const double xq = grid_coord(j, dst.spacing, dst.search_size, dst.x_offset);
+    const int ix = grid_interval(xq, ax.g0, ax.spacing, ax.len);
+    const double x0 = ax.g0 + (double)ix * ax.spacing, x1 = ax.g0 + (double)(ix + 1) * ax.spacing;
+    s_ix[j] = ix;
+    s_tx[j] = __ddiv_rn(__dsub_rn(xq, x0), __dsub_rn(x1, x0));
+  }
+  const double yq = grid_coord(i, dst.spacing, dst.search_size, dst.y_offset);
+  const int iy = grid_interval(yq, ay.g0, ay.spacing, ay.len);
+  const double y0 = ay.g0 + (double)iy * ay.spacing, y1 = ay.g0 + (double)(iy + 1) * ay.spacing;
+  const double ty = __ddiv_rn(__dsub_rn(yq, y0), __dsub_rn(y1, y0));
+  const double oy = __dsub_rn(1.0, ty);
+  __syncthreads();
+  const bool degenerate = ay.len < 2 || ax.len < 2;
+  const int n = src.n;
+  const long long src_sz = (long long)src.m * src.n, dst_sz = (long long)dst.m * dst.n;
+  for (int pair = blockIdx.y; pair < n_pairs; pair += gridDim.y) {
+    const double* us = u_src + pair * src_sz;
+    const double* vs = v_src + pair * src_sz;
+    const long long o = pair * dst_sz + (long long)i * dst.n;
+    for (int j = threadIdx.x; j < dst.n; j += blockDim.x) {
+      const int ix = s_ix[j];
+      if (degenerate) {
+        const int jy = ay.len < 2 ? 0 : iy, jx = ax.len < 2 ? 0 : ix;
+        u_dst[o + j] = us[jy * n + jx];
+        v_dst[o + j] = vs[jy * n + jx];
+        continue;
+      }
+      const double tx = s_tx[j], ox = __dsub_rn(1.0, tx);
+      const int k00 = iy * n + ix;
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        const double* v = f == 0 ? us : vs;
+        const double v00 = v[k00], v01 = v[k00 + 1], v10 = v[k00 + n], v11 = v[k00 + n + 1];
+        const double t1 = __dmul_rn(__dmul_rn(v00, oy), ox);
+        const double t2 = __dmul_rn(__dmul_rn(v01, oy), tx);
+        const double t3 = __dmul_rn(__dmul_rn(v10, ty), ox);
+        const double t4 = __dmul_rn(__dmul_rn(v11, ty), tx);
+        (f == 0 ? u_dst : v_dst)[o + j] = __dadd_rn(__dadd_rn(__dadd_rn(t1, t2), t3), t4);
+      }
+    }
+  }
 }
 
 int regrid(const piv_geometry& src, const piv_geometry& dst, int n_pairs, const double* u_src, const double* v_src,
            double* u_dst, double* v_dst, cudaStream_t stream) {
-  const long long total = (long long)dst.m * dst.n * n_pairs;
-  if (total == 0) return PIV_OK;
-  const int bs = 256;
-  k_regrid<<<(unsigned)((total + bs - 1) / bs), bs, 0, stream>>>(src, dst, n_pairs, u_src, v_src, u_dst, v_dst);
+  if ((long long)dst.m * dst.n * n_pairs == 0) return PIV_OK;
+  if (dst.n > kRegridMaxCols) return set_error(PIV_E_UNSUPPORTED, "regrid: more than %d field columns", kRegridMaxCols);
+  if (dst.m > 2147483647 || n_pairs < 1) return set_error(PIV_E_ARG, "regrid: bad field size");
+  const dim3 grid((unsigned)dst.m, (unsigned)std::min(n_pairs, kRegridPairGroups));
+  k_regrid<<<grid, 128, 0, stream>>>(src, dst, n_pairs, u_src, v_src, u_dst, v_dst);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_regrid launch");
 }
@@ -134,7 +158,9 @@ PIV_D void bspline3_weights(float t, float* w) {
   w[3] = t3 * (1.0f / 6.0f);
 }
 
-// Cubic B-spline sample of the coefficient frame at (yi, xi) clamped into the frame.
+// Cubic B-spline sample of the coefficient frame at (yi, xi) clamped into the
+// frame. Taps inside the frame are read directly; the mirror rule is only
+// evaluated for samples whose 4 x 4 support crosses an edge.
 PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi, float yi) {
   xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
   yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
@@ -143,17 +169,31 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
   bspline3_weights(xi - fx, wx);
   bspline3_weights(yi - fy, wy);
   const int x0 = (int)fx - 1, y0 = (int)fy - 1;
+  float acc = 0.0f;
+  if (x0 >= 0 && x0 + 3 < W && y0 >= 0 && y0 + 3 < H) {
+    const float* p = coef + (long long)y0 * W + x0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float* row = p + (long long)r * W;
+      float s = wx[0] * __ldg(row);
+      s = fmaf(wx[1], __ldg(row + 1), s);
+      s = fmaf(wx[2], __ldg(row + 2), s);
+      s = fmaf(wx[3], __ldg(row + 3), s);
+      acc = fmaf(wy[r], s, acc);
+    }
+    return acc;
+  }
   int cx[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) cx[c] = mirror_index(x0 + c, W);
-  float acc = 0.0f;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const float* row = coef + (long long)mirror_index(y0 + r, H) * W;
-    float s = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) s += wx[c] * __ldg(row + cx[c]);
-    acc += wy[r] * s;
+    float s = wx[0] * __ldg(row + cx[0]);
+    s = fmaf(wx[1], __ldg(row + cx[1]), s);
+    s = fmaf(wx[2], __ldg(row + cx[2]), s);
+    s = fmaf(wx[3], __ldg(row + cx[3]), s);
+    acc = fmaf(wy[r], s, acc);
   }
   return acc;
 }
@@ -175,28 +215,40 @@ PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
   return AxisWeight{i, t};
 }
 
-// Bilinear predictor value from four float64 field values, in float32.
-PIV_D float lerp2(const double* v, int n, const AxisWeight& wy, const AxisWeight& wx, int my, int nx) {
-  const int iy1 = my < 2 ? wy.i : wy.i + 1, ix1 = nx < 2 ? wx.i : wx.i + 1;
-  const float v00 = (float)__ldg(v + wy.i * n + wx.i), v01 = (float)__ldg(v + wy.i * n + ix1);
-  const float v10 = (float)__ldg(v + iy1 * n + wx.i), v11 = (float)__ldg(v + iy1 * n + ix1);
-  const float top = fmaf(wx.t, v01 - v00, v00);
-  const float bot = fmaf(wx.t, v11 - v10, v10);
-  return fmaf(wy.t, bot - top, top);
-}
+static constexpr int kDeformThreads = 256;
+// Field columns one CTA of kDeformThreads pixels can touch (spacing >= 1).
+static constexpr int kDeformMaxCols = kDeformThreads + 2;
 
-// One thread per pixel: predictor at the pixel (float32; the reference
-// evaluates it in float64 and casts to the frame type, a difference of one or
-// two float32 ulps), then frame A sampled at x + up*dta and frame B at
-// x + up*dtb.
-// Launch grid: x over the columns of a row, y over rows, z over pairs.
+// One thread per pixel of one row segment. The predictor (float32; the
+// reference evaluates it in float64 and casts to the frame type, a difference
+// of one or two float32 ulps) is interpolated along y once per field column
+// into shared memory, then along x per pixel. Frame A is sampled at
+// x + up*dta and frame B at x + up*dtb.
+// Launch grid: x over row segments, y over rows, z over pairs.
 template <typename T>
-__global__ void k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
+__global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
+  __shared__ float su[kDeformMaxCols], sv[kDeformMaxCols];
   const piv_geometry& g = a.geom;
   const int H = g.height, W = g.width;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= W) return;
+  const int j0 = blockIdx.x * kDeformThreads;
+  const int j = j0 + threadIdx.x;
   const int i = blockIdx.y, pair = blockIdx.z;
+  const AxisWeight wy = axis_weight(i, g.search_size, g.y_offset, g.spacing, g.m);
+  const int k_lo = axis_weight(j0, g.search_size, g.x_offset, g.spacing, g.n).i;
+  const int j_last = min(j0 + kDeformThreads, W) - 1;
+  const int k_hi = min(axis_weight(j_last, g.search_size, g.x_offset, g.spacing, g.n).i + 1, g.n - 1);
+  const long long fo = (long long)pair * g.m * g.n;
+  const int iy1 = g.m < 2 ? wy.i : wy.i + 1;
+  for (int k = k_lo + threadIdx.x; k <= k_hi; k += kDeformThreads) {
+    const double* u = a.up + fo;
+    const double* v = a.vp + fo;
+    const float u0 = (float)__ldg(u + wy.i * g.n + k), u1 = (float)__ldg(u + iy1 * g.n + k);
+    const float v0 = (float)__ldg(v + wy.i * g.n + k), v1 = (float)__ldg(v + iy1 * g.n + k);
+    su[k - k_lo] = fmaf(wy.t, u1 - u0, u0);
+    sv[k - k_lo] = fmaf(wy.t, v1 - v0, v0);
+  }
+  __syncthreads();
+  if (j >= W) return;
   const long long npix = (long long)H * W;
   const long long p = (long long)i * W + j;
   const long long base = (long long)pair * npix;
@@ -208,12 +260,11 @@ __global__ void k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
     out_b[t] = (T)0;
     return;
   }
-  const AxisWeight wy = axis_weight(i, g.search_size, g.y_offset, g.spacing, g.m);
   const AxisWeight wx = axis_weight(j, g.search_size, g.x_offset, g.spacing, g.n);
-  const long long fo = (long long)pair * g.m * g.n;
+  const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
   const T x = (T)j, y = (T)i;
-  const T up = (T)lerp2(a.up + fo, g.n, wy, wx, g.m, g.n);
-  const T vp = (T)lerp2(a.vp + fo, g.n, wy, wx, g.m, g.n);
+  const T up = (T)fmaf(wx.t, su[c1] - su[c0], su[c0]);
+  const T vp = (T)fmaf(wx.t, sv[c1] - sv[c0], sv[c0]);
   if (do_a) {
     const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
     out_a[t] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
@@ -235,6 +286,7 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   if (total == 0) return PIV_OK;
   if (a.order == 3 && (!a.coef_a || !a.coef_b))
     return set_error(PIV_E_ARG, "cubic deformation needs spline coefficient frames");
+  if (a.geom.spacing < 1) return set_error(PIV_E_ARG, "deformation: spacing must be >= 1");
   const double dp = a.deforming_par;
   double dta = 0, dtb = 0;
   int do_a = 0, do_b = 0;
@@ -243,159 +295,131 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   else { dta = -1; do_a = 1; }
   if (a.geom.height > 65535 || a.n_pairs > 65535)
     return set_error(PIV_E_UNSUPPORTED, "deformation grid limit (height and pairs <= 65535)");
-  const int bs = 256;
-  const dim3 grid((unsigned)((a.geom.width + bs - 1) / bs), (unsigned)a.geom.height, (unsigned)a.n_pairs);
+  const dim3 grid((unsigned)((a.geom.width + kDeformThreads - 1) / kDeformThreads), (unsigned)a.geom.height,
+                  (unsigned)a.n_pairs);
   if (a.dtype == PIV_DTYPE_F64)
-    k_deform<double><<<grid, bs, 0, stream>>>(a, dta, dtb, do_a, do_b);
+    k_deform<double><<<grid, kDeformThreads, 0, stream>>>(a, dta, dtb, do_a, do_b);
   else
-    k_deform<float><<<grid, bs, 0, stream>>>(a, (float)dta, (float)dtb, do_a, do_b);
+    k_deform<float><<<grid, kDeformThreads, 0, stream>>>(a, (float)dta, (float)dtb, do_a, do_b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_deform launch");
 }
 
 // ---------------------------------------------------------------------------
-// Cubic B-spline prefilter (one pole z = sqrt(3) - 2, gain 6 per axis),
-// mirror boundary, axis 0 then axis 1.
+// Cubic B-spline prefilter, mirror boundary. The exact prefilter (inverse of
+// the sampled cubic B-spline, one pole z = sqrt(3) - 2) is the symmetric
+// filter h[k] = sqrt(3) z^|k| applied to the mirror-extended frame. It runs
+// here as a separable FIR truncated at |k| <= 12: the dropped taps weigh
+// 2 sqrt(3) |z|^13 / (1 - |z|) < 2e-7 of the signal in total, below float32
+// rounding of the recursive form.
 // ---------------------------------------------------------------------------
-static constexpr float kPole = -0.26794919243112270f;  // sqrt(3) - 2
-static constexpr int kHorizon = 24;                     // |z|^24 < 2e-14
+static constexpr int kFirK = 12;
+struct FirTaps {
+  float h[2 * kFirK + 1];
+};
+constexpr FirTaps make_fir_taps() {
+  FirTaps t{};
+  double zk = 1.0;
+  for (int k = 0; k <= kFirK; ++k) {
+    t.h[kFirK + k] = (float)(1.7320508075688772 * zk);
+    t.h[kFirK - k] = t.h[kFirK + k];
+    zk *= -0.2679491924311227;
+  }
+  return t;
+}
+__constant__ FirTaps c_fir = make_fir_taps();
 
-// Causal initial value for the mirror boundary over n samples read by get(k).
-template <class Get>
-PIV_D float causal_init_mirror(Get get, int n) {
-  const float z = kPole;
-  if (n == 1) return get(0);
-  if (n > kHorizon) {
-    float zk = 1.0f, s = 0.0f;
-    for (int k = 0; k < kHorizon; ++k) { s += zk * get(k); zk *= z; }
-    return s;
-  }
-  // Exact sum over the mirrored sequence.
-  const float zn = powf(z, (float)(n - 1));
-  float s = get(0) + zn * get(n - 1);
-  float zk = z;
-  const float z2n = zn * zn;
-  for (int k = 1; k < n - 1; ++k) {
-    s += (zk + z2n / zk) * get(k);
-    zk *= z;
-  }
-  return s / (1.0f - z2n);
+// Mirror ('d c b | a b c d | c b a') index for any integer q.
+PIV_D int mirror_any(int q, int n) {
+  if (n == 1) return 0;
+  const int p = 2 * n - 2;
+  q %= p;
+  if (q < 0) q += p;
+  return q < n ? q : p - q;
 }
 
-// Column pass (axis 0): one thread per (frame, column); reads `in` of pixel
-// type (or float when in_f is set), writes out.
-__global__ void k_prefilter_cols(int H, int W, int n_frames, const void* in, int pixel_type, float* out) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n_frames * W) return;
-  const int f = (int)(t / W), x = (int)(t % W);
-  const long long base = (long long)f * H * W + x;
-  const float z = kPole, gain = 6.0f;
-  auto get = [&](int k) { return gain * load_pixel<float>(in, pixel_type, base + (long long)k * W); };
-  float c = causal_init_mirror(get, H);
-  out[base] = c;
-  for (int k = 1; k < H; ++k) {
-    c = get(k) + z * c;
-    out[base + (long long)k * W] = c;
-  }
-  if (H == 1) return;
-  const float cm2 = out[base + (long long)(H - 2) * W];
-  float a = (z / (z * z - 1.0f)) * (c + z * cm2);
-  out[base + (long long)(H - 1) * W] = a;
-  for (int k = H - 2; k >= 0; --k) {
-    a = z * (a - out[base + (long long)k * W]);
-    out[base + (long long)k * W] = a;
-  }
-}
+static constexpr int kPfTx = 64, kPfTy = 32;
+static constexpr int kPfRy = kPfTy + 2 * kFirK, kPfRx = kPfTx + 2 * kFirK;
+static constexpr int kPfRxS = kPfRx + 1, kPfTxS = kPfTx + 1;  // odd strides: conflict-free column access
 
-// Row pass (axis 1), in place on `io`: a warp filters 32 rows, staging 32 x 32
-// tiles through shared memory so global accesses stay coalesced.
-__global__ void k_prefilter_rows(int H, int W, int n_frames, float* io) {
-  __shared__ float tile[4][32][33];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long row0 = ((long long)blockIdx.x * 4 + warp) * 32;  // global row index over all frames
-  const long long n_rows = (long long)n_frames * H;
-  if (row0 >= n_rows) return;
-  float(*tl)[33] = tile[warp];
-  const float z = kPole, gain = 6.0f;
-  const long long my_row = row0 + lane;
-  const bool active = my_row < n_rows;
-  float* rowp = io + (active ? my_row : row0) * W;
-  const int n_chunks = (W + 31) / 32;
-  // Causal pass.
-  float c = 0.0f;
-  for (int ch = 0; ch < n_chunks; ++ch) {
-    const int x0 = ch * 32;
-    for (int r = 0; r < 32; ++r) {
-      const long long gr = row0 + r;
-      tl[r][lane] = (gr < n_rows && x0 + lane < W) ? io[gr * W + x0 + lane] * gain : 0.0f;
+// One CTA per 32 x 64 output tile of one frame: the tile and a 12-pixel
+// mirrored halo go to shared memory, the row FIR runs over every halo row,
+// then the column FIR writes the tile. P is the pixel type; the halo loads are
+// unrolled so that all of a thread's loads are in flight together.
+template <typename P>
+__global__ void __launch_bounds__(256) k_prefilter_fir(int H, int W, const P* __restrict__ in,
+                                                       float* __restrict__ out) {
+  __shared__ float reg[kPfRy * kPfRxS];
+  __shared__ float tmp[kPfRy * kPfTxS];
+  const int x0 = blockIdx.x * kPfTx, y0 = blockIdx.y * kPfTy;
+  const long long fbase = (long long)blockIdx.z * H * W;
+  constexpr int kLoads = (kPfRy * kPfRx + 255) / 256;
+  float vals[kLoads];
+#pragma unroll
+  for (int u = 0; u < kLoads; ++u) {
+    const int e = threadIdx.x + 256 * u;
+    vals[u] = 0.f;
+    if (e < kPfRy * kPfRx) {
+      const int ry = e / kPfRx, rx = e % kPfRx;
+      int gy = y0 - kFirK + ry, gx = x0 - kFirK + rx;
+      if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
+      if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
+      vals[u] = (float)__ldg(in + fbase + (long long)gy * W + gx);
     }
-    __syncwarp();
-    if (active) {
-      int k0 = 0;
-      if (ch == 0) {
-        auto get = [&](int k) { return k < 32 ? tl[lane][k] : rowp[k] * gain; };
-        c = causal_init_mirror(get, W);
-        tl[lane][0] = c;
-        k0 = 1;
-      }
-      for (int k = k0; k < 32 && x0 + k < W; ++k) {
-        c = tl[lane][k] + z * c;
-        tl[lane][k] = c;
-      }
-    }
-    __syncwarp();
-    for (int r = 0; r < 32; ++r) {
-      const long long gr = row0 + r;
-      if (gr < n_rows && x0 + lane < W) io[gr * W + x0 + lane] = tl[r][lane];
-    }
-    __syncwarp();
   }
-  if (W == 1) return;
-  // Anti-causal pass.
-  float a = 0.0f;
-  for (int ch = n_chunks - 1; ch >= 0; --ch) {
-    const int x0 = ch * 32;
-    for (int r = 0; r < 32; ++r) {
-      const long long gr = row0 + r;
-      tl[r][lane] = (gr < n_rows && x0 + lane < W) ? io[gr * W + x0 + lane] : 0.0f;
+#pragma unroll
+  for (int u = 0; u < kLoads; ++u) {
+    const int e = threadIdx.x + 256 * u;
+    if (e < kPfRy * kPfRx) reg[(e / kPfRx) * kPfRxS + e % kPfRx] = vals[u];
+  }
+  __syncthreads();
+  // Row FIR: item = (segment of 8 outputs, halo row); a warp's lanes take consecutive rows.
+  for (int it = threadIdx.x; it < kPfRy * (kPfTx / 8); it += 256) {
+    const int r = it % kPfRy, c0 = (it / kPfRy) * 8;
+    const float* src = reg + r * kPfRxS + c0;
+    float v[8 + 2 * kFirK];
+#pragma unroll
+    for (int k = 0; k < 8 + 2 * kFirK; ++k) v[k] = src[k];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k <= 2 * kFirK; ++k) acc = fmaf(c_fir.h[k], v[o + k], acc);
+      tmp[r * kPfTxS + c0 + o] = acc;
     }
-    __syncwarp();
-    if (active) {
-      int k = (ch == n_chunks - 1) ? (W - 1 - x0) : 31;
-      if (ch == n_chunks - 1) {
-        const float cl = tl[lane][k];
-        const float cm2 = k >= 1 ? tl[lane][k - 1] : rowp[W - 2];
-        a = (z / (z * z - 1.0f)) * (cl + z * cm2);
-        tl[lane][k] = a;
-        --k;
-      }
-      for (; k >= 0; --k) {
-        a = z * (a - tl[lane][k]);
-        tl[lane][k] = a;
-      }
+  }
+  __syncthreads();
+  // Column FIR: item = (column, segment of 8 output rows); lanes take consecutive columns.
+  for (int it = threadIdx.x; it < kPfTx * (kPfTy / 8); it += 256) {
+    const int c = it % kPfTx, r0 = (it / kPfTx) * 8;
+    float v[8 + 2 * kFirK];
+#pragma unroll
+    for (int k = 0; k < 8 + 2 * kFirK; ++k) v[k] = tmp[(r0 + k) * kPfTxS + c];
+    const int gx = x0 + c;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k <= 2 * kFirK; ++k) acc = fmaf(c_fir.h[k], v[o + k], acc);
+      const int gy = y0 + r0 + o;
+      if (gx < W && gy < H) out[fbase + (long long)gy * W + gx] = acc;
     }
-    __syncwarp();
-    for (int r = 0; r < 32; ++r) {
-      const long long gr = row0 + r;
-      if (gr < n_rows && x0 + lane < W) io[gr * W + x0 + lane] = tl[r][lane];
-    }
-    __syncwarp();
   }
 }
 
 int spline_prefilter(int H, int W, int n_frames, const void* frames, int pixel_type, float* coef,
                      cudaStream_t stream) {
   if ((long long)H * W * n_frames == 0) return PIV_OK;
-  const int bs = 128;
-  const long long ncols = (long long)n_frames * W;
-  k_prefilter_cols<<<(unsigned)((ncols + bs - 1) / bs), bs, 0, stream>>>(H, W, n_frames, frames, pixel_type, coef);
+  if (n_frames > 65535) return set_error(PIV_E_UNSUPPORTED, "spline prefilter: more than 65535 frames");
+  const dim3 grid((unsigned)((W + kPfTx - 1) / kPfTx), (unsigned)((H + kPfTy - 1) / kPfTy), (unsigned)n_frames);
+  switch (pixel_type) {
+    case PIV_PIXEL_U8: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const uint8_t*)frames, coef); break;
+    case PIV_PIXEL_U16: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const uint16_t*)frames, coef); break;
+    case PIV_PIXEL_F32: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const float*)frames, coef); break;
+    default: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const double*)frames, coef); break;
+  }
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return set_cuda_error(e, "k_prefilter_cols launch");
-  const long long nrows = (long long)n_frames * H;
-  const long long nblocks = (nrows + 127) / 128;
-  k_prefilter_rows<<<(unsigned)nblocks, 128, 0, stream>>>(H, W, n_frames, coef);
-  e = cudaGetLastError();
-  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_prefilter_rows launch");
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_prefilter_fir launch");
 }
 
 }  // namespace piv

@@ -84,6 +84,30 @@ PIV_D void sth(unsigned char* base, uint32_t off, float v) {
 // 2^e for |e| <= 126.
 PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
 
+// CNT consecutive pixels of one window row as float; the pixel type is
+// resolved once, outside the unrolled loads, so that all of them are in flight
+// together.
+template <typename P, int CNT>
+PIV_D void load_row_t(const void* frame, long long off, float (&r)[CNT]) {
+  const P* p = reinterpret_cast<const P*>(frame) + off;
+#pragma unroll
+  for (int x = 0; x < CNT; ++x) r[x] = (float)__ldg(p + x);
+}
+template <int CNT>
+PIV_D void load_row(const void* frame, int pixel_type, long long off, bool ok, float (&r)[CNT]) {
+  if (!ok) {
+#pragma unroll
+    for (int x = 0; x < CNT; ++x) r[x] = 0.f;
+    return;
+  }
+  switch (pixel_type) {
+    case PIV_PIXEL_U8: load_row_t<uint8_t>(frame, off, r); break;
+    case PIV_PIXEL_U16: load_row_t<uint16_t>(frame, off, r); break;
+    case PIV_PIXEL_F32: load_row_t<float>(frame, off, r); break;
+    default: load_row_t<double>(frame, off, r); break;
+  }
+}
+
 static constexpr uint32_t kMaxPolls = 1u << 24;
 
 // Product of one frequency pair: the outputs at f_r = g (q0) and f_r = N - g
@@ -218,12 +242,10 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       for (int f = 0; f < 2; ++f) {
         const void* frame = f == 0 ? a.frame_a : a.frame_b;
         float r[SS];
+        load_row(frame, a.pixel_type, rowoff, ok, r);
         float sum = 0.f;
 #pragma unroll
-        for (int x = 0; x < SS; ++x) {
-          r[x] = ok ? load_pixel<float>(frame, a.pixel_type, rowoff + x) : 0.f;
-          sum += r[x];
-        }
+        for (int x = 0; x < SS; ++x) sum += r[x];
         // Window sums over its SS rows (a window's lanes are contiguous, SS | 32).
 #pragma unroll
         for (int o = 1; o < SS; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
@@ -521,9 +543,480 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
   if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
 }
 
+// ---------------------------------------------------------------------------
+// 64-pixel windows (N = 128). The operands and constants need 208 KB of shared
+// memory and the stage-2 spectra all 512 TMEM columns, so one CTA runs per SM
+// with 512 threads, four per TMEM lane (warp w reads lanes 32 (w % 4)); each
+// phase splits its columns (or frames) between the four. The four operand
+// tiles live one after the other in a single 64 KB region: each phase writes
+// its operand only after the previous product has completed. Stage 3 uses
+// E = [[C, -S], [S, C]] / N from three 128 x 128 blocks instead of the full
+// 256 x 256 matrix.
+// ---------------------------------------------------------------------------
+struct Tc64 {
+  static constexpr int SS = 64, N = 128, HN = 64, W = 2, NT = 512, TCOLS = 512;
+  static constexpr int B1 = 0;                  // F [N][SS] K-major
+  static constexpr int BC = B1 + N * SS * 2;    // cos / N   [N][N] K-major, K = (b, g)
+  static constexpr int BS = BC + N * N * 2;     // sin / N
+  static constexpr int BNS = BS + N * N * 2;    // -sin / N
+  static constexpr int B4 = BNS + N * N * 2;    // [N][N] K-major, K = (part, c)
+  static constexpr int OP = B4 + N * N * 2;     // operand region
+  static constexpr int END = OP + 65536;
+  static constexpr int A1_BYTES = 128 * SS * 2; // per frame, K-major [128][SS]
+  static constexpr int A2_BYTES = 128 * SS * 2; // per (frame, tile), MN-major [128][SS]
+  static constexpr int A4_BYTES = 128 * N * 2;  // per tile, MN-major [128][N]
+  static constexpr size_t SMEM = END + 128;
+};
+
+__global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
+  using L = Tc64;
+  constexpr int SS = L::SS, N = L::N, HN = L::HN, W = L::W;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ float tw_re[N], tw_im[N];
+  __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
+  __shared__ int sc_e[2][W];
+  __shared__ long long win_base[W];
+  __shared__ int win_valid[W];
+  __shared__ float pk_val[W][8];
+  __shared__ int pk_idx[W][8];
+  __shared__ float nb[W][5][2];      // c, cd, cu, cl, cr (scaled) per column half
+
+  const int tid = threadIdx.x;
+  const int q = tid >> 7, t = tid & 127;
+  const int warp = tid >> 5, lane = tid & 31;
+  const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
+
+  for (int k = tid; k < N; k += L::NT) {
+    float sn, cs;
+    sincospif(2.0f * (float)k / (float)N, &sn, &cs);
+    tw_re[k] = cs;
+    tw_im[k] = -sn;
+  }
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  const float inv_n = 1.0f / (float)N;
+  const int p0 = SS / 2;
+  for (int e = tid; e < N * SS; e += L::NT) {  // F[k][x]
+    const int k = e / SS, x = e % SS, f = k >> 1, qq = (f * (x + p0)) % N;
+    float v;
+    if (k == 0) v = 1.0f;
+    else if (k == 1) v = ((x + p0) & 1) ? -1.0f : 1.0f;
+    else v = (k & 1) ? tw_im[qq] : tw_re[qq];
+    sth(sm + L::B1, off_k(k, x, SS), v);
+  }
+  for (int e = tid; e < N * N; e += L::NT) {  // C, S, -S [r][kappa = (b, g)]
+    const int r = e / N, kap = e % N, b = kap / HN, g = kap % HN;
+    const int fr = b == 0 ? g : (g == 0 ? HN : N - g);
+    const int qq = (fr * r) % N;
+    const float cs = tw_re[qq] * inv_n, sn = -tw_im[qq] * inv_n;
+    sth(sm + L::BC, off_k(r, kap, N), cs);
+    sth(sm + L::BS, off_k(r, kap, N), sn);
+    sth(sm + L::BNS, off_k(r, kap, N), -sn);
+  }
+  for (int e = tid; e < N * N; e += L::NT) {  // B4[s][kappa = (part, c)]
+    const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
+    const int qq = (c * s_) % N;
+    float v;
+    if (c == 0) v = part == 0 ? inv_n : ((s_ & 1) ? -inv_n : inv_n);
+    else v = part == 0 ? 2.0f * tw_re[qq] * inv_n : 2.0f * tw_im[qq] * inv_n;
+    sth(sm + L::B4, off_k(s_, kap, N), v);
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base_s, L::TCOLS);
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base_s;
+  const uint32_t sbase = tc::smem_u32(sm);
+  uint32_t phase = 0;
+
+  const int sp = a.spacing, nf = a.n;
+  const int n_wins = a.m * a.n;
+  const long long total = (long long)a.n_pairs * n_wins;
+  const int n_tiles = (int)((total + W - 1) / W);
+  const long long frame_elems = (long long)a.height * a.width;
+
+  auto wait_mma = [&]() -> bool {
+    bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
+    phase ^= 1u;
+    ok = __syncthreads_and(ok);
+    if (!ok && tid == 0) atomicExch(status, PIV_E_TIMEOUT);
+    tc::fence_after_sync();
+    return ok;
+  };
+  auto sync_for_mma = [&]() {
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  };
+
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const long long g0 = (long long)tile * W;
+    if (tid < W) {
+      const long long g = g0 + tid;
+      int ok = g < total;
+      long long base = 0;
+      if (ok) {
+        const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
+        if (a.win_mask) ok = a.win_mask[k] == 0;
+        base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
+      }
+      win_valid[tid] = ok;
+      win_base[tid] = base;
+    }
+    __syncthreads();
+
+    // ---- Staging: thread (q, t) loads half h = q >> 1 of row y of window w of frame f = q & 1.
+    {
+      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63, grp = h * 2 + ((t >> 5) & 1);
+      const bool ok = win_valid[w] != 0;
+      const void* frame = f == 0 ? a.frame_a : a.frame_b;
+      const long long rowoff = win_base[w] + (long long)y * a.width + 32 * h;
+      float r[32];
+      load_row(frame, a.pixel_type, rowoff, ok, r);
+      float sum = 0.f;
+#pragma unroll
+      for (int x = 0; x < 32; ++x) sum += r[x];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) red[f][w][grp] = sum;
+      __syncthreads();
+      const float mean = (red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3]) / (float)(SS * SS);
+      float l = 0.f;
+#pragma unroll
+      for (int x = 0; x < 32; ++x) {
+        r[x] -= mean;
+        l += fabsf(r[x]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+      __syncthreads();
+      if (lane == 0) red[f][w][grp] = l;
+      __syncthreads();
+      const float l1 = red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3];
+      int e = 0;
+      if (l1 > 0.f) e = min(120, max(-120, 11 - ilogbf(l1)));
+      const float s = pow2i(e);
+#pragma unroll
+      for (int x = 0; x < 32; ++x) r[x] *= s;
+      if (h == 0 && y == 0) sc_e[f][w] = e;
+#pragma unroll
+      for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
+    }
+    sync_for_mma();
+
+    // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
+    if (tid == 0) {
+      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
+        for (int ks = 0; ks < SS / 16; ++ks) {
+          const uint64_t ad = tc::sdesc(sbase + L::OP + f * L::A1_BYTES + ks * 256, 128, SS * 16);
+          const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
+          tc::mma_f16(tmem + f * N, ad, bd, id, ks > 0);
+        }
+      tc::mma_commit(&bar);
+    }
+    if (!wait_mma()) break;
+
+    // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
+    {
+      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
+      float v[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16)
+        tc::tmem_ld16(tmem + lane_sel + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int rt = 0; rt < 2; ++rt) {
+        unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 8) {
+          float v8[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
+          st8(dst, off_mn(w * HN + 32 * h + c0, y, 128), v8);
+        }
+      }
+    }
+    sync_for_mma();
+
+    // ---- Stage 2: X = T^T F^T -> TMEM cols [(rt 2 + f) N, +N).
+    if (tid == 0) {
+      const uint32_t id = tc::idesc_f16(128, N, 1, 0);
+#pragma unroll
+      for (int rt = 0; rt < 2; ++rt)
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+#pragma unroll
+          for (int ks = 0; ks < SS / 16; ++ks) {
+            const uint64_t ad =
+                tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
+            const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
+            tc::mma_f16(tmem + (rt * 2 + f) * N, ad, bd, id, ks > 0);
+          }
+      tc::mma_commit(&bar);
+    }
+    if (!wait_mma()) break;
+
+    // ---- Product: thread (q, t) forms g in [16 q, 16 q + 16) of row c = t % HN of window t / HN.
+    {
+      const bool special = (t % HN) == 0;
+      const float qs = 1.0f / 1024.0f;
+      unsigned char* dst = sm + L::OP;
+#pragma unroll
+      for (int gc = 0; gc < 16; gc += 8) {
+        const int g0 = 16 * q + gc;
+        float ea[16], eb[16], oa[16], ob[16];
+        tc::tmem_ld16(tmem + lane_sel + 0 * N + 2 * g0, ea);
+        tc::tmem_ld16(tmem + lane_sel + 1 * N + 2 * g0, eb);
+        tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
+        tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
+        tc::tmem_ld_wait();
+        float qr0[8], qi0[8], qr1[8], qi1[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          PairQ pq;
+          if (i == 0 && g0 == 0) {
+            const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
+            const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
+            pq.r0 = q0.r0; pq.i0 = q0.i0; pq.r1 = q1.r0; pq.i1 = q1.i0;
+          } else {
+            pq = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                              ob[2 * i], ob[2 * i + 1], special);
+          }
+          qr0[i] = pq.r0 * qs; qi0[i] = pq.i0 * qs; qr1[i] = pq.r1 * qs; qi1[i] = pq.i1 * qs;
+        }
+        st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
+        st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
+        st8(dst, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
+        st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
+      }
+    }
+    sync_for_mma();
+
+    // ---- Stage 3: Re U = Qr C - Qi S -> cols [0, N); Im U = Qr S + Qi C -> cols [N, 2N).
+    if (tid == 0) {
+      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const int bre = part == 0 ? L::BC : L::BS;   // multiplies Qr
+        const int bim = part == 0 ? L::BNS : L::BC;  // multiplies Qi
+#pragma unroll
+        for (int src = 0; src < 2; ++src)
+#pragma unroll
+          for (int ks = 0; ks < N / 16; ++ks) {
+            const uint64_t ad = tc::sdesc(sbase + L::OP + src * 2048 + ks * 256, 128, 2 * N * 16);
+            const uint64_t bd = tc::sdesc(sbase + (src == 0 ? bre : bim) + ks * 256, 128, N * 16);
+            tc::mma_f16(tmem + part * N, ad, bd, id, (src | ks) != 0);
+          }
+      }
+      tc::mma_commit(&bar);
+    }
+    if (!wait_mma()) break;
+
+    // ---- Stage 3 -> 4: thread (q, t) moves r in [64 rh, 64 rh + 64) of part q & 1 of row (w, c).
+    {
+      const int part = q & 1, rh = q >> 1, w = t / HN, c = t % HN;
+      float v[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16)
+        tc::tmem_ld16(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int r0 = 0; r0 < 64; r0 += 8) {
+        const int m = w * N + 64 * rh + r0;
+        st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
+      }
+    }
+    sync_for_mma();
+
+    // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
+    if (tid == 0) {
+      const uint32_t id = tc::idesc_f16(128, N, 1, 0);
+#pragma unroll
+      for (int rt = 0; rt < 2; ++rt)
+#pragma unroll
+        for (int ks = 0; ks < N / 16; ++ks) {
+          const uint64_t ad = tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
+          const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16);
+          tc::mma_f16(tmem + rt * N, ad, bd, id, ks > 0);
+        }
+      tc::mma_commit(&bar);
+    }
+    if (!wait_mma()) break;
+
+    // ---- Epilogue: thread (q, t) holds shifted columns [64 ch, 64 ch + 64) of
+    // map row t of window w = q & 1 (row index i = t ^ N/2).
+    const int w = q & 1, ch = q >> 1, i = t ^ HN;
+    const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
+    {
+      float v[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16)
+        tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+      tc::tmem_ld_wait();
+      if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
+      // First maximum of the half row: pairwise tree, the left operand wins ties.
+      float bv[32];
+      int bk[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const bool rgt = v[2 * k + 1] > v[2 * k];
+        bv[k] = rgt ? v[2 * k + 1] : v[2 * k];
+        bk[k] = rgt ? 2 * k + 1 : 2 * k;
+      }
+#pragma unroll
+      for (int span = 16; span > 0; span >>= 1)
+#pragma unroll
+        for (int k = 0; k < span; ++k) {
+          const bool rgt = bv[2 * k + 1] > bv[2 * k];
+          bv[k] = rgt ? bv[2 * k + 1] : bv[2 * k];
+          bk[k] = rgt ? bk[2 * k + 1] : bk[2 * k];
+        }
+      float best = bv[0];
+      int idx = i * N + 64 * ch + bk[0];
+      if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
+      }
+      if (lane == 0) {
+        pk_val[w][ch * 4 + (t >> 5)] = best;
+        pk_idx[w][ch * 4 + (t >> 5)] = idx;
+      }
+      if (a.maps && g0 + w < total) {
+        const int ue = 10 - sc_e[0][w] - sc_e[1][w];
+        float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
+#pragma unroll
+        for (int k = 0; k < 64; ++k) mo[k] = i == 0 ? 0.f : ldexpf(v[k], ue);
+      }
+    }
+    __syncthreads();
+    if (tid < W) {
+      float v = pk_val[tid][0];
+      int idx = pk_idx[tid][0];
+#pragma unroll
+      for (int p = 1; p < 8; ++p)
+        if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
+          v = pk_val[tid][p];
+          idx = pk_idx[tid][p];
+        }
+      pk_idx[tid][0] = idx;
+    }
+    __syncthreads();
+    {
+      const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
+      const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
+      if (__any_sync(0xffffffffu, mine)) {
+        float v[64];
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+        if (mine) {
+          float vc = 0.f, vl = 0.f, vr = 0.f;
+#pragma unroll
+          for (int k = 0; k < 64; ++k) {
+            const int j = 64 * ch + k;
+            const float x = (i == 0 || j == 0) ? 0.f : v[k];
+            vc = fmaf(j == pj ? 1.f : 0.f, x, vc);
+            vl = fmaf(j == pj - 1 ? 1.f : 0.f, x, vl);
+            vr = fmaf(j == pj + 1 ? 1.f : 0.f, x, vr);
+          }
+          if (i == pi_) {
+            nb[w][0][ch] = vc;
+            nb[w][3][ch] = vl;
+            nb[w][4][ch] = vr;
+          } else if (i == pi_ - 1) {
+            nb[w][1][ch] = vc;
+          } else {
+            nb[w][2][ch] = vc;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < W && g0 + tid < total) {
+      const int ww = tid;
+      const long long g = g0 + ww;
+      const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
+      float isp = (float)pi_, jsp = (float)pj;
+      if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
+        const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
+        float c = ldexpf(nb[ww][0][0] + nb[ww][0][1], ue), cd = ldexpf(nb[ww][1][0] + nb[ww][1][1], ue);
+        float cu = ldexpf(nb[ww][2][0] + nb[ww][2][1], ue), cl = ldexpf(nb[ww][3][0] + nb[ww][3][1], ue);
+        float cr = ldexpf(nb[ww][4][0] + nb[ww][4][1], ue);
+        const float eps = 1e-7f;
+        if (a.subpixel == PIV_SUBPIXEL_GAUSSIAN) {
+          if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
+            c = logf(c); cd = logf(cd); cu = logf(cu); cl = logf(cl); cr = logf(cr);
+            isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
+            jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
+          }
+        } else if (a.subpixel == PIV_SUBPIXEL_PARABOLIC) {
+          isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
+          jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
+        } else {
+          isp = add_rn((float)pi_, div_rn(sub_rn(cu, cd), add_rn(add_rn(add_rn(cd, c), cu), eps)));
+          jsp = add_rn((float)pj, div_rn(sub_rn(cr, cl), add_rn(add_rn(add_rn(cl, c), cr), eps)));
+        }
+      }
+      float* uo = reinterpret_cast<float*>(a.u);
+      float* vo = reinterpret_cast<float*>(a.v);
+      if (win_valid[ww]) {
+        uo[g] = sub_rn(jsp, (float)HN);
+        vo[g] = sub_rn(isp, (float)HN);
+      } else {
+        uo[g] = NAN;
+        vo[g] = NAN;
+      }
+      if (a.peak_i) a.peak_i[g] = pi_;
+      if (a.peak_j) a.peak_j[g] = pj;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
+}
+
+static int launch_tc64(const CorrArgs& a, cudaStream_t stream) {
+  const long long total = (long long)a.n_pairs * a.m * a.n;
+  if (total == 0) return PIV_OK;
+  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
+  const int n_tiles = (int)((total + Tc64::W - 1) / Tc64::W);
+  static thread_local int configured_dev = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (configured_dev != dev) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_corr_tc64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Tc64::SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_corr_tc64, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc64)");
+    configured_dev = dev;
+  }
+  int grid = sm_count();
+  if (grid > n_tiles) grid = n_tiles;
+  k_corr_tc64<<<grid, Tc64::NT, Tc64::SMEM, stream>>>(a, a.status);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc64 launch");
+}
+
 bool correlate_tensor_supported(const CorrArgs& a) {
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
-         (a.ss == 16 || a.ss == 32);
+         (a.ss == 16 || a.ss == 32 || a.ss == 64);
 }
 
 // CTAs per SM and the dynamic shared memory that makes exactly that many fit:
@@ -593,6 +1086,7 @@ static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
 
 int correlate_tensor(const CorrArgs& a, cudaStream_t stream) {
   if (!correlate_tensor_supported(a)) return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
+  if (a.ss == 64) return launch_tc64(a, stream);
   return a.ss == 16 ? launch_tc<16>(a, stream) : launch_tc<32>(a, stream);
 }
 

@@ -202,6 +202,27 @@ def test_deform_cubic_matches_oracle(env):
     np.testing.assert_allclose(ob[0].cpu().numpy(), rb, atol=1e-2)
 
 
+@pytest.mark.parametrize("shape,pixel", [((7, 5), "u8"), ((1, 40), "f32"), ((13, 3), "u16"), ((70, 150), "f64"),
+                                         ((33, 65), "u8")])
+def test_spline_prefilter_matches_scipy(env, shape, pixel):
+    """Prefilter against scipy's mirror-mode cubic spline_filter, frames smaller
+    than the filter support and tiles that straddle the frame edge included."""
+    torch, _lib, lib = env
+    import scipy.ndimage
+
+    rng = np.random.default_rng(sum(shape))
+    dt = {"u8": np.uint8, "u16": np.uint16, "f32": np.float32, "f64": np.float64}[pixel]
+    hi = {"u8": 255, "u16": 4000, "f32": 1.0, "f64": 50.0}[pixel]
+    frames = (rng.random((2,) + shape) * hi).astype(dt)
+    d = torch.as_tensor(frames).cuda()
+    coef = torch.empty((2,) + shape, dtype=torch.float32, device="cuda")
+    _lib.check(lib.piv_spline_prefilter(shape[0], shape[1], 2, d.data_ptr(), _lib.PIXEL[pixel],
+                                        coef.data_ptr(), _stream(torch)))
+    for k in range(2):
+        ref = scipy.ndimage.spline_filter(frames[k].astype(np.float64), order=3, mode="mirror")
+        np.testing.assert_allclose(coef[k].cpu().numpy(), ref, atol=2e-6 * hi, rtol=1e-5)
+
+
 def _fields(seed, shape, n_out, fp32):
     rng = np.random.default_rng(seed)
     y, x = np.mgrid[0:shape[0], 0:shape[1]]
@@ -361,7 +382,8 @@ def test_replacement_multi_pair_odd_field(env, method):
         np.testing.assert_array_equal(dval[k].cpu().numpy().astype(bool), rval)
 
 
-TC_CASES = [(16, "gaussian"), (32, "gaussian"), (16, "parabolic"), (32, "centroid")]
+TC_CASES = [(16, "gaussian"), (32, "gaussian"), (16, "parabolic"), (32, "centroid"), (64, "gaussian"),
+            (64, "parabolic")]
 
 
 @pytest.mark.parametrize("ss,subpix", TC_CASES)
@@ -406,10 +428,10 @@ def test_tensor_correlation_accuracy(env, ss, subpix):
     assert e.max() < 0.1
 
 
-@pytest.mark.parametrize("ss", [16, 32])
+@pytest.mark.parametrize("ss", [16, 32, 64])
 def test_tensor_maps_match_oracle(env, ss):
     torch, _lib, lib = env
-    shape = (160, 192)
+    shape = (192, 192) if ss == 64 else (160, 192)  # 25 windows for ss = 64: a partial last tile
     fa, fb = _frames(400 + ss, shape)
     g = _geom(_lib, lib, shape, ss, 0.5)
     N = 2 * ss
