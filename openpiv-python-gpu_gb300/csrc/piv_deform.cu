@@ -171,10 +171,10 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
   const int x0 = (int)fx - 1, y0 = (int)fy - 1;
   float acc = 0.0f;
   if (x0 >= 0 && x0 + 3 < W && y0 >= 0 && y0 + 3 < H) {
-    const float* p = coef + (long long)y0 * W + x0;
+    const float* p = coef + (y0 * W + x0);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const float* row = p + (long long)r * W;
+      const float* row = p + r * W;
       float s = wx[0] * __ldg(row);
       s = fmaf(wx[1], __ldg(row + 1), s);
       s = fmaf(wx[2], __ldg(row + 2), s);
@@ -188,7 +188,7 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
   for (int c = 0; c < 4; ++c) cx[c] = mirror_index(x0 + c, W);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    const float* row = coef + (long long)mirror_index(y0 + r, H) * W;
+    const float* row = coef + mirror_index(y0 + r, H) * W;
     float s = wx[0] * __ldg(row + cx[0]);
     s = fmaf(wx[1], __ldg(row + cx[1]), s);
     s = fmaf(wx[2], __ldg(row + cx[2]), s);
@@ -206,13 +206,27 @@ struct AxisWeight {
   int i;
   float t;
 };
-PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
-  const int d2 = 2 * q - (ss + 2 * off), sp2 = 2 * sp;
-  int i = d2 >= 0 ? d2 / sp2 : -((-d2 + sp2 - 1) / sp2);  // floor division
-  i = i < 0 ? 0 : (i > len - 2 ? len - 2 : i);
-  if (len < 2) i = 0;
-  const float t = len < 2 ? 0.0f : (float)(d2 - i * sp2) / (float)sp2;
+// Per-launch constants of one axis: q -> d2 = 2 q - c0, interval i = floor(d2 / sp2).
+struct AxisMap {
+  int c0, sp2, len;
+  float inv_sp2;
+};
+PIV_HD AxisMap axis_map(int ss, int off, int sp, int len) {
+  return AxisMap{ss + 2 * off, 2 * sp, len, 1.0f / (float)(2 * sp)};
+}
+PIV_D AxisWeight axis_weight(int q, const AxisMap& a) {
+  const int d2 = 2 * q - a.c0;
+  // floor(d2 / sp2) from the float quotient, corrected to the exact integer.
+  int i = (int)floorf((float)d2 * a.inv_sp2);
+  if (i * a.sp2 > d2) --i;
+  else if ((i + 1) * a.sp2 <= d2) ++i;
+  i = i < 0 ? 0 : (i > a.len - 2 ? a.len - 2 : i);
+  if (a.len < 2) i = 0;
+  const float t = a.len < 2 ? 0.0f : (float)(d2 - i * a.sp2) / (float)a.sp2;
   return AxisWeight{i, t};
+}
+PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
+  return axis_weight(q, axis_map(ss, off, sp, len));
 }
 
 static constexpr int kDeformThreads = 256;
@@ -226,17 +240,23 @@ static constexpr int kDeformMaxCols = kDeformThreads + 2;
 // x + up*dta and frame B at x + up*dtb.
 // Launch grid: x over row segments, y over rows, z over pairs.
 template <typename T>
-__global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, T dta, T dtb, int do_a, int do_b) {
+__global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap ax, AxisMap ay, T dta, T dtb,
+                                                           int do_a, int do_b) {
   __shared__ float su[kDeformMaxCols], sv[kDeformMaxCols];
+  __shared__ int s_klo;
   const piv_geometry& g = a.geom;
   const int H = g.height, W = g.width;
   const int j0 = blockIdx.x * kDeformThreads;
   const int j = j0 + threadIdx.x;
   const int i = blockIdx.y, pair = blockIdx.z;
-  const AxisWeight wy = axis_weight(i, g.search_size, g.y_offset, g.spacing, g.m);
-  const int k_lo = axis_weight(j0, g.search_size, g.x_offset, g.spacing, g.n).i;
-  const int j_last = min(j0 + kDeformThreads, W) - 1;
-  const int k_hi = min(axis_weight(j_last, g.search_size, g.x_offset, g.spacing, g.n).i + 1, g.n - 1);
+  const AxisWeight wy = axis_weight(i, ay);
+  if (threadIdx.x == 0) s_klo = axis_weight(j0, ax).i;
+  const AxisWeight wx = axis_weight(min(j, W - 1), ax);
+  // The last thread of the segment knows the highest field column it needs.
+  __shared__ int s_khi;
+  if (threadIdx.x == kDeformThreads - 1 || j == W - 1) s_khi = min(wx.i + 1, g.n - 1);
+  __syncthreads();
+  const int k_lo = s_klo, k_hi = s_khi;
   const long long fo = (long long)pair * g.m * g.n;
   const int iy1 = g.m < 2 ? wy.i : wy.i + 1;
   for (int k = k_lo + threadIdx.x; k <= k_hi; k += kDeformThreads) {
@@ -249,35 +269,32 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, T dta, 
   }
   __syncthreads();
   if (j >= W) return;
-  const long long npix = (long long)H * W;
-  const long long p = (long long)i * W + j;
-  const long long base = (long long)pair * npix;
-  const long long t = base + p;
-  T* out_a = reinterpret_cast<T*>(a.out_a);
-  T* out_b = reinterpret_cast<T*>(a.out_b);
+  const long long base = (long long)pair * H * W;
+  const int p = i * W + j;
+  T* out_a = reinterpret_cast<T*>(a.out_a) + base;
+  T* out_b = reinterpret_cast<T*>(a.out_b) + base;
   if (a.frame_mask && a.frame_mask[p]) {
-    out_a[t] = (T)0;
-    out_b[t] = (T)0;
+    out_a[p] = (T)0;
+    out_b[p] = (T)0;
     return;
   }
-  const AxisWeight wx = axis_weight(j, g.search_size, g.x_offset, g.spacing, g.n);
   const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
   const T x = (T)j, y = (T)i;
   const T up = (T)fmaf(wx.t, su[c1] - su[c0], su[c0]);
   const T vp = (T)fmaf(wx.t, sv[c1] - sv[c0], sv[c0]);
   if (do_a) {
     const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
-    out_a[t] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
+    out_a[p] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
                             : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
   } else {
-    out_a[t] = load_pixel<T>(a.frames_a, a.pixel_type, t);
+    out_a[p] = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
   }
   if (do_b) {
     const T xi = add_rn(x, mul_rn(up, dtb)), yi = add_rn(y, mul_rn(vp, dtb));
-    out_b[t] = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
+    out_b[p] = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
                             : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
   } else {
-    out_b[t] = load_pixel<T>(a.frames_b, a.pixel_type, t);
+    out_b[p] = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
   }
 }
 
@@ -297,10 +314,14 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
     return set_error(PIV_E_UNSUPPORTED, "deformation grid limit (height and pairs <= 65535)");
   const dim3 grid((unsigned)((a.geom.width + kDeformThreads - 1) / kDeformThreads), (unsigned)a.geom.height,
                   (unsigned)a.n_pairs);
+  if ((long long)a.geom.height * a.geom.width > 2147483647LL)
+    return set_error(PIV_E_UNSUPPORTED, "deformation: frames above 2^31 pixels");
+  const AxisMap ax = axis_map(a.geom.search_size, a.geom.x_offset, a.geom.spacing, a.geom.n);
+  const AxisMap ay = axis_map(a.geom.search_size, a.geom.y_offset, a.geom.spacing, a.geom.m);
   if (a.dtype == PIV_DTYPE_F64)
-    k_deform<double><<<grid, kDeformThreads, 0, stream>>>(a, dta, dtb, do_a, do_b);
+    k_deform<double><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, dta, dtb, do_a, do_b);
   else
-    k_deform<float><<<grid, kDeformThreads, 0, stream>>>(a, (float)dta, (float)dtb, do_a, do_b);
+    k_deform<float><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb, do_a, do_b);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_deform launch");
 }

@@ -42,19 +42,81 @@ struct TcLayout {
   static constexpr int HN = N / 2;
   static constexpr int W = 128 / SS;         // window pairs per tile
   static constexpr int TCOLS = 4 * N;        // TMEM columns (stage 2: two frames x two row tiles)
-  // fp16 operand tiles (byte offsets). X and Y are each reused by two stages.
+  // Byte offsets in dynamic shared memory (16-byte aligned).
   static constexpr int B1 = 0;                          // F [N][SS] K-major (stages 1 and 2)
   static constexpr int B3 = B1 + N * SS * 2;            // [2N][2N] K-major
   static constexpr int B4 = B3 + 2 * N * 2 * N * 2;     // [N][N] K-major
-  static constexpr int XB = B4 + N * N * 2;             // A1: 2 x [128][SS] K-major;  A3: [128][2N] K-major
-  static constexpr int YB = XB + 1024 * SS;             // A2: 2 x 2 x [128][SS] MN-major;  A4: 2 x [128][N] MN-major
-  static constexpr int END = YB + 1024 * SS;
+  // Operand region, rewritten by each phase once the product that read it has
+  // completed: A1 2 x [128][SS] K-major; A2 2 x 2 x [128][SS] MN-major; A3
+  // [128][2N] K-major; A4 2 x [128][N] MN-major; then the peak-neighbour rows.
+  static constexpr int OP = B4 + N * N * 2;
+  static constexpr int STG = OP + 1024 * SS;            // next tile's float rows [frame][128][SS], 16-byte chunks swizzled
+  static constexpr int END = STG + 2 * 128 * SS * 4;
   static constexpr int A1_BYTES = 128 * SS * 2;
   static constexpr int A2_BYTES = 128 * SS * 2;
   static constexpr int A4_BYTES = 128 * N * 2;
-  static constexpr size_t SMEM = END + 128;             // + alignment slack
+  static constexpr size_t SMEM = END;
   static constexpr int MIN_BLOCKS = 512 / TCOLS;        // CTAs per SM that the TMEM allows
+  static constexpr int CH = SS / 4;                     // 16-byte chunks per staged row
 };
+
+// Swizzled chunk position of chunk c of staged row t: the eight rows a
+// quarter-warp reads together hit eight different 16-byte bank groups.
+template <int CH>
+PIV_D int stg_chunk(int t, int c) {
+  return CH >= 8 ? (c ^ (t & 7)) : (c ^ ((t >> 1) & (CH - 1)));
+}
+
+PIV_D void cp_async16(uint32_t smem_addr, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr), "l"(gmem) : "memory");
+}
+PIV_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+PIV_D void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// First maximum of x (lowest index among equal maxima) by a pairwise tree:
+// the left operand, which holds the lower indices, wins ties.
+template <int N>
+PIV_D void first_max(const float (&x)[N], float& best, int& bj) {
+  float bv[N / 2];
+  int bk[N / 2];
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) {
+    const bool rgt = x[2 * k + 1] > x[2 * k];
+    bv[k] = rgt ? x[2 * k + 1] : x[2 * k];
+    bk[k] = rgt ? 2 * k + 1 : 2 * k;
+  }
+#pragma unroll
+  for (int span = N / 4; span > 0; span >>= 1)
+#pragma unroll
+    for (int k = 0; k < span; ++k) {
+      const bool rgt = bv[2 * k + 1] > bv[2 * k];
+      bv[k] = rgt ? bv[2 * k + 1] : bv[2 * k];
+      bk[k] = rgt ? bk[2 * k + 1] : bk[2 * k];
+    }
+  best = bv[0];
+  bj = bk[0];
+}
+
+// Subpixel peak (gpu_process.py:1256-1294) from the five map values.
+PIV_D void subpixel_fit(int subpixel, int pi_, int pj, float c, float cd, float cu, float cl, float cr, float& isp,
+                        float& jsp) {
+  const float eps = 1e-7f;
+  isp = (float)pi_;
+  jsp = (float)pj;
+  if (subpixel == PIV_SUBPIXEL_GAUSSIAN) {
+    if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
+      c = logf(c); cd = logf(cd); cu = logf(cu); cl = logf(cl); cr = logf(cr);
+      isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
+      jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
+    }
+  } else if (subpixel == PIV_SUBPIXEL_PARABOLIC) {
+    isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
+    jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
+  } else {
+    isp = add_rn((float)pi_, div_rn(sub_rn(cu, cd), add_rn(add_rn(add_rn(cd, c), cu), eps)));
+    jsp = add_rn((float)pj, div_rn(sub_rn(cr, cl), add_rn(add_rn(add_rn(cl, c), cr), eps)));
+  }
+}
 
 // Byte offset of element (r, k) in a no-swizzle K-major tile with K columns.
 PIV_D uint32_t off_k(int r, int k, int K) {
@@ -129,28 +191,32 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
   return q;
 }
 
-template <int SS>
+// ASYNC: float32 frames whose window rows start on 16-byte boundaries. The
+// next tile's rows are then copied into shared memory with cp.async while the
+// current tile runs through its four products; otherwise each tile loads its
+// rows from global memory when it starts.
+template <int SS, bool ASYNC>
 __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
   using L = TcLayout<SS>;
-  constexpr int N = L::N, HN = L::HN, W = L::W;
+  constexpr int N = L::N, HN = L::HN, W = L::W, CH = L::CH;
   constexpr int NPART = N / 32;      // warps per window in the epilogue
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
-  __shared__ float tw_re[N], tw_im[N];
   __shared__ int sc_e[2][W];         // per frame and window: log2 of the operand scale
-  __shared__ long long win_base[W];
-  __shared__ int win_valid[W];
+  __shared__ long long win_base[2][W];
+  __shared__ int win_valid[2][W];
   __shared__ float pk_val[W][NPART];
   __shared__ int pk_idx[W][NPART];
-  __shared__ float nb[W][5];         // c, cd, cu, cl, cr (scaled)
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const uint32_t lane_sel = (uint32_t)(32 * warp) << 16;
 
-  // Twiddles W_N^k = exp(-2 pi i k / N).
+  // Constant DFT operands; the twiddles W_N^k = exp(-2 pi i k / N) sit in the
+  // operand region until the first tile.
+  float* tw_re = reinterpret_cast<float*>(sm + L::OP);
+  float* tw_im = tw_re + N;
   for (int k = tid; k < N; k += 128) {
     float sn, cs;
     sincospif(2.0f * (float)k / (float)N, &sn, &cs);
@@ -179,12 +245,12 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     sth(sm + L::B3, off_k(n, kap, 2 * N), v);
   }
   for (int e = tid; e < N * N; e += 128) {  // B4[s][kappa], kappa = (part, c)
-    const int s = e / N, kap = e % N, part = kap / HN, c = kap % HN;
-    const int q = (c * s) % N;
+    const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
+    const int q = (c * s_) % N;
     float v;
-    if (c == 0) v = part == 0 ? inv_n : ((s & 1) ? -inv_n : inv_n);
+    if (c == 0) v = part == 0 ? inv_n : ((s_ & 1) ? -inv_n : inv_n);
     else v = part == 0 ? 2.0f * tw_re[q] * inv_n : 2.0f * tw_im[q] * inv_n;
-    sth(sm + L::B4, off_k(s, kap, N), v);
+    sth(sm + L::B4, off_k(s_, kap, N), v);
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base_s, L::TCOLS);
   tc::fence_async_smem();
@@ -201,7 +267,6 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
   const int n_tiles = (int)((total + W - 1) / W);
   const long long frame_elems = (long long)a.height * a.width;
 
-  // Waits for the last commit; on timeout every thread leaves the tile loop.
   auto wait_mma = [&]() -> bool {
     bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
     phase ^= 1u;
@@ -216,33 +281,67 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     __syncthreads();
     tc::fence_after_sync();
   };
-
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const long long g0 = (long long)tile * W;
-    if (tid < W) {
-      const long long g = g0 + tid;
-      int ok = g < total;
-      long long base = 0;
-      if (ok) {
-        const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-        if (a.win_mask) ok = a.win_mask[k] == 0;
-        base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
-      }
-      win_valid[tid] = ok;
-      win_base[tid] = base;
+  // Window corners of tile `tl` into slot `sl` (threads tid < W).
+  auto window_setup = [&](int tl, int sl) {
+    const long long g = (long long)tl * W + tid;
+    int ok = tl < n_tiles && g < total;
+    long long base = 0;
+    if (ok) {
+      const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
+      if (a.win_mask) ok = a.win_mask[k] == 0;
+      base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
     }
+    win_valid[sl][tid] = ok;
+    win_base[sl][tid] = base;
+  };
+  // Thread t starts the copies of row t of both frames of the tile in slot `sl`.
+  auto stage_async = [&](int sl) {
+    const int w = tid / SS, y = tid % SS;
+    if (!win_valid[sl][w]) return;
+    const long long off = win_base[sl][w] + (long long)y * a.width;
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const float* src = reinterpret_cast<const float*>(f == 0 ? a.frame_a : a.frame_b) + off;
+      const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + tid) * SS * 4);
+#pragma unroll
+      for (int c = 0; c < CH; ++c) cp_async16(row + 16 * stg_chunk<CH>(tid, c), src + 4 * c);
+    }
+  };
+
+  if (tid < W) window_setup(blockIdx.x, 0);
+  __syncthreads();
+  if (ASYNC) {
+    stage_async(0);
+    cp_async_commit();
+  }
+
+  int sl = 0;
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
+    const long long g0 = (long long)tile * W;
+    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
+    if (ASYNC) cp_async_wait_all();
     __syncthreads();
 
-    // ---- Staging: thread (w, y) gathers row y of window w of both frames.
+    // ---- Staging: thread (w, y) takes row y of window w of both frames.
     {
       const int w = tid / SS, y = tid % SS;
-      const bool ok = win_valid[w] != 0;
-      const long long rowoff = win_base[w] + (long long)y * a.width;
+      const bool ok = win_valid[sl][w] != 0;
 #pragma unroll
       for (int f = 0; f < 2; ++f) {
-        const void* frame = f == 0 ? a.frame_a : a.frame_b;
         float r[SS];
-        load_row(frame, a.pixel_type, rowoff, ok, r);
+        if (ASYNC) {
+          const unsigned char* row = sm + L::STG + (f * 128 + tid) * SS * 4;
+#pragma unroll
+          for (int c = 0; c < CH; ++c) {
+            const float4 q4 = *reinterpret_cast<const float4*>(row + 16 * stg_chunk<CH>(tid, c));
+            r[4 * c] = ok ? q4.x : 0.f;
+            r[4 * c + 1] = ok ? q4.y : 0.f;
+            r[4 * c + 2] = ok ? q4.z : 0.f;
+            r[4 * c + 3] = ok ? q4.w : 0.f;
+          }
+        } else {
+          load_row(f == 0 ? a.frame_a : a.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * a.width, ok, r);
+        }
         float sum = 0.f;
 #pragma unroll
         for (int x = 0; x < SS; ++x) sum += r[x];
@@ -265,10 +364,14 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
         for (int x = 0; x < SS; ++x) r[x] *= s;
         if (y == 0) sc_e[f][w] = e;
 #pragma unroll
-        for (int x = 0; x < SS; x += 8) st8(sm + L::XB + f * L::A1_BYTES, off_k(tid, x, SS), r + x);
+        for (int x = 0; x < SS; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(tid, x, SS), r + x);
       }
     }
     sync_for_mma();
+    if (ASYNC) {
+      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
+      cp_async_commit();
+    }
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
     if (tid == 0) {
@@ -277,7 +380,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       for (int f = 0; f < 2; ++f)
 #pragma unroll
         for (int ks = 0; ks < SS / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::XB + f * L::A1_BYTES + ks * 256, 128, SS * 16);
+          const uint64_t ad = tc::sdesc(sbase + L::OP + f * L::A1_BYTES + ks * 256, 128, SS * 16);
           const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
           tc::mma_f16(tmem + f * N, ad, bd, id, ks > 0);
         }
@@ -298,7 +401,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
         tc::tmem_ld_wait();
 #pragma unroll
         for (int rt = 0; rt < 2; ++rt) {
-          unsigned char* dst = sm + L::YB + (f * 2 + rt) * L::A2_BYTES;
+          unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
 #pragma unroll
           for (int c0 = 0; c0 < HN; c0 += 8) {
             float v8[8];
@@ -321,7 +424,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
 #pragma unroll
           for (int ks = 0; ks < SS / 16; ++ks) {
             const uint64_t ad =
-                tc::sdesc(sbase + L::YB + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
+                tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
             const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
             tc::mma_f16(tmem + rt * 2 * N + f * N, ad, bd, id, ks > 0);
           }
@@ -334,7 +437,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     {
       const bool special = (tid % HN) == 0;
       const float qs = 1.0f / 1024.0f;
-      unsigned char* dst = sm + L::XB;
+      unsigned char* dst = sm + L::OP;
 #pragma unroll
       for (int g0 = 0; g0 < HN; g0 += 8) {
         float ea[16], eb[16], oa[16], ob[16];
@@ -371,7 +474,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
 #pragma unroll
       for (int ks = 0; ks < 2 * N / 16; ++ks) {
-        const uint64_t ad = tc::sdesc(sbase + L::XB + ks * 256, 128, 2 * N * 16);
+        const uint64_t ad = tc::sdesc(sbase + L::OP + ks * 256, 128, 2 * N * 16);
         const uint64_t bd = tc::sdesc(sbase + L::B3 + ks * 256, 128, 2 * N * 16);
         tc::mma_f16(tmem, ad, bd, id, ks > 0);
       }
@@ -392,7 +495,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
 #pragma unroll
         for (int r0 = 0; r0 < N; r0 += 8) {
           const int m = w * N + r0;
-          st8(sm + L::YB + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
+          st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
         }
       }
     }
@@ -405,7 +508,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       for (int rt = 0; rt < 2; ++rt)
 #pragma unroll
         for (int ks = 0; ks < N / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::YB + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
+          const uint64_t ad = tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
           const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16);
           tc::mma_f16(tmem + rt * N, ad, bd, id, ks > 0);
         }
@@ -414,7 +517,9 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     if (!wait_mma()) break;
 
     // ---- Epilogue. Row rt*128 + tid of the tile is map row r of window w
-    // (scaled by 2^-(10 - e_a - e_b)); shifted row index i = r ^ N/2.
+    // (scaled by 2^-(10 - e_a - e_b)); shifted row index i = r ^ N/2, shifted
+    // column j = s ^ N/2. Lags without window overlap (i = 0 or j = 0) are 0.
+    float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
 #pragma unroll
     for (int rt = 0; rt < 2; ++rt) {
       const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
@@ -423,16 +528,14 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       for (int c0 = 0; c0 < N; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
-      // Shifted row: column j holds lag s = j ^ N/2; lags without overlap are 0.
       float rowc[N];
 #pragma unroll
-      for (int j = 0; j < N; ++j) rowc[j] = (i == 0 || j == 0) ? 0.f : v[j ^ HN];
-      float best = rowc[0];
-      int bj = 0;
-#pragma unroll
-      for (int j = 1; j < N; ++j)
-        if (rowc[j] > best) { best = rowc[j]; bj = j; }
+      for (int j = 0; j < N; ++j) rowc[j] = j == 0 ? 0.f : v[j ^ HN];
+      float best;
+      int bj;
+      first_max<N>(rowc, best, bj);
       int idx = i * N + bj;
+      if (i == 0) { best = 0.f; idx = 0; }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
@@ -447,7 +550,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
         const int ue = 10 - sc_e[0][w] - sc_e[1][w];
         float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
 #pragma unroll
-        for (int j = 0; j < N; ++j) mo[j] = ldexpf(rowc[j], ue);
+        for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
       }
     }
     __syncthreads();
@@ -463,7 +566,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       pk_idx[tid][0] = idx;
     }
     __syncthreads();
-    // Neighbours of the peak: rows i-1, i, i+1 at column j, and j-1, j+1 of row i.
+    // The rows next to the peak go to shared memory for the five-point fit.
 #pragma unroll
     for (int rt = 0; rt < 2; ++rt) {
       const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
@@ -476,24 +579,9 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
           tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         if (mine) {
-          // Masked sums keep the row in registers; exactly one term of each is non-zero.
-          float vc = 0.f, vl = 0.f, vr = 0.f;
+          float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
 #pragma unroll
-          for (int j = 0; j < N; ++j) {
-            const float x = (i == 0 || j == 0) ? 0.f : v[j ^ HN];
-            vc = fmaf(j == pj ? 1.f : 0.f, x, vc);
-            vl = fmaf(j == pj - 1 ? 1.f : 0.f, x, vl);
-            vr = fmaf(j == pj + 1 ? 1.f : 0.f, x, vr);
-          }
-          if (i == pi_) {
-            nb[w][0] = vc;
-            nb[w][3] = vl;
-            nb[w][4] = vr;
-          } else if (i == pi_ - 1) {
-            nb[w][1] = vc;
-          } else {
-            nb[w][2] = vc;
-          }
+          for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
         }
       }
     }
@@ -505,26 +593,16 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
-        float c = ldexpf(nb[ww][0], ue), cd = ldexpf(nb[ww][1], ue), cu = ldexpf(nb[ww][2], ue);
-        float cl = ldexpf(nb[ww][3], ue), cr = ldexpf(nb[ww][4], ue);
-        const float eps = 1e-7f;
-        if (a.subpixel == PIV_SUBPIXEL_GAUSSIAN) {
-          if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
-            c = logf(c); cd = logf(cd); cu = logf(cu); cl = logf(cl); cr = logf(cr);
-            isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-            jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
-          }
-        } else if (a.subpixel == PIV_SUBPIXEL_PARABOLIC) {
-          isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-          jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
-        } else {
-          isp = add_rn((float)pi_, div_rn(sub_rn(cu, cd), add_rn(add_rn(add_rn(cd, c), cu), eps)));
-          jsp = add_rn((float)pj, div_rn(sub_rn(cr, cl), add_rn(add_rn(add_rn(cl, c), cr), eps)));
-        }
+        // Shifted (i, j) -> stored row slot i - pi + 1, natural column j ^ N/2.
+        auto at = [&](int i, int j) -> float {
+          return (i == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (i - pi_ + 1)) * N + (j ^ HN)], ue);
+        };
+        subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
+                     at(pi_, pj + 1), isp, jsp);
       }
       float* uo = reinterpret_cast<float*>(a.u);
       float* vo = reinterpret_cast<float*>(a.v);
-      if (win_valid[ww]) {
+      if (win_valid[sl][ww]) {
         uo[g] = sub_rn(jsp, (float)HN);
         vo[g] = sub_rn(isp, (float)HN);
       } else {
@@ -538,6 +616,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     __syncthreads();
     tc::fence_after_sync();
   }
+  if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
@@ -560,35 +639,41 @@ struct Tc64 {
   static constexpr int BS = BC + N * N * 2;     // sin / N
   static constexpr int BNS = BS + N * N * 2;    // -sin / N
   static constexpr int B4 = BNS + N * N * 2;    // [N][N] K-major, K = (part, c)
-  static constexpr int OP = B4 + N * N * 2;     // operand region
-  static constexpr int END = OP + 65536;
+  static constexpr int OP = B4 + N * N * 2;     // operand region (then the peak-neighbour rows)
+  static constexpr int STG = OP + 65536;        // next tile's 8-bit rows [frame][w][y][64 B], chunks swizzled
+  static constexpr int END = STG + 2 * W * SS * SS;
   static constexpr int A1_BYTES = 128 * SS * 2; // per frame, K-major [128][SS]
   static constexpr int A2_BYTES = 128 * SS * 2; // per (frame, tile), MN-major [128][SS]
   static constexpr int A4_BYTES = 128 * N * 2;  // per tile, MN-major [128][N]
-  static constexpr size_t SMEM = END + 128;
+  static constexpr size_t SMEM = END;
 };
 
+// Swizzled 16-byte chunk k (0..3) of staged 8-bit row t.
+PIV_D int stg64_chunk(int t, int k) { return k ^ ((t >> 1) & 3); }
+
+// ASYNC: 8-bit frames whose window rows start on 16-byte boundaries; the next
+// tile's rows are copied with cp.async while the current tile runs.
+template <bool ASYNC>
 __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   using L = Tc64;
   constexpr int SS = L::SS, N = L::N, HN = L::HN, W = L::W;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
-  __shared__ float tw_re[N], tw_im[N];
   __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
   __shared__ int sc_e[2][W];
-  __shared__ long long win_base[W];
-  __shared__ int win_valid[W];
+  __shared__ long long win_base[2][W];
+  __shared__ int win_valid[2][W];
   __shared__ float pk_val[W][8];
   __shared__ int pk_idx[W][8];
-  __shared__ float nb[W][5][2];      // c, cd, cu, cl, cr (scaled) per column half
 
   const int tid = threadIdx.x;
   const int q = tid >> 7, t = tid & 127;
   const int warp = tid >> 5, lane = tid & 31;
   const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
 
+  float* tw_re = reinterpret_cast<float*>(sm + L::OP);
+  float* tw_im = tw_re + N;
   for (int k = tid; k < N; k += L::NT) {
     float sn, cs;
     sincospif(2.0f * (float)k / (float)N, &sn, &cs);
@@ -653,31 +738,61 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     __syncthreads();
     tc::fence_after_sync();
   };
-
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const long long g0 = (long long)tile * W;
-    if (tid < W) {
-      const long long g = g0 + tid;
-      int ok = g < total;
-      long long base = 0;
-      if (ok) {
-        const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-        if (a.win_mask) ok = a.win_mask[k] == 0;
-        base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
-      }
-      win_valid[tid] = ok;
-      win_base[tid] = base;
+  auto window_setup = [&](int tl, int sl) {
+    const long long g = (long long)tl * W + tid;
+    int ok = tl < n_tiles && g < total;
+    long long base = 0;
+    if (ok) {
+      const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
+      if (a.win_mask) ok = a.win_mask[k] == 0;
+      base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
     }
+    win_valid[sl][tid] = ok;
+    win_base[sl][tid] = base;
+  };
+  // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it stages itself.
+  auto stage_async = [&](int sl) {
+    const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
+    if (!win_valid[sl][w]) return;
+    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? a.frame_a : a.frame_b) + win_base[sl][w] +
+                         (long long)y * a.width;
+    const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) cp_async16(row + 16 * stg64_chunk(t, 2 * h + c), src + 16 * (2 * h + c));
+  };
+
+  if (tid < W) window_setup(blockIdx.x, 0);
+  __syncthreads();
+  if (ASYNC) {
+    stage_async(0);
+    cp_async_commit();
+  }
+
+  int sl = 0;
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
+    const long long g0 = (long long)tile * W;
+    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
+    if (ASYNC) cp_async_wait_all();
     __syncthreads();
 
-    // ---- Staging: thread (q, t) loads half h = q >> 1 of row y of window w of frame f = q & 1.
+    // ---- Staging: thread (q, t) takes half h = q >> 1 of row y of window w of frame f = q & 1.
     {
       const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63, grp = h * 2 + ((t >> 5) & 1);
-      const bool ok = win_valid[w] != 0;
-      const void* frame = f == 0 ? a.frame_a : a.frame_b;
-      const long long rowoff = win_base[w] + (long long)y * a.width + 32 * h;
+      const bool ok = win_valid[sl][w] != 0;
       float r[32];
-      load_row(frame, a.pixel_type, rowoff, ok, r);
+      if (ASYNC) {
+        const unsigned char* row = sm + L::STG + (f * 128 + t) * SS;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const uint4 q4 = *reinterpret_cast<const uint4*>(row + 16 * stg64_chunk(t, 2 * h + c));
+          const uint32_t wds[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+          for (int k = 0; k < 16; ++k) r[16 * c + k] = ok ? (float)((wds[k >> 2] >> (8 * (k & 3))) & 0xffu) : 0.f;
+        }
+      } else {
+        load_row(f == 0 ? a.frame_a : a.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * a.width + 32 * h,
+                 ok, r);
+      }
       float sum = 0.f;
 #pragma unroll
       for (int x = 0; x < 32; ++x) sum += r[x];
@@ -708,6 +823,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     }
     sync_for_mma();
+    if (ASYNC) {
+      stage_async(sl ^ 1);
+      cp_async_commit();
+    }
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
     if (tid == 0) {
@@ -855,6 +974,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     // map row t of window w = q & 1 (row index i = t ^ N/2).
     const int w = q & 1, ch = q >> 1, i = t ^ HN;
     const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
+    float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
     {
       float v[64];
 #pragma unroll
@@ -862,25 +982,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
       if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
-      // First maximum of the half row: pairwise tree, the left operand wins ties.
-      float bv[32];
-      int bk[32];
-#pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const bool rgt = v[2 * k + 1] > v[2 * k];
-        bv[k] = rgt ? v[2 * k + 1] : v[2 * k];
-        bk[k] = rgt ? 2 * k + 1 : 2 * k;
-      }
-#pragma unroll
-      for (int span = 16; span > 0; span >>= 1)
-#pragma unroll
-        for (int k = 0; k < span; ++k) {
-          const bool rgt = bv[2 * k + 1] > bv[2 * k];
-          bv[k] = rgt ? bv[2 * k + 1] : bv[2 * k];
-          bk[k] = rgt ? bk[2 * k + 1] : bk[2 * k];
-        }
-      float best = bv[0];
-      int idx = i * N + 64 * ch + bk[0];
+      float best;
+      int bk;
+      first_max<64>(v, best, bk);
+      int idx = i * N + 64 * ch + bk;
       if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -922,24 +1027,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
           tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         if (mine) {
-          float vc = 0.f, vl = 0.f, vr = 0.f;
+          float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N + s0);
 #pragma unroll
-          for (int k = 0; k < 64; ++k) {
-            const int j = 64 * ch + k;
-            const float x = (i == 0 || j == 0) ? 0.f : v[k];
-            vc = fmaf(j == pj ? 1.f : 0.f, x, vc);
-            vl = fmaf(j == pj - 1 ? 1.f : 0.f, x, vl);
-            vr = fmaf(j == pj + 1 ? 1.f : 0.f, x, vr);
-          }
-          if (i == pi_) {
-            nb[w][0][ch] = vc;
-            nb[w][3][ch] = vl;
-            nb[w][4][ch] = vr;
-          } else if (i == pi_ - 1) {
-            nb[w][1][ch] = vc;
-          } else {
-            nb[w][2][ch] = vc;
-          }
+          for (int c4 = 0; c4 < 16; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
         }
       }
     }
@@ -951,27 +1041,15 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
-        float c = ldexpf(nb[ww][0][0] + nb[ww][0][1], ue), cd = ldexpf(nb[ww][1][0] + nb[ww][1][1], ue);
-        float cu = ldexpf(nb[ww][2][0] + nb[ww][2][1], ue), cl = ldexpf(nb[ww][3][0] + nb[ww][3][1], ue);
-        float cr = ldexpf(nb[ww][4][0] + nb[ww][4][1], ue);
-        const float eps = 1e-7f;
-        if (a.subpixel == PIV_SUBPIXEL_GAUSSIAN) {
-          if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
-            c = logf(c); cd = logf(cd); cu = logf(cu); cl = logf(cl); cr = logf(cr);
-            isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-            jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
-          }
-        } else if (a.subpixel == PIV_SUBPIXEL_PARABOLIC) {
-          isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-          jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
-        } else {
-          isp = add_rn((float)pi_, div_rn(sub_rn(cu, cd), add_rn(add_rn(add_rn(cd, c), cu), eps)));
-          jsp = add_rn((float)pj, div_rn(sub_rn(cr, cl), add_rn(add_rn(add_rn(cl, c), cr), eps)));
-        }
+        auto at = [&](int ii, int j) -> float {
+          return (ii == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)], ue);
+        };
+        subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
+                     at(pi_, pj + 1), isp, jsp);
       }
       float* uo = reinterpret_cast<float*>(a.u);
       float* vo = reinterpret_cast<float*>(a.v);
-      if (win_valid[ww]) {
+      if (win_valid[sl][ww]) {
         uo[g] = sub_rn(jsp, (float)HN);
         vo[g] = sub_rn(isp, (float)HN);
       } else {
@@ -985,33 +1063,43 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     __syncthreads();
     tc::fence_after_sync();
   }
+  if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
 }
 
-static int launch_tc64(const CorrArgs& a, cudaStream_t stream) {
+template <bool ASYNC>
+static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
   const long long total = (long long)a.n_pairs * a.m * a.n;
-  if (total == 0) return PIV_OK;
-  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
   const int n_tiles = (int)((total + Tc64::W - 1) / Tc64::W);
   static thread_local int configured_dev = -1;
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_dev != dev) {
     cudaError_t e =
-        cudaFuncSetAttribute(k_corr_tc64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Tc64::SMEM);
+        cudaFuncSetAttribute(k_corr_tc64<ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Tc64::SMEM);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_corr_tc64, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(k_corr_tc64<ASYNC>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc64)");
     configured_dev = dev;
   }
   int grid = sm_count();
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc64<<<grid, Tc64::NT, Tc64::SMEM, stream>>>(a, a.status);
+  k_corr_tc64<ASYNC><<<grid, Tc64::NT, Tc64::SMEM, stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc64 launch");
+}
+
+static int launch_tc64(const CorrArgs& a, cudaStream_t stream) {
+  const long long total = (long long)a.n_pairs * a.m * a.n;
+  if (total == 0) return PIV_OK;
+  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
+  const bool aligned = a.pixel_type == PIV_PIXEL_U8 && ((uintptr_t)a.frame_a % 16) == 0 &&
+                       ((uintptr_t)a.frame_b % 16) == 0 && a.width % 16 == 0 && a.x_offset % 16 == 0 &&
+                       a.spacing % 16 == 0;
+  return aligned ? launch_tc64_t<true>(a, stream) : launch_tc64_t<false>(a, stream);
 }
 
 bool correlate_tensor_supported(const CorrArgs& a) {
@@ -1027,13 +1115,13 @@ struct TcLaunch {
   size_t smem = 0;
 };
 
-template <int SS>
+template <int SS, bool ASYNC>
 static int tc_launch_config(TcLaunch& out) {
   using L = TcLayout<SS>;
   int dev = 0;
   cudaGetDevice(&dev);
   cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, k_corr_tc<SS>);
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_corr_tc<SS, ASYNC>);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncGetAttributes(k_corr_tc)");
   int smem_sm = 0, smem_optin = 0, resv = 0, regs_sm = 0;
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -1049,11 +1137,11 @@ static int tc_launch_config(TcLaunch& out) {
   if (per_sm < 1) return set_error(PIV_E_UNSUPPORTED, "tensor correlation does not fit on an SM");
   size_t smem = (size_t)smem_sm / per_sm - fa.sharedSizeBytes - resv;
   smem = std::min(smem, (size_t)smem_optin - fa.sharedSizeBytes);
-  smem = std::max(smem, L::SMEM) & ~(size_t)127;
+  smem = std::max(smem, L::SMEM) & ~(size_t)15;
   if (smem < L::SMEM) smem = L::SMEM;
-  e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_corr_tc<SS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc)");
   out.per_sm = per_sm;
@@ -1061,27 +1149,38 @@ static int tc_launch_config(TcLaunch& out) {
   return PIV_OK;
 }
 
-template <int SS>
-static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
+template <int SS, bool ASYNC>
+static int launch_tc_t(const CorrArgs& a, cudaStream_t stream) {
   using L = TcLayout<SS>;
   const long long total = (long long)a.n_pairs * a.m * a.n;
-  if (total == 0) return PIV_OK;
-  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
   const int n_tiles = (int)((total + L::W - 1) / L::W);
   static thread_local int configured_dev = -1;
   static thread_local TcLaunch cfg;
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_dev != dev) {
-    const int rc = tc_launch_config<SS>(cfg);
+    const int rc = tc_launch_config<SS, ASYNC>(cfg);
     if (rc != PIV_OK) return rc;
     configured_dev = dev;
   }
   int grid = sm_count() * cfg.per_sm;
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc<SS><<<grid, 128, cfg.smem, stream>>>(a, a.status);
+  k_corr_tc<SS, ASYNC><<<grid, 128, cfg.smem, stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
+}
+
+template <int SS>
+static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
+  const long long total = (long long)a.n_pairs * a.m * a.n;
+  if (total == 0) return PIV_OK;
+  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
+  // Row starts on 16-byte boundaries: float frames, 16-byte aligned buffers,
+  // and widths, offsets and spacings that are multiples of four pixels.
+  const bool aligned = a.pixel_type == PIV_PIXEL_F32 && ((uintptr_t)a.frame_a % 16) == 0 &&
+                       ((uintptr_t)a.frame_b % 16) == 0 && a.width % 4 == 0 && a.x_offset % 4 == 0 &&
+                       a.spacing % 4 == 0;
+  return aligned ? launch_tc_t<SS, true>(a, stream) : launch_tc_t<SS, false>(a, stream);
 }
 
 int correlate_tensor(const CorrArgs& a, cudaStream_t stream) {

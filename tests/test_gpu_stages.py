@@ -382,27 +382,32 @@ def test_replacement_multi_pair_odd_field(env, method):
         np.testing.assert_array_equal(dval[k].cpu().numpy().astype(bool), rval)
 
 
-TC_CASES = [(16, "gaussian"), (32, "gaussian"), (16, "parabolic"), (32, "centroid"), (64, "gaussian"),
-            (64, "parabolic")]
+# (ss, subpixel, pixel type, frame shape). float frames with 16-byte aligned
+# rows take the engine's asynchronous staging for ss 16/32, 8-bit ones for ss
+# 64; the other combinations (and the 300-pixel width) load synchronously.
+TC_CASES = [(16, "gaussian", "u8", (256, 288)), (32, "gaussian", "f32", (256, 288)),
+            (16, "parabolic", "f32", (256, 288)), (32, "centroid", "u8", (256, 300)),
+            (64, "gaussian", "u8", (256, 288)), (64, "parabolic", "f32", (256, 288)),
+            (64, "gaussian", "u8", (256, 300))]
 
 
-@pytest.mark.parametrize("ss,subpix", TC_CASES)
-def test_tensor_correlation_accuracy(env, ss, subpix):
+@pytest.mark.parametrize("ss,subpix,pixel,shape", TC_CASES)
+def test_tensor_correlation_accuracy(env, ss, subpix, pixel, shape):
     """tcgen05 engine (fp16 operands, fp32 accumulation) against the float64
     oracle: displacement RMS within 0.01 px (the target accuracy of the tensor
     form), integer peaks equal except where the two largest map values are
     within fp16 resolution (relative 5e-3) or the window is fragile."""
     torch, _lib, lib = env
-    shape = (256, 288)
     fa, fb = _frames(300 + ss, shape, n_pairs=3)
     g = _geom(_lib, lib, shape, ss, 0.5)
     N = 2 * ss
-    da, db = torch.as_tensor(fa).cuda(), torch.as_tensor(fb).cuda()
+    dt = np.float32 if pixel == "f32" else np.uint8
+    da, db = torch.as_tensor(fa.astype(dt)).cuda(), torch.as_tensor(fb.astype(dt)).cuda()
     u = torch.empty((3, g.m, g.n), dtype=torch.float32, device="cuda")
     v = torch.empty_like(u)
     pi = torch.empty((3, g.m, g.n), dtype=torch.int32, device="cuda")
     pj = torch.empty_like(pi)
-    _lib.check(lib.piv_correlate(ctypes.byref(g), 3, da.data_ptr(), db.data_ptr(), 0, 0, N, 1,
+    _lib.check(lib.piv_correlate(ctypes.byref(g), 3, da.data_ptr(), db.data_ptr(), _lib.PIXEL[pixel], 0, N, 1,
                                  _lib.SUBPIXEL[subpix], None, u.data_ptr(), v.data_ptr(), pi.data_ptr(), pj.data_ptr(),
                                  0, 2, None, _lib.DFT["tensor"], _stream(torch)))
     field = po.Field(shape, ss, ss, 0.5, True, None, np.float64)
@@ -423,7 +428,7 @@ def test_tensor_correlation_accuracy(env, ss, subpix):
         errs.append(np.sqrt(du[ok] ** 2 + dv[ok] ** 2))
     e = np.concatenate(errs)
     rms = float(np.sqrt(np.mean(e ** 2)))
-    print(f"tensor ss={ss} {subpix}: rms {rms:.2e} px, max {e.max():.2e} px, excluded {n_excl}/{3 * g.m * g.n}")
+    print(f"tensor ss={ss} {subpix} {pixel} {shape}: rms {rms:.2e} px, max {e.max():.2e} px, excluded {n_excl}/{3 * g.m * g.n}")
     assert rms < 0.01
     assert e.max() < 0.1
 
