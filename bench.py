@@ -53,6 +53,7 @@ def parse_args():
     ap.add_argument("--dft", choices=["fft", "tensor"], default="tensor", help="correlation engine of the chosen form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
     return ap.parse_args()
 
 
@@ -336,7 +337,8 @@ def run_gpu(args):
     value = B * world / (ms_step * 1e-3)
     windows_per_pair = sum(f.n_wins for f in proc.piv_fields)
     plain = None
-    if args.dft != "fft":
+    proc_plain = None
+    if args.dft != "fft" and not args.no_plain:
         proc_plain = make("fft")
         ms_p, _, _ = graph_time(proc_plain)
         if dist:
@@ -428,7 +430,7 @@ def run_gpu(args):
         accuracy = {"form": args.dft, "rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64),
                     "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
                     "max_px_vs_fp32_oracle": float(max(np.abs(gu - u32).max(), np.abs(gv - v32).max()))}
-        if args.dft != "fft":
+        if proc_plain is not None:
             pu, pv = proc_plain.run_batch(fa[:1], fb[:1])
             pu, pv = pu[0].cpu().numpy(), pv[0].cpu().numpy()
             accuracy["plain_rms_px_vs_fp64_oracle"] = rms(pu, u64, pv, v64)
