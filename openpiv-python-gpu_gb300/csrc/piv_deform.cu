@@ -222,7 +222,7 @@ PIV_D AxisWeight axis_weight(int q, const AxisMap& a) {
   else if ((i + 1) * a.sp2 <= d2) ++i;
   i = i < 0 ? 0 : (i > a.len - 2 ? a.len - 2 : i);
   if (a.len < 2) i = 0;
-  const float t = a.len < 2 ? 0.0f : (float)(d2 - i * a.sp2) / (float)a.sp2;
+  const float t = a.len < 2 ? 0.0f : (float)(d2 - i * a.sp2) * a.inv_sp2;
   return AxisWeight{i, t};
 }
 PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
@@ -328,27 +328,21 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
 
 // ---------------------------------------------------------------------------
 // Cubic B-spline prefilter, mirror boundary. The exact prefilter (inverse of
-// the sampled cubic B-spline, one pole z = sqrt(3) - 2) is the symmetric
-// filter h[k] = sqrt(3) z^|k| applied to the mirror-extended frame. It runs
-// here as a separable FIR truncated at |k| <= 12: the dropped taps weigh
-// 2 sqrt(3) |z|^13 / (1 - |z|) < 2e-7 of the signal in total, below float32
-// rounding of the recursive form.
+// the sampled cubic B-spline, one pole z = sqrt(3) - 2, gain 6 per axis) is
+// the symmetric filter h[k] = sqrt(3) z^|k| applied to the mirror-extended
+// frame. Each CTA filters a 64 x 64 output tile from a 12-pixel mirrored halo
+// in shared memory with the causal / anti-causal recursions
+//   c+[k] = s[k] + z c+[k-1],   c-[k] = z (c-[k+1] - c+[k]),   c = 6 c-
+// started from zero at the halo's outer edge: the start-up error reaching the
+// tile is below |z|^12 / (1 - |z|) < 2e-7 of the signal, under float32
+// rounding of the recursion itself.
 // ---------------------------------------------------------------------------
-static constexpr int kFirK = 12;
-struct FirTaps {
-  float h[2 * kFirK + 1];
-};
-constexpr FirTaps make_fir_taps() {
-  FirTaps t{};
-  double zk = 1.0;
-  for (int k = 0; k <= kFirK; ++k) {
-    t.h[kFirK + k] = (float)(1.7320508075688772 * zk);
-    t.h[kFirK - k] = t.h[kFirK + k];
-    zk *= -0.2679491924311227;
-  }
-  return t;
-}
-__constant__ FirTaps c_fir = make_fir_taps();
+static constexpr int kPfK = 12;
+static constexpr int kPfT = 64;                    // output tile edge
+static constexpr int kPfR = kPfT + 2 * kPfK;       // region edge (a multiple of 8)
+static_assert(kPfR % 8 == 0, "the recursions run in chunks of eight");
+static constexpr int kPfS = kPfR + 1;              // odd row stride: conflict-free row and column walks
+static constexpr float kPole = -0.26794919243112270f;  // sqrt(3) - 2
 
 // Mirror ('d c b | a b c d | c b a') index for any integer q.
 PIV_D int mirror_any(int q, int n) {
@@ -359,71 +353,126 @@ PIV_D int mirror_any(int q, int n) {
   return q < n ? q : p - q;
 }
 
-static constexpr int kPfTx = 64, kPfTy = 32;
-static constexpr int kPfRy = kPfTy + 2 * kFirK, kPfRx = kPfTx + 2 * kFirK;
-static constexpr int kPfRxS = kPfRx + 1, kPfTxS = kPfTx + 1;  // odd strides: conflict-free column access
-
-// One CTA per 32 x 64 output tile of one frame: the tile and a 12-pixel
-// mirrored halo go to shared memory, the row FIR runs over every halo row,
-// then the column FIR writes the tile. P is the pixel type; the halo loads are
-// unrolled so that all of a thread's loads are in flight together.
 template <typename P>
-__global__ void __launch_bounds__(256) k_prefilter_fir(int H, int W, const P* __restrict__ in,
-                                                       float* __restrict__ out) {
-  __shared__ float reg[kPfRy * kPfRxS];
-  __shared__ float tmp[kPfRy * kPfTxS];
-  const int x0 = blockIdx.x * kPfTx, y0 = blockIdx.y * kPfTy;
+__global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __restrict__ in, float* __restrict__ out) {
+  __shared__ float reg[kPfR * kPfS];
+  const int x0 = blockIdx.x * kPfT, y0 = blockIdx.y * kPfT;
   const long long fbase = (long long)blockIdx.z * H * W;
-  constexpr int kLoads = (kPfRy * kPfRx + 255) / 256;
-  float vals[kLoads];
+  const P* src = in + fbase;
+  constexpr int kElems = kPfR * kPfR;
+  const bool interior = x0 >= kPfK && y0 >= kPfK && x0 + kPfT + kPfK <= W && y0 + kPfT + kPfK <= H;
+  if (sizeof(P) == 1 && interior && (W & 3) == 0 && ((uintptr_t)in & 3) == 0) {
+    // 8-bit frames away from the edges: the region's rows start on 4-byte
+    // boundaries (x0 - 12 is a multiple of 4), so each thread reads whole words.
+    constexpr int kWords = kPfR / 4, kTotal = kPfR * kWords;
+    const uint32_t* wsrc = reinterpret_cast<const uint32_t*>(src + (long long)(y0 - kPfK) * W + (x0 - kPfK));
+    const int wstride = W / 4;
+    uint32_t wv[(kTotal + 127) / 128];
 #pragma unroll
-  for (int u = 0; u < kLoads; ++u) {
-    const int e = threadIdx.x + 256 * u;
-    vals[u] = 0.f;
-    if (e < kPfRy * kPfRx) {
-      const int ry = e / kPfRx, rx = e % kPfRx;
-      int gy = y0 - kFirK + ry, gx = x0 - kFirK + rx;
-      if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
-      if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
-      vals[u] = (float)__ldg(in + fbase + (long long)gy * W + gx);
+    for (int u = 0; u < (kTotal + 127) / 128; ++u) {
+      const int e = threadIdx.x + 128 * u;
+      wv[u] = e < kTotal ? __ldg(wsrc + (long long)(e / kWords) * wstride + e % kWords) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < (kTotal + 127) / 128; ++u) {
+      const int e = threadIdx.x + 128 * u;
+      if (e < kTotal) {
+        float* d = reg + (e / kWords) * kPfS + 4 * (e % kWords);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) d[k] = (float)((wv[u] >> (8 * k)) & 0xffu);
+      }
+    }
+  } else {
+    // Any pixel type, mirrored edges: eight scalar loads per thread in flight.
+    for (int e0 = threadIdx.x; e0 < kElems; e0 += 128 * 8) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + 128 * u;
+        v[u] = 0.f;
+        if (e < kElems) {
+          const int ry = e / kPfR, rx = e % kPfR;
+          int gy = y0 - kPfK + ry, gx = x0 - kPfK + rx;
+          if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
+          if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
+          v[u] = (float)__ldg(src + (long long)gy * W + gx);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + 128 * u;
+        if (e < kElems) reg[(e / kPfR) * kPfS + e % kPfR] = v[u];
+      }
     }
   }
-#pragma unroll
-  for (int u = 0; u < kLoads; ++u) {
-    const int e = threadIdx.x + 256 * u;
-    if (e < kPfRy * kPfRx) reg[(e / kPfRx) * kPfRxS + e % kPfRx] = vals[u];
-  }
   __syncthreads();
-  // Row FIR: item = (segment of 8 outputs, halo row); a warp's lanes take consecutive rows.
-  for (int it = threadIdx.x; it < kPfRy * (kPfTx / 8); it += 256) {
-    const int r = it % kPfRy, c0 = (it / kPfRy) * 8;
-    const float* src = reg + r * kPfRxS + c0;
-    float v[8 + 2 * kFirK];
+  const float z = kPole;
+  // The recursions run in chunks of eight: the chunk's shared-memory reads
+  // are issued together, then the dependent chain runs in registers.
+  // Along x: one thread per region row; only the tile's columns are kept.
+  if (threadIdx.x < kPfR) {
+    float* row = reg + threadIdx.x * kPfS;
+    float c = 0.f;
+    for (int k0 = 0; k0 < kPfR; k0 += 8) {
+      float v[8];
 #pragma unroll
-    for (int k = 0; k < 8 + 2 * kFirK; ++k) v[k] = src[k];
+      for (int k = 0; k < 8; ++k) v[k] = row[k0 + k];
 #pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      float acc = 0.f;
+      for (int k = 0; k < 8; ++k) {
+        c = fmaf(z, c, v[k]);
+        v[k] = c;
+      }
 #pragma unroll
-      for (int k = 0; k <= 2 * kFirK; ++k) acc = fmaf(c_fir.h[k], v[o + k], acc);
-      tmp[r * kPfTxS + c0 + o] = acc;
+      for (int k = 0; k < 8; ++k) row[k0 + k] = v[k];
+    }
+    float d = 0.f;
+    for (int k0 = kPfR - 8; k0 + 8 > kPfK; k0 -= 8) {
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = row[k0 + k];
+#pragma unroll
+      for (int k = 7; k >= 0; --k) {
+        d = z * (d - v[k]);
+        v[k] = d;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) row[k0 + k] = v[k];
     }
   }
   __syncthreads();
-  // Column FIR: item = (column, segment of 8 output rows); lanes take consecutive columns.
-  for (int it = threadIdx.x; it < kPfTx * (kPfTy / 8); it += 256) {
-    const int c = it % kPfTx, r0 = (it / kPfTx) * 8;
-    float v[8 + 2 * kFirK];
+  // Along y: one thread per tile column; writes the tile with the gain 6 * 6.
+  if (threadIdx.x < kPfT) {
+    const int col = kPfK + threadIdx.x;
+    float c = 0.f;
+    for (int k0 = 0; k0 < kPfR; k0 += 8) {
+      float v[8];
 #pragma unroll
-    for (int k = 0; k < 8 + 2 * kFirK; ++k) v[k] = tmp[(r0 + k) * kPfTxS + c];
-    const int gx = x0 + c;
+      for (int k = 0; k < 8; ++k) v[k] = reg[(k0 + k) * kPfS + col];
 #pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      float acc = 0.f;
+      for (int k = 0; k < 8; ++k) {
+        c = fmaf(z, c, v[k]);
+        v[k] = c;
+      }
 #pragma unroll
-      for (int k = 0; k <= 2 * kFirK; ++k) acc = fmaf(c_fir.h[k], v[o + k], acc);
-      const int gy = y0 + r0 + o;
-      if (gx < W && gy < H) out[fbase + (long long)gy * W + gx] = acc;
+      for (int k = 0; k < 8; ++k) reg[(k0 + k) * kPfS + col] = v[k];
+    }
+    float d = 0.f;
+    const int gx = x0 + threadIdx.x;
+    float* dst = out + fbase + gx;
+    for (int k0 = kPfR - 8; k0 + 8 > kPfK; k0 -= 8) {
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = reg[(k0 + k) * kPfS + col];
+#pragma unroll
+      for (int k = 7; k >= 0; --k) {
+        d = z * (d - v[k]);
+        v[k] = d;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int gy = y0 + k0 + k - kPfK;
+        if (k0 + k >= kPfK && k0 + k < kPfK + kPfT && gx < W && gy < H) dst[(long long)gy * W] = 36.0f * v[k];
+      }
     }
   }
 }
@@ -432,15 +481,15 @@ int spline_prefilter(int H, int W, int n_frames, const void* frames, int pixel_t
                      cudaStream_t stream) {
   if ((long long)H * W * n_frames == 0) return PIV_OK;
   if (n_frames > 65535) return set_error(PIV_E_UNSUPPORTED, "spline prefilter: more than 65535 frames");
-  const dim3 grid((unsigned)((W + kPfTx - 1) / kPfTx), (unsigned)((H + kPfTy - 1) / kPfTy), (unsigned)n_frames);
+  const dim3 grid((unsigned)((W + kPfT - 1) / kPfT), (unsigned)((H + kPfT - 1) / kPfT), (unsigned)n_frames);
   switch (pixel_type) {
-    case PIV_PIXEL_U8: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const uint8_t*)frames, coef); break;
-    case PIV_PIXEL_U16: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const uint16_t*)frames, coef); break;
-    case PIV_PIXEL_F32: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const float*)frames, coef); break;
-    default: k_prefilter_fir<<<grid, 256, 0, stream>>>(H, W, (const double*)frames, coef); break;
+    case PIV_PIXEL_U8: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint8_t*)frames, coef); break;
+    case PIV_PIXEL_U16: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint16_t*)frames, coef); break;
+    case PIV_PIXEL_F32: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const float*)frames, coef); break;
+    default: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const double*)frames, coef); break;
   }
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_prefilter_fir launch");
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_prefilter launch");
 }
 
 }  // namespace piv

@@ -58,6 +58,11 @@ struct TcLayout {
   static constexpr size_t SMEM = END;
   static constexpr int MIN_BLOCKS = 512 / TCOLS;        // CTAs per SM that the TMEM allows
   static constexpr int CH = SS / 4;                     // 16-byte chunks per staged row
+  // Threads per TMEM lane: with two, every phase splits its frames, columns
+  // or row tiles between the pair, which doubles the warps an SM holds when
+  // the TMEM allows only two CTAs.
+  static constexpr int TPL = SS == 32 ? 2 : 1;
+  static constexpr int NT = 128 * TPL;
 };
 
 // Swizzled chunk position of chunk c of staged row t: the eight rows a
@@ -196,9 +201,9 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
 // current tile runs through its four products; otherwise each tile loads its
 // rows from global memory when it starts.
 template <int SS, bool ASYNC>
-__global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
+__global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
   using L = TcLayout<SS>;
-  constexpr int N = L::N, HN = L::HN, W = L::W, CH = L::CH;
+  constexpr int N = L::N, HN = L::HN, W = L::W, CH = L::CH, TPL = L::TPL, NT = L::NT;
   constexpr int NPART = N / 32;      // warps per window in the epilogue
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint64_t bar;
@@ -210,14 +215,16 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
   __shared__ int pk_idx[W][NPART];
 
   const int tid = threadIdx.x;
+  const int t = tid & 127;           // TMEM lane (row of the tile) of this thread
+  const int half = tid >> 7;         // which of the TPL threads of lane t
   const int warp = tid >> 5, lane = tid & 31;
-  const uint32_t lane_sel = (uint32_t)(32 * warp) << 16;
+  const uint32_t lane_sel = (uint32_t)(32 * (warp & 3)) << 16;
 
   // Constant DFT operands; the twiddles W_N^k = exp(-2 pi i k / N) sit in the
   // operand region until the first tile.
   float* tw_re = reinterpret_cast<float*>(sm + L::OP);
   float* tw_im = tw_re + N;
-  for (int k = tid; k < N; k += 128) {
+  for (int k = tid; k < N; k += NT) {
     float sn, cs;
     sincospif(2.0f * (float)k / (float)N, &sn, &cs);
     tw_re[k] = cs;
@@ -227,7 +234,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
   __syncthreads();
   const float inv_n = 1.0f / (float)N;
   const int p0 = SS / 2;
-  for (int e = tid; e < N * SS; e += 128) {  // F[k][x]
+  for (int e = tid; e < N * SS; e += NT) {  // F[k][x]
     const int k = e / SS, x = e % SS, f = k >> 1, q = (f * (x + p0)) % N;
     float v;
     if (k == 0) v = 1.0f;
@@ -235,7 +242,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     else v = (k & 1) ? tw_im[q] : tw_re[q];
     sth(sm + L::B1, off_k(k, x, SS), v);
   }
-  for (int e = tid; e < 4 * N * N; e += 128) {  // B3[n][kappa], kappa = (part, b, g)
+  for (int e = tid; e < 4 * N * N; e += NT) {  // B3[n][kappa], kappa = (part, b, g)
     const int n = e / (2 * N), kap = e % (2 * N);
     const int part = kap / N, b = (kap % N) / HN, g = kap % HN;
     const int fr = b == 0 ? g : (g == 0 ? HN : N - g), r = n % N;
@@ -244,7 +251,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     const float v = n < N ? (part == 0 ? cs : -sn) : (part == 0 ? sn : cs);
     sth(sm + L::B3, off_k(n, kap, 2 * N), v);
   }
-  for (int e = tid; e < N * N; e += 128) {  // B4[s][kappa], kappa = (part, c)
+  for (int e = tid; e < N * N; e += NT) {  // B4[s][kappa], kappa = (part, c)
     const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
     const int q = (c * s_) % N;
     float v;
@@ -294,17 +301,18 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
   };
-  // Thread t starts the copies of row t of both frames of the tile in slot `sl`.
+  // Thread (half, t) starts the copies of row t of its frames of the tile in slot `sl`.
   auto stage_async = [&](int sl) {
-    const int w = tid / SS, y = tid % SS;
+    const int w = t / SS, y = t % SS;
     if (!win_valid[sl][w]) return;
     const long long off = win_base[sl][w] + (long long)y * a.width;
 #pragma unroll
-    for (int f = 0; f < 2; ++f) {
+    for (int fi = 0; fi < 2 / TPL; ++fi) {
+      const int f = TPL == 2 ? half : fi;
       const float* src = reinterpret_cast<const float*>(f == 0 ? a.frame_a : a.frame_b) + off;
-      const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + tid) * SS * 4);
+      const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS * 4);
 #pragma unroll
-      for (int c = 0; c < CH; ++c) cp_async16(row + 16 * stg_chunk<CH>(tid, c), src + 4 * c);
+      for (int c = 0; c < CH; ++c) cp_async16(row + 16 * stg_chunk<CH>(t, c), src + 4 * c);
     }
   };
 
@@ -322,18 +330,19 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     if (ASYNC) cp_async_wait_all();
     __syncthreads();
 
-    // ---- Staging: thread (w, y) takes row y of window w of both frames.
+    // ---- Staging: thread (half, t = (w, y)) takes row y of window w of its frames.
     {
-      const int w = tid / SS, y = tid % SS;
+      const int w = t / SS, y = t % SS;
       const bool ok = win_valid[sl][w] != 0;
 #pragma unroll
-      for (int f = 0; f < 2; ++f) {
+      for (int fi = 0; fi < 2 / TPL; ++fi) {
+        const int f = TPL == 2 ? half : fi;
         float r[SS];
         if (ASYNC) {
-          const unsigned char* row = sm + L::STG + (f * 128 + tid) * SS * 4;
+          const unsigned char* row = sm + L::STG + (f * 128 + t) * SS * 4;
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
-            const float4 q4 = *reinterpret_cast<const float4*>(row + 16 * stg_chunk<CH>(tid, c));
+            const float4 q4 = *reinterpret_cast<const float4*>(row + 16 * stg_chunk<CH>(t, c));
             r[4 * c] = ok ? q4.x : 0.f;
             r[4 * c + 1] = ok ? q4.y : 0.f;
             r[4 * c + 2] = ok ? q4.z : 0.f;
@@ -364,7 +373,7 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
         for (int x = 0; x < SS; ++x) r[x] *= s;
         if (y == 0) sc_e[f][w] = e;
 #pragma unroll
-        for (int x = 0; x < SS; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(tid, x, SS), r + x);
+        for (int x = 0; x < SS; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, x, SS), r + x);
       }
     }
     sync_for_mma();
@@ -391,9 +400,10 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
     // (w, c) of tile e (k = 2c) and tile o (k = 2c + 1).
     {
-      const int w = tid / SS, y = tid % SS;
+      const int w = t / SS, y = t % SS;
 #pragma unroll
-      for (int f = 0; f < 2; ++f) {
+      for (int fi = 0; fi < 2 / TPL; ++fi) {
+        const int f = TPL == 2 ? half : fi;
         float v[N];
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16)
@@ -435,11 +445,12 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     // ---- Product: thread (w, c) forms row c of Q, K = (Re|Im, b, g) with
     // f_r = g (b = 0) or N - g (b = 1; g = 0 pairs with f_r = N/2).
     {
-      const bool special = (tid % HN) == 0;
+      const bool special = (t % HN) == 0;
       const float qs = 1.0f / 1024.0f;
       unsigned char* dst = sm + L::OP;
 #pragma unroll
-      for (int g0 = 0; g0 < HN; g0 += 8) {
+      for (int gi = 0; gi < HN / TPL; gi += 8) {
+        const int g0 = half * (HN / TPL) + gi;
         float ea[16], eb[16], oa[16], ob[16];
         tc::tmem_ld16(tmem + lane_sel + 0 * N + 2 * g0, ea);
         tc::tmem_ld16(tmem + lane_sel + 1 * N + 2 * g0, eb);
@@ -461,10 +472,10 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
           }
           qr0[i] = q.r0 * qs; qi0[i] = q.i0 * qs; qr1[i] = q.r1 * qs; qi1[i] = q.i1 * qs;
         }
-        st8(dst, off_k(tid, 0 * N + 0 * HN + g0, 2 * N), qr0);
-        st8(dst, off_k(tid, 0 * N + 1 * HN + g0, 2 * N), qr1);
-        st8(dst, off_k(tid, 1 * N + 0 * HN + g0, 2 * N), qi0);
-        st8(dst, off_k(tid, 1 * N + 1 * HN + g0, 2 * N), qi1);
+        st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
+        st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
+        st8(dst, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
+        st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
     }
     sync_for_mma();
@@ -484,9 +495,10 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
 
     // ---- Stage 3 -> 4: row (w, c) of U becomes columns (Re|Im, c) of the MN-major rows (w, r).
     {
-      const int w = tid / HN, c = tid % HN;
+      const int w = t / HN, c = t % HN;
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
+      for (int pi = 0; pi < 2 / TPL; ++pi) {
+        const int part = TPL == 2 ? half : pi;
         float v[N];
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16)
@@ -521,8 +533,9 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     // column j = s ^ N/2. Lags without window overlap (i = 0 or j = 0) are 0.
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
 #pragma unroll
-    for (int rt = 0; rt < 2; ++rt) {
-      const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
+    for (int ri = 0; ri < 2 / TPL; ++ri) {
+      const int rt = TPL == 2 ? half : ri;
+      const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
       float v[N];
 #pragma unroll
       for (int c0 = 0; c0 < N; c0 += 16)
@@ -568,8 +581,9 @@ __global__ void __launch_bounds__(128, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrA
     __syncthreads();
     // The rows next to the peak go to shared memory for the five-point fit.
 #pragma unroll
-    for (int rt = 0; rt < 2; ++rt) {
-      const int m = rt * 128 + tid, w = m / N, r = m % N, i = r ^ HN;
+    for (int ri = 0; ri < 2 / TPL; ++ri) {
+      const int rt = TPL == 2 ? half : ri;
+      const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
       const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
       const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
       if (__any_sync(0xffffffffu, mine)) {
@@ -1131,7 +1145,7 @@ static int tc_launch_config(TcLaunch& out) {
   const size_t per_cta = L::SMEM + fa.sharedSizeBytes + resv;
   int per_sm = 512 / L::TCOLS;
   const int by_smem = (int)(smem_sm / per_cta);
-  const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * 4;
+  const int regs_cta = ((fa.numRegs * 32 + 255) / 256) * 256 * (L::NT / 32);
   const int by_regs = regs_cta > 0 ? regs_sm / regs_cta : per_sm;
   per_sm = std::min(per_sm, std::min(by_smem, by_regs));
   if (per_sm < 1) return set_error(PIV_E_UNSUPPORTED, "tensor correlation does not fit on an SM");
@@ -1165,7 +1179,7 @@ static int launch_tc_t(const CorrArgs& a, cudaStream_t stream) {
   }
   int grid = sm_count() * cfg.per_sm;
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc<SS, ASYNC><<<grid, 128, cfg.smem, stream>>>(a, a.status);
+  k_corr_tc<SS, ASYNC><<<grid, L::NT, cfg.smem, stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
 }
