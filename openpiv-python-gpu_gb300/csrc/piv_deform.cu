@@ -158,34 +158,19 @@ PIV_D void bspline3_weights(float t, float* w) {
   w[3] = t3 * (1.0f / 6.0f);
 }
 
-// Cubic B-spline sample of the coefficient frame at (yi, xi) clamped into the
-// frame. Taps inside the frame are read directly; the mirror rule is only
-// evaluated for samples whose 4 x 4 support crosses an edge.
-PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi, float yi) {
-  xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
-  yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
+// Cubic B-spline sample at clamped (yi, xi) whose 4 x 4 support crosses an
+// edge: mirror taps. Kept out of line so that the interior path below stays a
+// short branch.
+__device__ __noinline__ float sample_cubic_edge(const float* __restrict__ coef, int W, int H, float xi, float yi) {
   const float fx = floorf(xi), fy = floorf(yi);
   float wx[4], wy[4];
   bspline3_weights(xi - fx, wx);
   bspline3_weights(yi - fy, wy);
   const int x0 = (int)fx - 1, y0 = (int)fy - 1;
-  float acc = 0.0f;
-  if (x0 >= 0 && x0 + 3 < W && y0 >= 0 && y0 + 3 < H) {
-    const float* p = coef + (y0 * W + x0);
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const float* row = p + r * W;
-      float s = wx[0] * __ldg(row);
-      s = fmaf(wx[1], __ldg(row + 1), s);
-      s = fmaf(wx[2], __ldg(row + 2), s);
-      s = fmaf(wx[3], __ldg(row + 3), s);
-      acc = fmaf(wy[r], s, acc);
-    }
-    return acc;
-  }
   int cx[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) cx[c] = mirror_index(x0 + c, W);
+  float acc = 0.0f;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const float* row = coef + mirror_index(y0 + r, H) * W;
@@ -193,6 +178,32 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
     s = fmaf(wx[1], __ldg(row + cx[1]), s);
     s = fmaf(wx[2], __ldg(row + cx[2]), s);
     s = fmaf(wx[3], __ldg(row + cx[3]), s);
+    acc = fmaf(wy[r], s, acc);
+  }
+  return acc;
+}
+
+// Cubic B-spline sample of the coefficient frame at (yi, xi) clamped into the
+// frame. Taps inside the frame are read directly; the mirror rule is only
+// evaluated for samples whose 4 x 4 support crosses an edge.
+PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi, float yi) {
+  xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
+  yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
+  const float fx = floorf(xi), fy = floorf(yi);
+  const int x0 = (int)fx - 1, y0 = (int)fy - 1;
+  if (x0 < 0 || x0 + 3 >= W || y0 < 0 || y0 + 3 >= H) return sample_cubic_edge(coef, W, H, xi, yi);
+  float wx[4], wy[4];
+  bspline3_weights(xi - fx, wx);
+  bspline3_weights(yi - fy, wy);
+  const float* p = coef + (y0 * W + x0);
+  float acc = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float* row = p + r * W;
+    float s = wx[0] * __ldg(row);
+    s = fmaf(wx[1], __ldg(row + 1), s);
+    s = fmaf(wx[2], __ldg(row + 2), s);
+    s = fmaf(wx[3], __ldg(row + 3), s);
     acc = fmaf(wy[r], s, acc);
   }
   return acc;
@@ -230,71 +241,84 @@ PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
 }
 
 static constexpr int kDeformThreads = 256;
-// Field columns one CTA of kDeformThreads pixels can touch (spacing >= 1).
+static constexpr int kDeformRows = 4;                       // image rows per CTA
+// Field columns / rows one CTA can touch (spacing >= 1).
 static constexpr int kDeformMaxCols = kDeformThreads + 2;
+static constexpr int kDeformMaxGridRows = kDeformRows + 1;
 
-// One thread per pixel of one row segment. The predictor (float32; the
-// reference evaluates it in float64 and casts to the frame type, a difference
-// of one or two float32 ulps) is interpolated along y once per field column
-// into shared memory, then along x per pixel. Frame A is sampled at
-// x + up*dta and frame B at x + up*dtb.
-// Launch grid: x over row segments, y over rows, z over pairs.
+// One thread per pixel column of a 4-row x 256-pixel block; each thread
+// handles the block's four rows. The predictor (float32; the reference
+// evaluates it in float64 and casts to the frame type, a difference of one or
+// two float32 ulps) is staged as the field rows and columns the block touches
+// and interpolated along y, then x. Frame A is sampled at x + up*dta and frame
+// B at x + up*dtb.
+// Launch grid: x over row segments, y over blocks of rows, z over pairs.
 template <typename T>
 __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap ax, AxisMap ay, T dta, T dtb,
                                                            int do_a, int do_b) {
-  __shared__ float su[kDeformMaxCols], sv[kDeformMaxCols];
-  __shared__ int s_klo;
+  __shared__ float su[kDeformMaxGridRows][kDeformMaxCols], sv[kDeformMaxGridRows][kDeformMaxCols];
+  __shared__ int s_klo, s_khi;
   const piv_geometry& g = a.geom;
   const int H = g.height, W = g.width;
   const int j0 = blockIdx.x * kDeformThreads;
   const int j = j0 + threadIdx.x;
-  const int i = blockIdx.y, pair = blockIdx.z;
-  const AxisWeight wy = axis_weight(i, ay);
-  if (threadIdx.x == 0) s_klo = axis_weight(j0, ax).i;
+  const int i0 = blockIdx.y * kDeformRows, pair = blockIdx.z;
+  const int i_last = min(i0 + kDeformRows, H) - 1;
+  const int r_lo = axis_weight(i0, ay).i;
+  const int r_hi = min(axis_weight(i_last, ay).i + 1, g.m - 1);
   const AxisWeight wx = axis_weight(min(j, W - 1), ax);
-  // The last thread of the segment knows the highest field column it needs.
-  __shared__ int s_khi;
+  if (threadIdx.x == 0) s_klo = axis_weight(j0, ax).i;
   if (threadIdx.x == kDeformThreads - 1 || j == W - 1) s_khi = min(wx.i + 1, g.n - 1);
   __syncthreads();
   const int k_lo = s_klo, k_hi = s_khi;
+  const int nc = k_hi - k_lo + 1, nr = r_hi - r_lo + 1;
   const long long fo = (long long)pair * g.m * g.n;
-  const int iy1 = g.m < 2 ? wy.i : wy.i + 1;
-  for (int k = k_lo + threadIdx.x; k <= k_hi; k += kDeformThreads) {
-    const double* u = a.up + fo;
-    const double* v = a.vp + fo;
-    const float u0 = (float)__ldg(u + wy.i * g.n + k), u1 = (float)__ldg(u + iy1 * g.n + k);
-    const float v0 = (float)__ldg(v + wy.i * g.n + k), v1 = (float)__ldg(v + iy1 * g.n + k);
-    su[k - k_lo] = fmaf(wy.t, u1 - u0, u0);
-    sv[k - k_lo] = fmaf(wy.t, v1 - v0, v0);
+  for (int e = threadIdx.x; e < nr * nc; e += kDeformThreads) {
+    const int r = e / nc, c = e % nc;
+    const long long q = fo + (long long)(r_lo + r) * g.n + k_lo + c;
+    su[r][c] = (float)__ldg(a.up + q);
+    sv[r][c] = (float)__ldg(a.vp + q);
   }
   __syncthreads();
   if (j >= W) return;
   const long long base = (long long)pair * H * W;
-  const int p = i * W + j;
   T* out_a = reinterpret_cast<T*>(a.out_a) + base;
   T* out_b = reinterpret_cast<T*>(a.out_b) + base;
-  if (a.frame_mask && a.frame_mask[p]) {
-    out_a[p] = (T)0;
-    out_b[p] = (T)0;
-    return;
-  }
   const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
-  const T x = (T)j, y = (T)i;
-  const T up = (T)fmaf(wx.t, su[c1] - su[c0], su[c0]);
-  const T vp = (T)fmaf(wx.t, sv[c1] - sv[c0], sv[c0]);
-  if (do_a) {
-    const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
-    out_a[p] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
-                            : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
-  } else {
-    out_a[p] = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
-  }
-  if (do_b) {
-    const T xi = add_rn(x, mul_rn(up, dtb)), yi = add_rn(y, mul_rn(vp, dtb));
-    out_b[p] = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
-                            : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
-  } else {
-    out_b[p] = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
+  const T x = (T)j;
+#pragma unroll
+  for (int rr = 0; rr < kDeformRows; ++rr) {
+    const int i = i0 + rr;
+    if (i > i_last) break;
+    const int p = i * W + j;
+    if (a.frame_mask && a.frame_mask[p]) {
+      out_a[p] = (T)0;
+      out_b[p] = (T)0;
+      continue;
+    }
+    const AxisWeight wy = axis_weight(i, ay);
+    const int y0r = wy.i - r_lo, y1r = (g.m < 2 ? wy.i : wy.i + 1) - r_lo;
+    const float u0 = fmaf(wy.t, su[y1r][c0] - su[y0r][c0], su[y0r][c0]);
+    const float u1 = fmaf(wy.t, su[y1r][c1] - su[y0r][c1], su[y0r][c1]);
+    const float v0 = fmaf(wy.t, sv[y1r][c0] - sv[y0r][c0], sv[y0r][c0]);
+    const float v1 = fmaf(wy.t, sv[y1r][c1] - sv[y0r][c1], sv[y0r][c1]);
+    const T up = (T)fmaf(wx.t, u1 - u0, u0);
+    const T vp = (T)fmaf(wx.t, v1 - v0, v0);
+    const T y = (T)i;
+    if (do_a) {
+      const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
+      out_a[p] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
+                              : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
+    } else {
+      out_a[p] = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
+    }
+    if (do_b) {
+      const T xi = add_rn(x, mul_rn(up, dtb)), yi = add_rn(y, mul_rn(vp, dtb));
+      out_b[p] = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
+                              : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
+    } else {
+      out_b[p] = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
+    }
   }
 }
 
@@ -310,10 +334,9 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   if (dp > 0 && dp < 1) { dta = dp - 1; dtb = dp; do_a = do_b = 1; }
   else if (dp == 1) { dtb = 1; do_b = 1; }
   else { dta = -1; do_a = 1; }
-  if (a.geom.height > 65535 || a.n_pairs > 65535)
-    return set_error(PIV_E_UNSUPPORTED, "deformation grid limit (height and pairs <= 65535)");
-  const dim3 grid((unsigned)((a.geom.width + kDeformThreads - 1) / kDeformThreads), (unsigned)a.geom.height,
-                  (unsigned)a.n_pairs);
+  if (a.n_pairs > 65535) return set_error(PIV_E_UNSUPPORTED, "deformation grid limit (pairs <= 65535)");
+  const dim3 grid((unsigned)((a.geom.width + kDeformThreads - 1) / kDeformThreads),
+                  (unsigned)((a.geom.height + kDeformRows - 1) / kDeformRows), (unsigned)a.n_pairs);
   if ((long long)a.geom.height * a.geom.width > 2147483647LL)
     return set_error(PIV_E_UNSUPPORTED, "deformation: frames above 2^31 pixels");
   const AxisMap ax = axis_map(a.geom.search_size, a.geom.x_offset, a.geom.spacing, a.geom.n);
