@@ -14,14 +14,15 @@
 //            tile e holds the rows k = 2c of T^T (Re T, or the DC column),
 //            tile o the rows k = 2c + 1 (Im T, or the Nyquist column), so
 //            each thread finds both halves of its complex column in its own lane.
-//   product  Q(f_r, c) = 2^-10 conj(A) B for c = 1 .. N/2-1 and all f_r; row c = 0
+//   product  Q(f_r, c) = conj(A) B for c = 1 .. N/2-1 and all f_r; row c = 0
 //            packs the two real-input columns: Q = conj(A0) B0 + i conj(AN) BN.
 //   stage 3  U = Q E / N rows (w, c),              K = (Re|Im, f_r), cols (Re|Im, r)
 //   stage 4  c = U E' / N rows (w, r),             K = (Re|Im, c),   cols s
 // where E is the inverse DFT along f_r and E' the real inverse along f_c
 // (U(r, N-c) = conj U(r, c)). Each frame's window is scaled by a power of two
-// 2^e with sum |2^e (a - mean)| <= 2^12, so every fp16 operand stays below
-// 2^15; the map is scaled back exactly by 2^(10 - e_a - e_b). The map in TMEM
+// 2^e with sum |2^e (a - mean)| <= 2^7, so every spectrum stays below 2^7 and
+// every fp16 operand below 2^15; the map is scaled back exactly by
+// 2^-(e_a + e_b). The map in TMEM
 // (one row per lane) then goes through the same peak search and subpixel fit
 // as the FFT engine: first maximum in the fftshift-ed row-major order, lags
 // without window overlap read as exact zeros.
@@ -177,22 +178,26 @@ PIV_D void load_row(const void* frame, int pixel_type, long long off, bool ok, f
 
 static constexpr uint32_t kMaxPolls = 1u << 24;
 
-// Product of one frequency pair: the outputs at f_r = g (q0) and f_r = N - g
-// (q1) from the spectra E (even row) and O (odd row) of frames a and b at f_r = g.
+// Product of one frequency pair: the outputs at f_r = g (r0, i0) and f_r = N - g
+// (r1, i1) from the spectra E (even row) and O (odd row) of frames a and b at
+// f_r = g. General rows: conj(A) B with A = E_a + i O_a, B = E_b + i O_b; at
+// N - g the real-input spectra are conjugated, A' = conj(E_a) + i conj(O_a).
+// Row c = 0 (`special`) packs the two real-input columns:
+// conj(E_a) E_b + i conj(O_a) O_b, and E_a conj(E_b) + i O_a conj(O_b) at N - g.
 struct PairQ {
   float r0, i0, r1, i1;
 };
 PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, float bi, float pr, float pi,
                          bool special) {
-  const float re1 = fmaf(ar, br, ai * bi), im1 = fmaf(ar, bi, -ai * br);     // conj(Ea) Eb
-  const float re2 = fmaf(orr, pr, oi * pi), im2 = fmaf(orr, pi, -oi * pr);   // conj(Oa) Ob
-  const float re3 = fmaf(ar, pr, ai * pi), im3 = fmaf(ar, pi, -ai * pr);     // conj(Ea) Ob
-  const float re4 = fmaf(orr, br, oi * bi), im4 = fmaf(orr, bi, -oi * br);   // conj(Oa) Eb
+  const float xr = ar - oi, xi = ai + orr, yr = br - pi, yi = bi + pr;        // A, B
+  const float xpr = ar + oi, xpi = orr - ai, ypr = br + pi, ypi = pr - bi;    // A', B'
+  const float re1 = fmaf(ar, br, ai * bi), im1 = fmaf(ar, bi, -ai * br);     // conj(E_a) E_b
+  const float re2 = fmaf(orr, pr, oi * pi), im2 = fmaf(orr, pi, -oi * pr);   // conj(O_a) O_b
   PairQ q;
-  q.r0 = special ? re1 - im2 : (re1 + re2) + (im4 - im3);
-  q.i0 = special ? im1 + re2 : (im1 + im2) + (re3 - re4);
-  q.r1 = special ? re1 + im2 : (re1 + re2) - (im4 - im3);
-  q.i1 = special ? re2 - im1 : (re3 - re4) - (im1 + im2);
+  q.r0 = special ? re1 - im2 : fmaf(xr, yr, xi * yi);
+  q.i0 = special ? im1 + re2 : fmaf(xr, yi, -xi * yr);
+  q.r1 = special ? re1 + im2 : fmaf(xpr, ypr, xpi * ypi);
+  q.i1 = special ? re2 - im1 : fmaf(xpr, ypi, -xpi * ypr);
   return q;
 }
 
@@ -367,7 +372,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
 #pragma unroll
         for (int o = 1; o < SS; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
         int e = 0;
-        if (l > 0.f) e = min(120, max(-120, 11 - ilogbf(l)));
+        if (l > 0.f) e = min(120, max(-120, 6 - ilogbf(l)));
         const float s = pow2i(e);
 #pragma unroll
         for (int x = 0; x < SS; ++x) r[x] *= s;
@@ -446,7 +451,6 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
     // f_r = g (b = 0) or N - g (b = 1; g = 0 pairs with f_r = N/2).
     {
       const bool special = (t % HN) == 0;
-      const float qs = 1.0f / 1024.0f;
       unsigned char* dst = sm + L::OP;
 #pragma unroll
       for (int gi = 0; gi < HN / TPL; gi += 8) {
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
             q = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
                              ob[2 * i], ob[2 * i + 1], special);
           }
-          qr0[i] = q.r0 * qs; qi0[i] = q.i0 * qs; qr1[i] = q.r1 * qs; qi1[i] = q.i1 * qs;
+          qr0[i] = q.r0; qi0[i] = q.i0; qr1[i] = q.r1; qi1[i] = q.i1;
         }
         st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
         st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
@@ -529,7 +533,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
     if (!wait_mma()) break;
 
     // ---- Epilogue. Row rt*128 + tid of the tile is map row r of window w
-    // (scaled by 2^-(10 - e_a - e_b)); shifted row index i = r ^ N/2, shifted
+    // (scaled by 2^(e_a + e_b)); shifted row index i = r ^ N/2, shifted
     // column j = s ^ N/2. Lags without window overlap (i = 0 or j = 0) are 0.
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
 #pragma unroll
@@ -560,7 +564,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         pk_idx[w][r / 32] = idx;
       }
       if (a.maps && g0 + w < total) {
-        const int ue = 10 - sc_e[0][w] - sc_e[1][w];
+        const int ue = -sc_e[0][w] - sc_e[1][w];
         float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
 #pragma unroll
         for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
@@ -606,7 +610,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
       const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-        const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
+        const int ue = -sc_e[0][ww] - sc_e[1][ww];
         // Shifted (i, j) -> stored row slot i - pi + 1, natural column j ^ N/2.
         auto at = [&](int i, int j) -> float {
           return (i == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (i - pi_ + 1)) * N + (j ^ HN)], ue);
@@ -828,7 +832,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       __syncthreads();
       const float l1 = red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3];
       int e = 0;
-      if (l1 > 0.f) e = min(120, max(-120, 11 - ilogbf(l1)));
+      if (l1 > 0.f) e = min(120, max(-120, 6 - ilogbf(l1)));
       const float s = pow2i(e);
 #pragma unroll
       for (int x = 0; x < 32; ++x) r[x] *= s;
@@ -900,7 +904,6 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     // ---- Product: thread (q, t) forms g in [16 q, 16 q + 16) of row c = t % HN of window t / HN.
     {
       const bool special = (t % HN) == 0;
-      const float qs = 1.0f / 1024.0f;
       unsigned char* dst = sm + L::OP;
 #pragma unroll
       for (int gc = 0; gc < 16; gc += 8) {
@@ -923,7 +926,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
             pq = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
                               ob[2 * i], ob[2 * i + 1], special);
           }
-          qr0[i] = pq.r0 * qs; qi0[i] = pq.i0 * qs; qr1[i] = pq.r1 * qs; qi1[i] = pq.i1 * qs;
+          qr0[i] = pq.r0; qi0[i] = pq.i0; qr1[i] = pq.r1; qi1[i] = pq.i1;
         }
         st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
         st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
@@ -1012,7 +1015,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         pk_idx[w][ch * 4 + (t >> 5)] = idx;
       }
       if (a.maps && g0 + w < total) {
-        const int ue = 10 - sc_e[0][w] - sc_e[1][w];
+        const int ue = -sc_e[0][w] - sc_e[1][w];
         float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
 #pragma unroll
         for (int k = 0; k < 64; ++k) mo[k] = i == 0 ? 0.f : ldexpf(v[k], ue);
@@ -1054,7 +1057,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-        const int ue = 10 - sc_e[0][ww] - sc_e[1][ww];
+        const int ue = -sc_e[0][ww] - sc_e[1][ww];
         auto at = [&](int ii, int j) -> float {
           return (ii == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)], ue);
         };
