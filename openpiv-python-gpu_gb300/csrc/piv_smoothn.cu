@@ -106,6 +106,17 @@ __global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, d
 
 static constexpr int kGcvThreads = 512;
 
+// 1/d for d >= 1 from the float32 reciprocal and two Newton steps in float64:
+// within an ulp or two of the rounded quotient, at a fraction of the cost of
+// a float64 division (float64 throughput on this GPU is low).
+PIV_D double rcp_fast(double d) {
+  double r = (double)__frcp_rn((float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 struct GcvEval {
   const double* f2;
   const double* lam2;
@@ -119,7 +130,7 @@ PIV_D double gcv_score(const GcvEval& g, double p, double* red) {
   const double s = pow(10.0, p);
   double rss = 0.0, tr = 0.0;
   for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
-    const double gm = 1.0 / (1.0 + s * g.lam2[e]);
+    const double gm = rcp_fast(1.0 + s * g.lam2[e]);
     const double d = gm - 1.0;
     rss += g.f2[e] * d * d;
     tr += gm;
@@ -214,15 +225,19 @@ k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __
   if (threadIdx.x == 0) p_out[pair] = p;
 }
 
-// fd *= gamma(p) for both fields of each pair.
+// fd *= gamma(p) for both fields of each pair. Grid: x over the 2 mn
+// coefficients of a pair, y over pairs; s = 10^p is formed once per CTA.
 __global__ void k_apply_gamma(long long mn, int n_pairs, const double* __restrict__ lam2,
                               const double* __restrict__ p, double fixed_p, double* __restrict__ fd) {
+  __shared__ double s_sh;
+  const int pair = blockIdx.y;
+  if (threadIdx.x == 0) s_sh = pow(10.0, p ? p[pair] : fixed_p);
+  __syncthreads();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2 * mn * n_pairs) return;
-  const long long pair = t / (2 * mn), e = t % mn;
-  const double pp = p ? p[pair] : fixed_p;
-  const double s = pow(10.0, pp);
-  fd[t] = (1.0 / (1.0 + s * lam2[e])) * fd[t];
+  if (t >= 2 * mn) return;
+  const long long e = t % mn;
+  double* f = fd + (long long)pair * 2 * mn + t;
+  *f = rcp_fast(1.0 + s_sh * lam2[e]) * *f;
 }
 
 __global__ void k_fill(int count, double value, double* out) {
@@ -281,7 +296,9 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
   } else {
     fixed_p = log10(s);
   }
-  k_apply_gamma<<<grid, bs, 0, stream>>>(mn, n_pairs, sc.lam2, pvec, fixed_p, sc.tmp);
+  if (n_pairs > 65535) return set_error(PIV_E_UNSUPPORTED, "smoothn: more than 65535 pairs in one call");
+  k_apply_gamma<<<dim3((unsigned)((2 * mn + bs - 1) / bs), (unsigned)n_pairs), bs, 0, stream>>>(mn, n_pairs, sc.lam2,
+                                                                                               pvec, fixed_p, sc.tmp);
   // Inverse DCT (DCT-III): rows then columns.
   k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 1, sc.cn, sc.tmp, sc.fd);
   k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 3, sc.cm, sc.fd, sc.tmp);

@@ -43,7 +43,7 @@ PIV_D T median_of(T* a, int n) {
   if (n == 0) return (T)NAN;
   sort_small(a, n);
   const T lo = a[(n - 1) / 2], hi = a[n / 2];
-  return div_rn(add_rn(lo, hi), (T)2);
+  return mul_rn(add_rn(lo, hi), (T)0.5);  // exact: the same value as the division by 2
 }
 
 // numpy's pairwise summation (n <= 128 branch) of n values.
@@ -87,9 +87,67 @@ PIV_D T fv_at(const FieldView& v, int i, int j) {
   return (T)v.f[p];
 }
 
+// Order-preserving integer keys: signed comparison of the keys orders the
+// values like the floating-point comparison (-0 sorts below +0). The sorting
+// network then runs on the integer ALUs; float64 min/max are slow here.
+PIV_D int sort_key(float v) {
+  const int b = __float_as_int(v);
+  return b ^ ((b >> 31) & 0x7fffffff);
+}
+PIV_D long long sort_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+PIV_D float key_value(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+PIV_D double key_value(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
+
+// Median (kind 0) or MAD (kind 2, |v - med|) of the eight neighbours of (i, j)
+// in registers: missing values sort last as +inf, a 19-comparator network
+// (Batcher's odd-even merge) sorts their keys, and the middle pair of the cnt
+// valid values is picked by selects. Same result as median_of on the valid
+// values.
+template <typename T>
+PIV_D T median8(const FieldView& fv, int i, int j, int kind, T med) {
+  using K = decltype(sort_key(T(0)));
+  K a[8];
+  int cnt = 0, k = 0;
+#pragma unroll
+  for (int di = -1; di <= 1; ++di)
+#pragma unroll
+    for (int dj = -1; dj <= 1; ++dj) {
+      if (di == 0 && dj == 0) continue;
+      T v = fv_at<T>(fv, i + di, j + dj);
+      const bool ok = !is_nan(v);
+      if (kind == 2) v = fabs(sub_rn(v, med));
+      a[k++] = sort_key(ok ? v : (T)INFINITY);
+      cnt += ok ? 1 : 0;
+    }
+  auto cx = [&](int x, int y) {
+    const K lo = min(a[x], a[y]), hi = max(a[x], a[y]);
+    a[x] = lo;
+    a[y] = hi;
+  };
+  cx(0, 1); cx(2, 3); cx(4, 5); cx(6, 7);
+  cx(0, 2); cx(1, 3); cx(4, 6); cx(5, 7);
+  cx(1, 2); cx(5, 6);
+  cx(0, 4); cx(1, 5); cx(2, 6); cx(3, 7);
+  cx(2, 4); cx(3, 5);
+  cx(1, 2); cx(3, 4); cx(5, 6);
+  if (cnt == 0) return (T)NAN;
+  const int il = (cnt - 1) / 2, ih = cnt / 2;
+  K lo = a[0], hi = a[0];
+#pragma unroll
+  for (int q = 1; q < 8; ++q) {
+    lo = il == q ? a[q] : lo;
+    hi = ih == q ? a[q] : hi;
+  }
+  return mul_rn(add_rn(key_value(lo), key_value(hi)), (T)0.5);  // exact: the same value as the division by 2
+}
+
 // Neighbourhood statistics at (i, j): kind 0 median, 1 mean, 2 MAD (needs med).
 template <typename T>
 PIV_D T nbr_stat(const FieldView& fv, int i, int j, int s, int kind, T med) {
+  if (s == 1 && kind != 1) return median8<T>(fv, i, j, kind, med);
   T vals[kMaxNbrs];
   const int k = 2 * s + 1;
   if (kind == 1) {
