@@ -96,6 +96,105 @@ __global__ void k_dct_apply(int m, int n, int batch, int mode, const double* __r
   out[t] = acc;
 }
 
+// The orthonormal DCT-II matrix has C[k][L-1-i] = (-1)^k C[k][i], so along a
+// line of length L the forward transform needs only the sums x[i] + x[L-1-i]
+// (even k) or differences (odd k) of the first L/2 positions, and the inverse
+// gives x[i] and x[L-1-i] from one pass over the even and the odd k: half the
+// float64 multiply-adds of the plain product. One CTA takes 32 lines staged
+// in shared memory as [position][line]; `cols` selects lines along the
+// columns of the [m][n] fields (stride n) instead of along the rows.
+// Lines up to 90 long keep the staging under the default 48 KB of shared memory.
+static constexpr int kDctLines = 32, kDctThreads = 256, kDctMaxLen = 90;
+
+template <bool INV>
+__global__ void __launch_bounds__(kDctThreads) k_dct_lines(int m, int n, int batch, int cols, const double* __restrict__ c,
+                                                           const double* __restrict__ in, double* __restrict__ out) {
+  extern __shared__ double dsm[];
+  const int L = cols ? m : n;
+  const long long mn = (long long)m * n;
+  const long long n_lines = (long long)batch * (cols ? n : m);
+  const long long l0 = (long long)blockIdx.x * kDctLines;
+  constexpr int S = kDctLines + 1;           // odd stride (in doubles): conflict-free rows of 32 lines
+  double* xs = dsm;                          // [L][S]
+  double* es = dsm + L * S;                  // [h][S] sums, then outputs
+  double* os = es + ((L + 1) / 2) * S;       // [h][S] differences
+  const int h = L / 2, hc = (L + 1) / 2;
+  auto addr = [&](long long line, int e) -> long long {
+    if (cols) {
+      const long long f = line / n, col = line % n;
+      return f * mn + (long long)e * n + col;
+    }
+    return line * n + e;
+  };
+  // Load: coalesced along the line for rows, across lines for columns.
+  for (int idx = threadIdx.x; idx < kDctLines * L; idx += kDctThreads) {
+    int e, l;
+    if (cols) { e = idx / kDctLines; l = idx % kDctLines; }
+    else { l = idx / L; e = idx % L; }
+    const long long line = l0 + l;
+    xs[e * S + l] = line < n_lines ? in[addr(line, e)] : 0.0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kDctThreads / 32;
+  if (!INV) {
+    for (int i = warp; i < h; i += nw) {
+      const double a = xs[i * S + lane], b = xs[(L - 1 - i) * S + lane];
+      es[i * S + lane] = a + b;
+      os[i * S + lane] = a - b;
+    }
+    __syncthreads();
+    // y[k] into xs (the inputs are no longer needed once es/os are built).
+    const double mid = (L & 1) ? xs[h * S + lane] : 0.0;
+    __syncthreads();
+    for (int k = warp; k < L; k += nw) {
+      const double* src = (k & 1) ? os : es;
+      const double* ck = c + (long long)k * L;
+      double acc = (L & 1) ? ck[h] * mid : 0.0;
+      for (int i = 0; i < h; ++i) acc = fma(ck[i], src[i * S + lane], acc);
+      xs[k * S + lane] = acc;
+    }
+  } else {
+    for (int i = warp; i < hc; i += nw) {
+      double ev = 0.0, od = 0.0;
+      for (int k = 0; k < L; k += 2) ev = fma(c[(long long)k * L + i], xs[k * S + lane], ev);
+      for (int k = 1; k < L; k += 2) od = fma(c[(long long)k * L + i], xs[k * S + lane], od);
+      es[i * S + lane] = ev + od;         // x[i]
+      os[i * S + lane] = ev - od;         // x[L-1-i]
+    }
+    __syncthreads();
+    for (int i = warp; i < hc; i += nw) {
+      xs[i * S + lane] = es[i * S + lane];
+      if (L - 1 - i != i) xs[(L - 1 - i) * S + lane] = os[i * S + lane];
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kDctLines * L; idx += kDctThreads) {
+    int e, l;
+    if (cols) { e = idx / kDctLines; l = idx % kDctLines; }
+    else { l = idx / L; e = idx % L; }
+    const long long line = l0 + l;
+    if (line < n_lines) out[addr(line, e)] = xs[e * S + l];
+  }
+}
+
+// One DCT pass over `batch` fields: forward (DCT-II) or inverse (DCT-III)
+// along rows (cols = 0, matrix c of size n) or columns (cols = 1, size m).
+static void dct_pass(int m, int n, int batch, bool inverse, int cols, const double* c, const double* in, double* out,
+                     cudaStream_t stream) {
+  const int L = cols ? m : n;
+  const long long n_lines = (long long)batch * (cols ? n : m);
+  if (L > kDctMaxLen) {
+    const long long tot = (long long)m * n * batch;
+    const int mode = cols ? (inverse ? 3 : 2) : (inverse ? 1 : 0);
+    k_dct_apply<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(m, n, batch, mode, c, in, out);
+    return;
+  }
+  const size_t smem = (size_t)(L + 2 * ((L + 1) / 2)) * (kDctLines + 1) * sizeof(double);
+  const unsigned grid = (unsigned)((n_lines + kDctLines - 1) / kDctLines);
+  if (inverse) k_dct_lines<true><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, c, in, out);
+  else k_dct_lines<false><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, c, in, out);
+}
+
 __global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, double* __restrict__ f2) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= mn * n_pairs) return;
@@ -270,11 +369,9 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
     cudaMemcpy2DAsync(sc.tmp + f * mn, 2 * mn * 8, f == 0 ? u_in : v_in, mn * 8, mn * 8, n_pairs,
                       cudaMemcpyDeviceToDevice, stream);
   }
-  const long long tot = 2 * mn * n_pairs;
-  const unsigned grid = (unsigned)((tot + bs - 1) / bs);
   // Forward DCT-II: rows then columns.
-  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 0, sc.cn, sc.tmp, sc.fd);
-  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 2, sc.cm, sc.fd, sc.tmp);
+  dct_pass(m, n, 2 * n_pairs, false, 0, sc.cn, sc.tmp, sc.fd, stream);
+  dct_pass(m, n, 2 * n_pairs, false, 1, sc.cm, sc.fd, sc.tmp, stream);
   int rc = check("smoothn forward dct");
   if (rc) return rc;
   // tmp now holds the DCT coefficients.
@@ -300,8 +397,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
   k_apply_gamma<<<dim3((unsigned)((2 * mn + bs - 1) / bs), (unsigned)n_pairs), bs, 0, stream>>>(mn, n_pairs, sc.lam2,
                                                                                                pvec, fixed_p, sc.tmp);
   // Inverse DCT (DCT-III): rows then columns.
-  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 1, sc.cn, sc.tmp, sc.fd);
-  k_dct_apply<<<grid, bs, 0, stream>>>(m, n, 2 * n_pairs, 3, sc.cm, sc.fd, sc.tmp);
+  dct_pass(m, n, 2 * n_pairs, true, 0, sc.cn, sc.tmp, sc.fd, stream);
+  dct_pass(m, n, 2 * n_pairs, true, 1, sc.cm, sc.fd, sc.tmp, stream);
   for (int f = 0; f < 2; ++f) {
     cudaMemcpy2DAsync(f == 0 ? u_out : v_out, mn * 8, sc.tmp + f * mn, 2 * mn * 8, mn * 8, n_pairs,
                       cudaMemcpyDeviceToDevice, stream);

@@ -313,7 +313,7 @@ def test_replacement_all_outliers_gives_zero(env):
     np.testing.assert_array_equal(du.cpu().numpy(), np.zeros(shape))
 
 
-@pytest.mark.parametrize("shape", [(31, 31), (63, 63), (15, 23), (127, 127)])
+@pytest.mark.parametrize("shape", [(31, 31), (63, 63), (15, 23), (127, 127), (20, 32), (64, 90)])
 @pytest.mark.parametrize("s", [0.8, None])
 def test_smoothn_matches_oracle(env, shape, s):
     torch, _lib, lib = env
