@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap
   T* out_b = reinterpret_cast<T*>(a.out_b) + base;
   const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
   const T x = (T)j;
-#pragma unroll
+#pragma unroll 1
   for (int rr = 0; rr < kDeformRows; ++rr) {
     const int i = i0 + rr;
     if (i > i_last) break;

@@ -256,6 +256,32 @@ PIV_D double gcv_grad(const GcvEval& g, double p, double f0, double pmax, double
   return (f0 - gcv_score(g, p - h, red)) / h;
 }
 
+// GCV score in float32 arithmetic (float64 block reduction): enough to rank the
+// ten scan points, whose scores differ by far more than its error.
+PIV_D double gcv_score_f32(const GcvEval& g, double p, double* red) {
+  const float s = (float)pow(10.0, p);
+  float rss = 0.f, tr = 0.f;
+  for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
+    const float gm = __frcp_rn(fmaf(s, (float)g.lam2[e], 1.0f));
+    const float d = gm - 1.0f;
+    rss = fmaf((float)g.f2[e] * d, d, rss);
+    tr += gm;
+  }
+  double drss = rss, dtr = tr;
+  for (int o = 16; o > 0; o >>= 1) {
+    drss += __shfl_xor_sync(~0u, drss, o);
+    dtr += __shfl_xor_sync(~0u, dtr, o);
+  }
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { red[w] = drss; red[32 + w] = dtr; }
+  __syncthreads();
+  double trss = 0.0, ttr = 0.0;
+  for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
+  const double q = 1.0 - ttr / (double)g.mn;
+  return trss / g.n_finite / (q * q) / g.n_fields;
+}
+
 __global__ void __launch_bounds__(kGcvThreads)
 k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2, double pmin,
       double pmax, double* __restrict__ p_out) {
@@ -263,17 +289,16 @@ k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __
   const int pair = blockIdx.x;
   const long long mn = (long long)m * n;
   GcvEval g{f2 + pair * mn, lam2, mn, (double)mn, 2};
-  // 10-point scan.
+  // 10-point scan (gpu_smoothn.py:182-188), ranked in float32; the best point
+  // is scored again in float64 for the gradient test and the local search.
   double best_p = pmin, best_f = INFINITY;
   for (int k = 0; k < 10; ++k) {
     const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
-    const double fk = gcv_score(g, pk, red);
-    if (fk < best_f || (k == 0)) {
-      if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
-    }
+    const double fk = gcv_score_f32(g, pk, red);
+    if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
   }
   double p = best_p;
-  const double f0 = best_f;
+  const double f0 = gcv_score(g, p, red);
   const double g0 = gcv_grad(g, p, f0, pmax, red);
   const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
   if (!(fabs(pg) <= 1e-5)) {

@@ -213,6 +213,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
   __shared__ int sc_e[2][W];         // per frame and window: log2 of the operand scale
   __shared__ long long win_base[2][W];
   __shared__ int win_valid[2][W];
@@ -235,7 +236,10 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
     tw_re[k] = cs;
     tw_im[k] = -sn;
   }
-  if (tid == 0) tc::mbar_init(&bar, 1);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_s = 0;
+  }
   __syncthreads();
   const float inv_n = 1.0f / (float)N;
   const int p0 = SS / 2;
@@ -279,19 +283,24 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
   const int n_tiles = (int)((total + W - 1) / W);
   const long long frame_elems = (long long)a.height * a.width;
 
-  auto wait_mma = [&]() -> bool {
-    bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
+  // Every thread waits for the last commit itself; a wait that gives up sets
+  // abort_s, which all threads read after the next barrier and leave the tile
+  // loop together.
+  auto wait_mma = [&]() {
+    const bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
     phase ^= 1u;
-    ok = __syncthreads_and(ok);
-    if (!ok && tid == 0) atomicExch(status, PIV_E_TIMEOUT);
+    if (!ok) {
+      abort_s = 1;
+      atomicExch(status, PIV_E_TIMEOUT);
+    }
     tc::fence_after_sync();
-    return ok;
   };
-  auto sync_for_mma = [&]() {
+  auto sync_for_mma = [&]() -> bool {
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    return abort_s == 0;
   };
   // Window corners of tile `tl` into slot `sl` (threads tid < W).
   auto window_setup = [&](int tl, int sl) {
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         for (int x = 0; x < SS; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, x, SS), r + x);
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
     if (ASYNC) {
       stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
       cp_async_commit();
@@ -400,7 +409,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
     // (w, c) of tile e (k = 2c) and tile o (k = 2c + 1).
@@ -427,7 +436,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         }
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
     if (tid == 0) {
@@ -445,7 +454,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
           }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Product: thread (w, c) forms row c of Q, K = (Re|Im, b, g) with
     // f_r = g (b = 0) or N - g (b = 1; g = 0 pairs with f_r = N/2).
@@ -482,7 +491,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 3: U = Q E / N -> TMEM cols [0, 2N).
     if (tid == 0) {
@@ -495,7 +504,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
       }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Stage 3 -> 4: row (w, c) of U becomes columns (Re|Im, c) of the MN-major rows (w, r).
     {
@@ -515,7 +524,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         }
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
     if (tid == 0) {
@@ -530,7 +539,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Epilogue. Row rt*128 + tid of the tile is map row r of window w
     // (scaled by 2^(e_a + e_b)); shifted row index i = r ^ N/2, shifted
@@ -633,6 +642,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (abort_s) break;
   }
   if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
@@ -678,6 +688,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
   __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
   __shared__ int sc_e[2][W];
   __shared__ long long win_base[2][W];
@@ -698,7 +709,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     tw_re[k] = cs;
     tw_im[k] = -sn;
   }
-  if (tid == 0) tc::mbar_init(&bar, 1);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_s = 0;
+  }
   __syncthreads();
   const float inv_n = 1.0f / (float)N;
   const int p0 = SS / 2;
@@ -742,19 +756,24 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   const int n_tiles = (int)((total + W - 1) / W);
   const long long frame_elems = (long long)a.height * a.width;
 
-  auto wait_mma = [&]() -> bool {
-    bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
+  // Every thread waits for the last commit itself; a wait that gives up sets
+  // abort_s, which all threads read after the next barrier and leave the tile
+  // loop together.
+  auto wait_mma = [&]() {
+    const bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
     phase ^= 1u;
-    ok = __syncthreads_and(ok);
-    if (!ok && tid == 0) atomicExch(status, PIV_E_TIMEOUT);
+    if (!ok) {
+      abort_s = 1;
+      atomicExch(status, PIV_E_TIMEOUT);
+    }
     tc::fence_after_sync();
-    return ok;
   };
-  auto sync_for_mma = [&]() {
+  auto sync_for_mma = [&]() -> bool {
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    return abort_s == 0;
   };
   auto window_setup = [&](int tl, int sl) {
     const long long g = (long long)tl * W + tid;
@@ -840,7 +859,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
 #pragma unroll
       for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
     if (ASYNC) {
       stage_async(sl ^ 1);
       cp_async_commit();
@@ -859,7 +878,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
     {
@@ -881,7 +900,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         }
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 2: X = T^T F^T -> TMEM cols [(rt 2 + f) N, +N).
     if (tid == 0) {
@@ -899,7 +918,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
           }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Product: thread (q, t) forms g in [16 q, 16 q + 16) of row c = t % HN of window t / HN.
     {
@@ -934,7 +953,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 3: Re U = Qr C - Qi S -> cols [0, N); Im U = Qr S + Qi C -> cols [N, 2N).
     if (tid == 0) {
@@ -954,7 +973,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Stage 3 -> 4: thread (q, t) moves r in [64 rh, 64 rh + 64) of part q & 1 of row (w, c).
     {
@@ -970,7 +989,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
       }
     }
-    sync_for_mma();
+    if (!sync_for_mma()) break;
 
     // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
     if (tid == 0) {
@@ -985,7 +1004,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         }
       tc::mma_commit(&bar);
     }
-    if (!wait_mma()) break;
+    wait_mma();
 
     // ---- Epilogue: thread (q, t) holds shifted columns [64 ch, 64 ch + 64) of
     // map row t of window w = q & 1 (row index i = t ^ N/2).
@@ -1079,6 +1098,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (abort_s) break;
   }
   if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
