@@ -305,20 +305,25 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap
     const T up = (T)fmaf(wx.t, u1 - u0, u0);
     const T vp = (T)fmaf(wx.t, v1 - v0, v0);
     const T y = (T)i;
+    // Both samples are formed before either store, so that the loads of the
+    // second frame need not wait behind the first frame's store.
+    T ra, rb;
     if (do_a) {
       const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
-      out_a[p] = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
-                              : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
+      ra = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
+                        : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
     } else {
-      out_a[p] = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
+      ra = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
     }
     if (do_b) {
       const T xi = add_rn(x, mul_rn(up, dtb)), yi = add_rn(y, mul_rn(vp, dtb));
-      out_b[p] = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
-                              : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
+      rb = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
+                        : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
     } else {
-      out_b[p] = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
+      rb = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
     }
+    out_a[p] = ra;
+    out_b[p] = rb;
   }
 }
 

@@ -79,6 +79,19 @@ PIV_D void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 PIV_D void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Register fence for the destinations of tcgen05.ld: after tmem_ld_wait(),
+// pass the loaded array through this so that the compiler sees its values
+// produced at the fence and cannot move their uses above the wait.
+template <int K>
+PIV_D void reg_fence(float (&v)[K]) {
+  static_assert(K % 8 == 0, "reg_fence takes multiples of 8 registers");
+#pragma unroll
+  for (int i = 0; i < K; i += 8)
+    asm volatile(""
+                 : "+f"(v[i]), "+f"(v[i + 1]), "+f"(v[i + 2]), "+f"(v[i + 3]), "+f"(v[i + 4]), "+f"(v[i + 5]),
+                   "+f"(v[i + 6]), "+f"(v[i + 7]));
+}
+
 // ---- MMA --------------------------------------------------------------------
 // Instruction descriptor of kind::f16 with fp16 A/B and fp32 D.
 // a_mn / b_mn: 1 when the operand is stored MN-major (transposed), 0 K-major.

@@ -423,6 +423,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         for (int c0 = 0; c0 < N; c0 += 16)
           tc::tmem_ld16(tmem + lane_sel + f * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
+        tc::reg_fence(v);
 #pragma unroll
         for (int rt = 0; rt < 2; ++rt) {
           unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
@@ -470,6 +471,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
         tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
+        tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
         float qr0[8], qi0[8], qr1[8], qi1[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -517,6 +519,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         for (int c0 = 0; c0 < N; c0 += 16)
           tc::tmem_ld16(tmem + lane_sel + part * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
+        tc::reg_fence(v);
 #pragma unroll
         for (int r0 = 0; r0 < N; r0 += 8) {
           const int m = w * N + r0;
@@ -554,6 +557,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
       for (int c0 = 0; c0 < N; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
+      tc::reg_fence(v);
       float rowc[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) rowc[j] = j == 0 ? 0.f : v[j ^ HN];
@@ -605,6 +609,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_
         for (int c0 = 0; c0 < N; c0 += 16)
           tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
+        tc::reg_fence(v);
         if (mine) {
           float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
 #pragma unroll
@@ -888,6 +893,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int c0 = 0; c0 < 64; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
+      tc::reg_fence(v);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt) {
         unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
@@ -933,6 +939,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
         tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
+        tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
         float qr0[8], qi0[8], qr1[8], qi1[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -983,6 +990,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int c0 = 0; c0 < 64; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
+      tc::reg_fence(v);
 #pragma unroll
       for (int r0 = 0; r0 < 64; r0 += 8) {
         const int m = w * N + 64 * rh + r0;
@@ -1017,6 +1025,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int c0 = 0; c0 < 64; c0 += 16)
         tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
+      tc::reg_fence(v);
       if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
       float best;
       int bk;
@@ -1062,6 +1071,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         for (int c0 = 0; c0 < 64; c0 += 16)
           tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
+        tc::reg_fence(v);
         if (mine) {
           float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N + s0);
 #pragma unroll
