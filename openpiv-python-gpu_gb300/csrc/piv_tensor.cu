@@ -64,6 +64,8 @@ struct TcLayout {
   // the TMEM allows only two CTAs.
   static constexpr int TPL = SS == 32 ? 2 : 1;
   static constexpr int NT = 128 * TPL;
+  // CTAs per SM the register budget is compiled for.
+  static constexpr int LB_BLOCKS = MIN_BLOCKS;
 };
 
 // Swizzled chunk position of chunk c of staged row t: the eight rows a
@@ -206,7 +208,7 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
 // current tile runs through its four products; otherwise each tile loads its
 // rows from global memory when it starts.
 template <int SS, bool ASYNC>
-__global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::MIN_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
+__global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
   using L = TcLayout<SS>;
   constexpr int N = L::N, HN = L::HN, W = L::W, CH = L::CH, TPL = L::TPL, NT = L::NT;
   constexpr int NPART = N / 32;      // warps per window in the epilogue

@@ -352,6 +352,10 @@ int scale_fields(int count, const double* u, const double* v, double scaling, do
 // ---------------------------------------------------------------------------
 static constexpr int kRepThreads = 512;
 static constexpr int kCgMaxIters = 20000;
+// Up to kCgSmall outliers per pair, the conjugate-gradient vectors stay in
+// registers (kCgPer per thread) and the search direction in shared memory.
+static constexpr int kCgPer = 4;
+static constexpr int kCgSmall = kRepThreads * kCgPer;
 
 struct RepScratch {
   double* init_u;   // [mn]
@@ -359,6 +363,8 @@ struct RepScratch {
   double* new_u;    // [mn] replacement values by outlier rank
   double* new_v;
   double* cg;       // 8 * [mn]: x_u, x_v, r_u, r_v, p_u, p_v, q_u, q_v
+  double* dinv;     // [mn] spring row scale 1/c_r by outlier rank
+  int* nbr;         // 4 * [mn] outlier ranks of the linked neighbours (-1: none)
   int* list;        // [mn] outlier positions
   int* rank;        // [mn] position -> outlier rank or -1
   uint8_t* flag;    // [mn] anchored / scratch flags
@@ -368,7 +374,7 @@ struct RepScratch {
 // Bytes of one pair's replacement scratch, rounded up to 256 so that every
 // pair's block (and the doubles at its start) stays aligned.
 PIV_HD size_t rep_scratch_stride(size_t mn) {
-  return ((mn * (12 * sizeof(double) + 2 * sizeof(int) + 2) + 255) / 256) * 256;
+  return ((mn * (13 * sizeof(double) + 6 * sizeof(int) + 2) + 255) / 256) * 256;
 }
 
 size_t replace_scratch_bytes(int m, int n, int n_pairs) {
@@ -383,6 +389,8 @@ static __device__ RepScratch rep_scratch(void* base, int mn, int pair) {
   s.new_u = (double*)p; p += mn * sizeof(double);
   s.new_v = (double*)p; p += mn * sizeof(double);
   s.cg = (double*)p; p += 8 * (size_t)mn * sizeof(double);
+  s.dinv = (double*)p; p += mn * sizeof(double);
+  s.nbr = (int*)p; p += 4 * (size_t)mn * sizeof(int);
   s.list = (int*)p; p += mn * sizeof(int);
   s.rank = (int*)p; p += mn * sizeof(int);
   s.flag = (uint8_t*)p; p += mn;
@@ -400,6 +408,21 @@ PIV_D double block_sum(double v, double* red) {
   double t = 0;
   for (int k = 0; k < nw; ++k) t += red[k];
   return t;
+}
+
+// Block-wide sums of two doubles in one reduction (all threads get both).
+PIV_D double2 block_sum2(double a, double b, double* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(~0u, a, o);
+    b += __shfl_xor_sync(~0u, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0) { red[w] = a; red[32 + w] = b; }
+  __syncthreads();
+  double ta = 0, tb = 0;
+  for (int k = 0; k < nw; ++k) { ta += red[k]; tb += red[32 + k]; }
+  return make_double2(ta, tb);
 }
 
 PIV_D int block_count(int v, int* red) {
@@ -476,7 +499,8 @@ PIV_D T spring_rhs(const FieldView& fv, int i, int j, int s) {
 
 template <typename T>
 __global__ void __launch_bounds__(kRepThreads) k_replace(RepArgs a, int* status) {
-  __shared__ double red_d[40];
+  __shared__ double red_d[64];
+  __shared__ double cg_pu[kCgSmall], cg_pv[kCgSmall];
   __shared__ int red_i[40];
   const int pair = blockIdx.x;
   const int m = a.val.m, n = a.val.n, mn = m * n;
@@ -503,7 +527,92 @@ __global__ void __launch_bounds__(kRepThreads) k_replace(RepArgs a, int* status)
     const int nv = block_compact(val, mn, sc.list, sc.rank, red_i);
     if (nv == 0) break;
     // 1. Replacement values from the current fields.
-    if (a.method == PIV_REPLACE_SPRING) {
+    if (a.method == PIV_REPLACE_SPRING && nv <= kCgSmall) {
+      // Conjugate gradients on (D - Adj) x = D rhs for both fields, the
+      // vectors of outlier r = tid + k nt in registers, p in shared memory.
+      FieldView fu{u, m, n, val, 0.0}, fv{v, m, n, val, 0.0};
+      double xu[kCgPer], xv[kCgPer], ru[kCgPer], rv[kCgPer], dd[kCgPer];
+      int nb[kCgPer][4];
+      double rr_u = 0, rr_v = 0;
+#pragma unroll
+      for (int k = 0; k < kCgPer; ++k) {
+        const int r = tid + k * nt;
+        xu[k] = xv[k] = ru[k] = rv[k] = dd[k] = 0;
+        nb[k][0] = nb[k][1] = nb[k][2] = nb[k][3] = -1;
+        if (r < nv) {
+          const int p = sc.list[r], i = p / n, j = p % n;
+          dd[k] = 1.0 / spring_coef(i, j, m, n, s, a.dtype);
+          ru[k] = dd[k] * (double)spring_rhs<T>(fu, i, j, s);
+          rv[k] = dd[k] * (double)spring_rhs<T>(fv, i, j, s);
+          const int oi[4] = {-s, 0, 0, s}, oj[4] = {0, -s, s, 0};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int ii = i + oi[e], jj = j + oj[e];
+            nb[k][e] = (ii < 0 || ii >= m || jj < 0 || jj >= n) ? -1 : sc.rank[ii * n + jj];
+          }
+          cg_pu[r] = ru[k];
+          cg_pv[r] = rv[k];
+          rr_u += ru[k] * ru[k];
+          rr_v += rv[k] * rv[k];
+        }
+      }
+      const double2 rr = block_sum2(rr_u, rr_v, red_d);  // also publishes cg_pu / cg_pv
+      rr_u = rr.x;
+      rr_v = rr.y;
+      const double tol_u = rr_u * 1e-28, tol_v = rr_v * 1e-28;
+      bool done_u = rr_u <= tol_u || rr_u == 0, done_v = rr_v <= tol_v || rr_v == 0;
+      int iter = 0;
+      for (; iter < kCgMaxIters && !(done_u && done_v); ++iter) {
+        double qu[kCgPer], qv[kCgPer], pq_u = 0, pq_v = 0;
+#pragma unroll
+        for (int k = 0; k < kCgPer; ++k) {
+          const int r = tid + k * nt;
+          qu[k] = qv[k] = 0;
+          if (r < nv) {
+            double au = dd[k] * cg_pu[r], av = dd[k] * cg_pv[r];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int q = nb[k][e];
+              if (q >= 0) { au -= cg_pu[q]; av -= cg_pv[q]; }
+            }
+            qu[k] = au; qv[k] = av;
+            pq_u += cg_pu[r] * au; pq_v += cg_pv[r] * av;
+          }
+        }
+        const double2 pq = block_sum2(pq_u, pq_v, red_d);
+        const double al_u = done_u ? 0.0 : rr_u / pq.x, al_v = done_v ? 0.0 : rr_v / pq.y;
+        double nr_u = 0, nr_v = 0;
+#pragma unroll
+        for (int k = 0; k < kCgPer; ++k) {
+          const int r = tid + k * nt;
+          if (r < nv) {
+            xu[k] += al_u * cg_pu[r]; xv[k] += al_v * cg_pv[r];
+            ru[k] -= al_u * qu[k]; rv[k] -= al_v * qv[k];
+            nr_u += ru[k] * ru[k]; nr_v += rv[k] * rv[k];
+          }
+        }
+        const double2 nr = block_sum2(nr_u, nr_v, red_d);
+        const double be_u = done_u ? 0.0 : nr.x / rr_u, be_v = done_v ? 0.0 : nr.y / rr_v;
+#pragma unroll
+        for (int k = 0; k < kCgPer; ++k) {
+          const int r = tid + k * nt;
+          if (r < nv) {
+            if (!done_u) cg_pu[r] = ru[k] + be_u * cg_pu[r];
+            if (!done_v) cg_pv[r] = rv[k] + be_v * cg_pv[r];
+          }
+        }
+        rr_u = nr.x; rr_v = nr.y;
+        done_u = done_u || rr_u <= tol_u;
+        done_v = done_v || rr_v <= tol_v;
+        __syncthreads();
+      }
+      if (iter >= kCgMaxIters && tid == 0 && status) atomicExch(status, PIV_E_TIMEOUT);
+#pragma unroll
+      for (int k = 0; k < kCgPer; ++k) {
+        const int r = tid + k * nt;
+        if (r < nv) { sc.new_u[r] = xu[k]; sc.new_v[r] = xv[k]; }
+      }
+    } else if (a.method == PIV_REPLACE_SPRING) {
       FieldView fu{u, m, n, val, 0.0}, fv{v, m, n, val, 0.0};
       double* xu = sc.cg;
       double* xv = sc.cg + mn;
@@ -525,14 +634,24 @@ __global__ void __launch_bounds__(kRepThreads) k_replace(RepArgs a, int* status)
         xu[r] = 0; xv[r] = 0;
         ru[r] = b1; rv[r] = b2;
         pu[r] = b1; pv[r] = b2;
+        // The row's coupling to the other outliers, resolved once for the
+        // iterations: scale and neighbour ranks.
+        sc.dinv[r] = d;
+        const int oi[4] = {-s, 0, 0, s}, oj[4] = {0, -s, s, 0};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int ii = i + oi[e], jj = j + oj[e];
+          sc.nbr[e * mn + r] = (ii < 0 || ii >= m || jj < 0 || jj >= n) ? -1 : sc.rank[ii * n + jj];
+        }
       }
       __syncthreads();
       {
         // Conjugate gradients on (D - Adj) x = D rhs for both fields at once.
         double rr_u = 0, rr_v = 0;
         for (int r = tid; r < nv; r += nt) { rr_u += ru[r] * ru[r]; rr_v += rv[r] * rv[r]; }
-        rr_u = block_sum(rr_u, red_d);
-        rr_v = block_sum(rr_v, red_d);
+        const double2 rr = block_sum2(rr_u, rr_v, red_d);
+        rr_u = rr.x;
+        rr_v = rr.y;
         const double tol_u = rr_u * 1e-28, tol_v = rr_v * 1e-28;
         bool done_u = rr_u <= tol_u || rr_u == 0, done_v = rr_v <= tol_v || rr_v == 0;
         int iter = 0;
@@ -540,36 +659,31 @@ __global__ void __launch_bounds__(kRepThreads) k_replace(RepArgs a, int* status)
           // q = A p
           double pq_u = 0, pq_v = 0;
           for (int r = tid; r < nv; r += nt) {
-            const int p = sc.list[r], i = p / n, j = p % n;
-            const double d = 1.0 / spring_coef(i, j, m, n, s, a.dtype);
+            const double d = sc.dinv[r];
             double au = d * pu[r], av = d * pv[r];
-            const int oi[4] = {-s, 0, 0, s}, oj[4] = {0, -s, s, 0};
+#pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const int ii = i + oi[e], jj = j + oj[e];
-              if (ii < 0 || ii >= m || jj < 0 || jj >= n) continue;
-              const int k = sc.rank[ii * n + jj];
+              const int k = sc.nbr[e * mn + r];
               if (k >= 0) { au -= pu[k]; av -= pv[k]; }
             }
             qu[r] = au; qv[r] = av;
             pq_u += pu[r] * au; pq_v += pv[r] * av;
           }
-          pq_u = block_sum(pq_u, red_d);
-          pq_v = block_sum(pq_v, red_d);
-          const double al_u = done_u ? 0.0 : rr_u / pq_u, al_v = done_v ? 0.0 : rr_v / pq_v;
+          const double2 pq = block_sum2(pq_u, pq_v, red_d);
+          const double al_u = done_u ? 0.0 : rr_u / pq.x, al_v = done_v ? 0.0 : rr_v / pq.y;
           double nr_u = 0, nr_v = 0;
           for (int r = tid; r < nv; r += nt) {
             xu[r] += al_u * pu[r]; xv[r] += al_v * pv[r];
             ru[r] -= al_u * qu[r]; rv[r] -= al_v * qv[r];
             nr_u += ru[r] * ru[r]; nr_v += rv[r] * rv[r];
           }
-          nr_u = block_sum(nr_u, red_d);
-          nr_v = block_sum(nr_v, red_d);
-          const double be_u = done_u ? 0.0 : nr_u / rr_u, be_v = done_v ? 0.0 : nr_v / rr_v;
+          const double2 nr = block_sum2(nr_u, nr_v, red_d);
+          const double be_u = done_u ? 0.0 : nr.x / rr_u, be_v = done_v ? 0.0 : nr.y / rr_v;
           for (int r = tid; r < nv; r += nt) {
             if (!done_u) pu[r] = ru[r] + be_u * pu[r];
             if (!done_v) pv[r] = rv[r] + be_v * pv[r];
           }
-          rr_u = nr_u; rr_v = nr_v;
+          rr_u = nr.x; rr_v = nr.y;
           done_u = done_u || rr_u <= tol_u;
           done_v = done_v || rr_v <= tol_v;
           __syncthreads();
