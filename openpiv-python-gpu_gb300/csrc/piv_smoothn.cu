@@ -32,10 +32,17 @@ struct SmoothScratch {
 
 static size_t align_up(size_t v) { return (v + 255) / 256 * 256; }
 
+// Per-pair block of the weighted path: f, z, t, fd, tmp (2 mn doubles each),
+// w (mn doubles) and the column-nearest table (mn ints).
+static size_t weighted_pair_bytes(size_t mn) { return align_up(11 * mn * 8 + mn * 4); }
+
 size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
   const size_t mn = (size_t)m * n;
-  return align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + align_up((size_t)m * m * 8) +
-         align_up((size_t)n * n * 8) + align_up(mn * 8) + align_up((size_t)n_pairs * 8);
+  const size_t shared = align_up((size_t)m * m * 8) + align_up((size_t)n * n * 8) + align_up(mn * 8) +
+                        align_up((size_t)n_pairs * 8);
+  const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared;
+  const size_t weighted = shared + weighted_pair_bytes(mn) * n_pairs;
+  return plain > weighted ? plain : weighted;
 }
 
 static SmoothScratch carve(void* base, int m, int n, int n_pairs) {
@@ -374,16 +381,325 @@ static int check(const char* what) {
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, what);
 }
 
+// ---------------------------------------------------------------------------
+// Weighted smoothn (a field mask, or fields with non-finite values): Garcia's
+// iteration as SmoothnGPU runs it with weights (gpu_smoothn.py:123-231):
+// missing values take the value of their nearest finite neighbour
+// (replace_non_finite, gpu_smoothn.py:233-251, with scipy's feature-transform
+// choice among equidistant neighbours: per column the nearest finite row, the
+// lower one on a tie, then the nearest column, the lower one on a tie), the
+// start z keeps the low DCT coefficients (get_init_z, gpu_smoothn.py:284-297),
+// then z <- rf IDCT2(gamma DCT2(w (f - z) + z)) + (1 - rf) z with rf = 1.75
+// until ||z_old - z|| / (||z|| + 1e-6) <= 1e-3 or 100 iterations; with s unset
+// the GCV search runs at iterations 1, 2, 4, 8, ... (gpu_smoothn.py:176-193),
+// with the w_mean <= 0.9 score refitting the field for every candidate s
+// (gpu_smoothn.py:359-368). Output zero inside the mask (gpu_smoothn.py:224-225).
+// One CTA per pair does the whole iteration; float64 throughout.
+// ---------------------------------------------------------------------------
+static constexpr int kSwThreads = 512;
+
+PIV_D double cta_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double t = l < nw ? red[l] : 0.0;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(~0u, t, o);
+  return t;
+}
+
+// 2-D orthonormal DCT-II (inv = false) or DCT-III of one m x n field inside the CTA.
+PIV_D void cta_dct2(const double* in, double* tmp, double* out, int m, int n, const double* __restrict__ cm,
+                    const double* __restrict__ cn, bool inv) {
+  const int mn = m * n;
+  for (int e = threadIdx.x; e < mn; e += blockDim.x) {
+    const int i = e / n, l = e % n;
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) acc = fma(in[i * n + j], inv ? cn[j * n + l] : cn[l * n + j], acc);
+    tmp[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < mn; e += blockDim.x) {
+    const int k = e / n, j = e % n;
+    double acc = 0.0;
+    for (int i = 0; i < m; ++i) acc = fma(inv ? cm[i * m + k] : cm[k * m + i], tmp[i * n + j], acc);
+    out[e] = acc;
+  }
+  __syncthreads();
+}
+
+struct SwCtx {
+  int m, n, mn;
+  const double *cm, *cn, *lam2;
+  double *f, *z, *t, *fd, *tmp, *w;
+  double n_finite, w_mean;
+  double* red;
+};
+
+// GCV score at p (gpu_smoothn.py:353-372). fd: DCT of both fields.
+PIV_D double sw_gcv(const SwCtx& c, double p) {
+  const double s = pow(10.0, p);
+  double rss = 0.0, tr = 0.0;
+  if (c.w_mean > 0.9) {
+    for (int e = threadIdx.x; e < c.mn; e += blockDim.x) {
+      const double gm = 1.0 / (1.0 + s * c.lam2[e]);
+      const double d = gm - 1.0;
+      rss += (c.fd[e] * c.fd[e] + c.fd[c.mn + e] * c.fd[c.mn + e]) * d * d;
+      tr += gm;
+    }
+  } else {
+    for (int e = threadIdx.x; e < c.mn; e += blockDim.x) tr += 1.0 / (1.0 + s * c.lam2[e]);
+    for (int fi = 0; fi < 2; ++fi) {
+      // f_hat = IDCT2(gamma fd); t holds gamma fd, z is kept.
+      for (int e = threadIdx.x; e < c.mn; e += blockDim.x) c.t[fi * c.mn + e] = c.fd[fi * c.mn + e] / (1.0 + s * c.lam2[e]);
+      __syncthreads();
+      cta_dct2(c.t + fi * c.mn, c.tmp, c.tmp + c.mn, c.m, c.n, c.cm, c.cn, true);
+      for (int e = threadIdx.x; e < c.mn; e += blockDim.x) {
+        const double fv = c.f[fi * c.mn + e];
+        if (isfinite(fv) || c.w[e] > 0) {
+          const double d = fv - c.tmp[c.mn + e];
+          rss += c.w[e] * d * d;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  rss = cta_sum(rss, c.red);
+  tr = cta_sum(tr, c.red);
+  const double q = 1.0 - tr / (double)c.mn;
+  return rss / c.n_finite / (q * q) / 2.0;
+}
+
+// The search of k_gcv (scan on the first call, then the projected-gradient
+// stopping test and Brent's bounded minimisation around the start point).
+PIV_D double sw_search(const SwCtx& c, double p, bool have_p, double pmin, double pmax) {
+  if (!have_p) {
+    double best_f = INFINITY;
+    for (int k = 0; k < 10; ++k) {
+      const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
+      const double fk = sw_gcv(c, pk);
+      if (k == 0 || fk < best_f) { best_f = fk; p = pk; }
+    }
+  }
+  const double f0 = sw_gcv(c, p);
+  const double h = 1e-8;
+  const double g0 = p + h <= pmax ? (sw_gcv(c, p + h) - f0) / h : (f0 - sw_gcv(c, p - h)) / h;
+  const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
+  if (fabs(pg) <= 1e-5) return p;
+  const double step = (pmax - pmin) / 9.0;
+  double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
+  const double cg = 0.3819660112501051;
+  double x = p, w = p, v = p, fx = f0, fw = f0, fv = f0, d = 0.0, e = 0.0;
+  for (int it = 0; it < 200; ++it) {
+    const double xm = 0.5 * (a + b);
+    const double tol1 = 1e-11 * fabs(x) + 1e-13, tol2 = 2.0 * tol1;
+    if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
+    bool golden = true;
+    if (fabs(e) > tol1) {
+      double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
+      q = 2.0 * (q - r);
+      if (q > 0) pp = -pp;
+      q = fabs(q);
+      const double etemp = e;
+      e = d;
+      if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
+        d = pp / q;
+        const double u = x + d;
+        if (u - a < tol2 || b - u < tol2) d = xm >= x ? tol1 : -tol1;
+        golden = false;
+      }
+    }
+    if (golden) {
+      e = (x >= xm) ? a - x : b - x;
+      d = cg * e;
+    }
+    const double u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
+    const double fu = sw_gcv(c, u);
+    if (fu <= fx) {
+      if (u >= x) a = x; else b = x;
+      v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
+    } else {
+      if (u < x) a = u; else b = u;
+      if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
+      else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+    }
+  }
+  if (x - pmin < 1e-9) x = pmin;
+  if (pmax - x < 1e-9) x = pmax;
+  return x;
+}
+
+__global__ void __launch_bounds__(kSwThreads)
+k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double* u_out, double* v_out,
+                   const uint8_t* __restrict__ mask,
+                   double fixed_p, int is_auto, double pmin, double pmax, const double* __restrict__ cm,
+                   const double* __restrict__ cn, const double* __restrict__ lam2, unsigned char* scratch,
+                   size_t pair_bytes, double* p_out) {
+  __shared__ double red[32];
+  __shared__ int s_flag;
+  const int pair = blockIdx.x, mn = m * n, tid = threadIdx.x, nt = blockDim.x;
+  double* base = reinterpret_cast<double*>(scratch + pair_bytes * pair);
+  SwCtx c;
+  c.m = m; c.n = n; c.mn = mn; c.cm = cm; c.cn = cn; c.lam2 = lam2;
+  c.f = base; c.z = base + 2 * mn; c.t = base + 4 * mn; c.fd = base + 6 * mn; c.tmp = base + 8 * mn;
+  c.w = base + 10 * mn; c.red = red;
+  int* near = reinterpret_cast<int*>(base + 11 * mn);
+  const long long off = (long long)pair * mn;
+  // Fields, finite mask and weights.
+  double nf = 0.0, ws = 0.0;
+  for (int e = tid; e < mn; e += nt) {
+    const double a = u_in[off + e], b = v_in[off + e];
+    const bool fin = isfinite(a) && isfinite(b);
+    c.f[e] = a;
+    c.f[mn + e] = b;
+    const double wv = (fin && !(mask && mask[e])) ? 1.0 : 0.0;
+    c.w[e] = wv;
+    nf += fin ? 1.0 : 0.0;
+    ws += wv;
+  }
+  nf = cta_sum(nf, red);
+  ws = cta_sum(ws, red);
+  c.n_finite = nf;
+  c.w_mean = ws / (double)mn;
+  const bool weighted = ws != (double)mn;
+  // Nearest finite neighbour of the missing points: first the nearest finite
+  // row in every column (ties: the lower row), then the nearest column.
+  if (nf < (double)mn && nf > 0) {
+    for (int col = tid; col < n; col += nt) {
+      int last = -1;
+      for (int y = 0; y < m; ++y) {
+        if (isfinite(c.f[y * n + col]) && isfinite(c.f[mn + y * n + col])) last = y;
+        near[y * n + col] = last;
+      }
+      int next = -1;
+      for (int y = m - 1; y >= 0; --y) {
+        if (isfinite(c.f[y * n + col]) && isfinite(c.f[mn + y * n + col])) next = y;
+        const int up = near[y * n + col];
+        int r = up;
+        if (up < 0 || (next >= 0 && next - y < y - up)) r = next;
+        near[y * n + col] = r;
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < mn; e += nt) {
+      if (isfinite(c.f[e]) && isfinite(c.f[mn + e])) continue;
+      const int y = e / n, x = e % n;
+      long long best = -1;
+      int br = 0, bc = 0;
+      for (int col = 0; col < n; ++col) {
+        const int r = near[y * n + col];
+        if (r < 0) continue;
+        const long long d = (long long)(col - x) * (col - x) + (long long)(r - y) * (r - y);
+        if (best < 0 || d < best) { best = d; br = r; bc = col; }
+      }
+      c.t[e] = c.f[br * n + bc];
+      c.t[mn + e] = c.f[mn + br * n + bc];
+    }
+    __syncthreads();
+    for (int e = tid; e < mn; e += nt) {
+      if (isfinite(c.f[e]) && isfinite(c.f[mn + e])) continue;
+      c.f[e] = c.t[e];
+      c.f[mn + e] = c.t[mn + e];
+    }
+    __syncthreads();
+  }
+  // Start: the low DCT coefficients of f (one trailing block cleared), or 0.
+  const int n0 = (m + 9) / 10 + 1, n1 = (n + 9) / 10 + 1;
+  for (int fi = 0; fi < 2; ++fi) {
+    if (weighted) {
+      cta_dct2(c.f + fi * mn, c.tmp, c.t + fi * mn, m, n, cm, cn, false);
+      for (int e = tid; e < mn; e += nt)
+        if (e / n >= n0 && e % n >= n1) c.t[fi * mn + e] = 0.0;
+      __syncthreads();
+      cta_dct2(c.t + fi * mn, c.tmp, c.z + fi * mn, m, n, cm, cn, true);
+    } else {
+      for (int e = tid; e < mn; e += nt) c.z[fi * mn + e] = 0.0;
+    }
+  }
+  __syncthreads();
+  const double rf = weighted ? 1.75 : 1.0;
+  double p = fixed_p;
+  bool have_p = !is_auto;
+  for (int k = 0; k < 100; ++k) {
+    for (int e = tid; e < 2 * mn; e += nt) {
+      const double wv = c.w[e % mn];
+      c.t[e] = wv * (c.f[e] - c.z[e]) + c.z[e];
+    }
+    __syncthreads();
+    for (int fi = 0; fi < 2; ++fi) cta_dct2(c.t + fi * mn, c.tmp, c.fd + fi * mn, m, n, cm, cn, false);
+    if (is_auto && ((k + 1) & k) == 0) {
+      p = sw_search(c, p, have_p, pmin, pmax);
+      have_p = true;
+    }
+    const double s = pow(10.0, p);
+    double num = 0.0, den = 0.0;
+    for (int fi = 0; fi < 2; ++fi) {
+      for (int e = tid; e < mn; e += nt) c.t[fi * mn + e] = c.fd[fi * mn + e] / (1.0 + s * lam2[e]);
+      __syncthreads();
+      cta_dct2(c.t + fi * mn, c.tmp, c.tmp + mn, m, n, cm, cn, true);
+      for (int e = tid; e < mn; e += nt) {
+        const double z0 = c.z[fi * mn + e];
+        const double z1 = rf * c.tmp[mn + e] + (1.0 - rf) * z0;
+        c.z[fi * mn + e] = z1;
+        num += (z0 - z1) * (z0 - z1);
+        den += z1 * z1;
+      }
+      __syncthreads();
+    }
+    num = cta_sum(num, red);
+    den = cta_sum(den, red);
+    const double tol = weighted ? sqrt(num) / (sqrt(den) + 1e-6) : 0.0;
+    if (tid == 0) s_flag = tol <= 1e-3;
+    __syncthreads();
+    if (s_flag) break;
+  }
+  for (int e = tid; e < mn; e += nt) {
+    const bool in_mask = mask && mask[e];
+    u_out[off + e] = in_mask ? 0.0 : c.z[e];
+    v_out[off + e] = in_mask ? 0.0 : c.z[mn + e];
+  }
+  if (tid == 0 && p_out) p_out[pair] = p;
+}
+
+static int smoothn_weighted(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out,
+                            double* v_out, const uint8_t* field_mask, double s, double* p_out, void* scratch,
+                            cudaStream_t stream) {
+  const size_t mn = (size_t)m * n;
+  char* p = (char*)scratch;
+  double* cm = (double*)p; p += align_up((size_t)m * m * 8);
+  double* cn = (double*)p; p += align_up((size_t)n * n * 8);
+  double* lam2 = (double*)p; p += align_up(mn * 8);
+  p += align_up((size_t)n_pairs * 8);
+  const int bs = 256;
+  k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, cm);
+  k_dct_matrix<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n, cn);
+  k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, lam2);
+  const bool is_auto = !(s > 0);
+  double pmin = 0, pmax = 0;
+  if (is_auto) {
+    const double h_min = 1e-3, h_max = 1.0 - h_min;
+    const int rank = (m != 1) + (n != 1);
+    const double a_max = pow(h_max, 2.0 / rank), a_min = pow(h_min, 2.0 / rank);
+    pmin = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_max)) / 4.0 / a_max, 2.0) - 1.0) / 16.0);
+    pmax = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_min)) / 4.0 / a_min, 2.0) - 1.0) / 16.0);
+  }
+  k_smoothn_weighted<<<n_pairs, kSwThreads, 0, stream>>>(m, n, u_in, v_in, u_out, v_out, field_mask,
+                                                          is_auto ? 0.0 : log10(s), is_auto ? 1 : 0, pmin, pmax, cm, cn,
+                                                          lam2, (unsigned char*)p, weighted_pair_bytes(mn), p_out);
+  return check("k_smoothn_weighted");
+}
+
 int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out, double* v_out,
             const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream) {
   const long long mn = (long long)m * n;
   if (n_pairs == 0 || mn == 0) return PIV_OK;
-  if (field_mask) return set_error(PIV_E_UNSUPPORTED, "smoothn with a field mask (weighted smoothing) is not implemented");
   if (mn < 2) {
     cudaMemcpyAsync(u_out, u_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
     cudaMemcpyAsync(v_out, v_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
     return check("smoothn copy");
   }
+  if (field_mask) return smoothn_weighted(m, n, n_pairs, u_in, v_in, u_out, v_out, field_mask, s, p_out, scratch, stream);
   SmoothScratch sc = carve(scratch, m, n, n_pairs);
   const int bs = 256;
   k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, sc.cm);

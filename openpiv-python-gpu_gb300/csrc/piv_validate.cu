@@ -410,7 +410,9 @@ PIV_D double block_sum(double v, double* red) {
   return t;
 }
 
-// Block-wide sums of two doubles in one reduction (all threads get both).
+// Block-wide sums of two doubles in one reduction (all threads get both). The
+// warps' partial sums are combined by a shuffle tree rather than a serial
+// chain: the conjugate-gradient loop waits on this twice per iteration.
 PIV_D double2 block_sum2(double a, double b, double* red) {
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_xor_sync(~0u, a, o);
@@ -420,8 +422,11 @@ PIV_D double2 block_sum2(double a, double b, double* red) {
   __syncthreads();
   if (l == 0) { red[w] = a; red[32 + w] = b; }
   __syncthreads();
-  double ta = 0, tb = 0;
-  for (int k = 0; k < nw; ++k) { ta += red[k]; tb += red[32 + k]; }
+  double ta = l < nw ? red[l] : 0.0, tb = l < nw ? red[32 + l] : 0.0;
+  for (int o = 16; o > 0; o >>= 1) {
+    ta += __shfl_xor_sync(~0u, ta, o);
+    tb += __shfl_xor_sync(~0u, tb, o);
+  }
   return make_double2(ta, tb);
 }
 

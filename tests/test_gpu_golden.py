@@ -71,8 +71,6 @@ def test_pipeline_matches_reference(api, case):
 
     name = case[0]
     g, a, b, piv = _load(*case)
-    if piv.get("mask") is not None and int(g["n_iters"]) > 1:
-        pytest.skip("masked multi-pass runs need weighted smoothn, not implemented on the GPU yet")
     mss = piv.pop("min_search_size")
     proc = api.piv_gpu(a.shape, mss, **piv)
     u, v = proc(a, b)

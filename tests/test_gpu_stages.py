@@ -331,6 +331,32 @@ def test_smoothn_matches_oracle(env, shape, s):
         assert abs(float(p.item()) - tr["p"]) < 1e-2
 
 
+@pytest.mark.parametrize("shape,frac", [((31, 31), 0.05), ((24, 40), 0.2), ((11, 11), 0.12), ((63, 63), 0.08)])
+@pytest.mark.parametrize("s", [0.8, None])
+def test_weighted_smoothn_matches_oracle(env, shape, frac, s):
+    """smoothn with a field mask (weighted iteration, nearest-neighbour fill of
+    the masked NaNs, GCV with the w_mean <= 0.9 score for the larger masks)."""
+    torch, _lib, lib = env
+    u, v = _fields(17, shape, 0, False)
+    y, x = np.mgrid[0:shape[0], 0:shape[1]]
+    r2 = (x - 0.45 * shape[1]) ** 2 + (y - 0.55 * shape[0]) ** 2
+    mask = r2 < frac * shape[0] * shape[1] / np.pi
+    u[mask] = np.nan
+    v[mask] = np.nan
+    tr = {}
+    ref = po.smoothn([u.copy(), v.copy()], mask=mask, s=s, trace=tr)
+    du, dv = torch.as_tensor(u).cuda(), torch.as_tensor(v).cuda()
+    dm = torch.as_tensor(mask.astype(np.uint8)).cuda()
+    p = torch.empty(1, dtype=torch.float64, device="cuda")
+    _lib.check(lib.piv_smoothn(shape[0], shape[1], 1, du.data_ptr(), dv.data_ptr(), dm.data_ptr(),
+                               float("nan") if s is None else s, p.data_ptr(), _stream(torch)))
+    tol = 1e-5 if s is not None else 1e-3
+    np.testing.assert_allclose(du.cpu().numpy(), ref[0], atol=tol)
+    np.testing.assert_allclose(dv.cpu().numpy(), ref[1], atol=tol)
+    if s is None:
+        assert abs(float(p.item()) - tr["p"]) < 2e-2
+
+
 @pytest.mark.parametrize("ss,n_fft,dtype", [(8, 2, "float32"), (8, 1, "float32"), (16, 1, "float32"),
                                            (16, 2, "float32"), (32, 2, "float64"), (64, 2, "float32")])
 def test_correlation_maps_match_oracle(env, ss, n_fft, dtype):
