@@ -54,6 +54,11 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving form instead: Poisson arrivals of mixed-size pairs through the continuous-batching "
+                         "loop, p50/p99 latency and pairs/s beside the plain per-pair path")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--requests", type=int, default=400, help="serving: number of requests")
     return ap.parse_args()
 
 
@@ -70,6 +75,15 @@ def _make_pair(k):
     from openpiv_gpu import synthetic
 
     a, b, _, _ = synthetic.config_case(2, k)
+    return a, b
+
+
+def _make_serving_pair(args):
+    k, shape = args
+    sys.path.insert(0, PKG)
+    from openpiv_gpu import synthetic
+
+    a, b, _, _ = synthetic.config_case(5, k, shape=tuple(shape))
     return a, b
 
 
@@ -399,24 +413,26 @@ def run_gpu(args):
     if on_tensor:
         roofline["executed_tflops"] = n_win * tc_executed_flops(f.search_size, N) / (corr[dom] * 1e-3) / 1e12
 
-    # End to end through the public API: pinned host frames in, fields out.
+    # End to end through the public API: pinned host frames in, fields out
+    # (PIVGPU.run_batches: two plans on two streams, so that a batch's upload
+    # and download overlap the previous batch's kernels).
     pin_a = torch.as_tensor(host_a).pin_memory()
     pin_b = torch.as_tensor(host_b).pin_memory()
     na, nb = pin_a.numpy(), pin_b.numpy()
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            proc.run_batch(na, nb, host_out=True)
+    for _ in proc.run_batches((na, nb) for _ in range(args.warmup)):
+        pass
+    torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for _ in range(args.steps):
-            res_u, res_v = proc.run_batch(na, nb, host_out=True)
+    for res_u, res_v in proc.run_batches((na, nb) for _ in range(args.steps)):
+        pass
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
+    device_status = proc.status()  # PIV_OK unless a bounded device-side wait gave up
     m, n = proc.piv_fields[-1].field_shape
     e2e = {"value": B * world * args.steps / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": int(2 * B * FRAME[0] * FRAME[1]),
            "d2h_bytes_per_step": int(B * m * n * (8 + 8 + 1 + 1))}
@@ -456,6 +472,7 @@ def run_gpu(args):
             "plain_form": plain,
             "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
+            "device_status": device_status,
             "stage_ms": stage_ms,
         }
         print(json.dumps(line), flush=True)
@@ -463,8 +480,81 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_serve(args):
+    """Serving form: Poisson arrivals (rate args.rate) of pairs whose size is
+    drawn uniformly from the five serving sizes, through PIVServer (tensor
+    form, continuous batching, lanes per size) and, beside it, through the
+    plain per-pair path (each pair alone, in arrival order, FP32 FFT form)."""
+    import multiprocessing as mp
+
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, PKG)
+    from openpiv_gpu import _build, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+    from openpiv_gpu.serving import PIVServer, serve_arrivals
+
+    shapes = list(synthetic._CFG5_SHAPES)
+    per_shape = 2
+    jobs = [(100 + k, shapes[k % len(shapes)]) for k in range(per_shape * len(shapes))]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        rendered = pool.map(_make_serving_pair, jobs)
+    pool_by_shape = {}
+    for (k, shape), pair in zip(jobs, rendered):
+        pool_by_shape.setdefault(tuple(shape), []).append(pair)
+    _build.build()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(5000)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
+    picks = rng.integers(len(shapes), size=args.requests)
+    frames = [pool_by_shape[tuple(shapes[i])][j % per_shape] for j, i in enumerate(picks)]
+    settings = dict(synthetic.CONFIGS[5]["piv"])
+    server = PIVServer(settings, max_batch=8, slots_per_shape=2, dft=args.dft)
+    for shape in shapes:  # lanes, plans and first launches outside the timed run
+        a, b = pool_by_shape[tuple(shape)][0]
+        server.submit(a, b)
+    server.drain()
+    server.done = []
+    done, secs = serve_arrivals(server, frames, arrivals)
+    stats = server.latency_stats()
+    # Plain per-pair path: each pair alone, in arrival order, on the FP32 FFT form.
+    kw = dict(settings)
+    mss = kw.pop("min_search_size")
+    plain = {tuple(sh): PIVGPU(tuple(sh), mss, dft="fft", **kw) for sh in shapes}
+    for sh in shapes:
+        a, b = pool_by_shape[tuple(sh)][0]
+        plain[tuple(sh)].run_batch(a[None], b[None], host_out=True)
+    lat = []
+    t0 = time.perf_counter()
+    for t_arr, (a, b) in zip(arrivals, frames):
+        while time.perf_counter() - t0 < t_arr:
+            pass
+        plain[a.shape].run_batch(a[None], b[None], host_out=True)
+        lat.append(time.perf_counter() - t0 - t_arr)
+    plain_secs = time.perf_counter() - t0
+    lat = np.array(lat)
+    line = {
+        "metric": "serving pairs/s with p50/p99 latency (Poisson arrivals, 5 frame sizes, 64->32->16 px three-pass PIV)",
+        "value": len(done) / secs, "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True,
+        "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"], "mean_ms": stats["mean_ms"], "requests": len(done),
+        "arrival_rate": args.rate, "form": args.dft, "max_batch": 8, "slots_per_shape": 2,
+        "plain_per_pair": {"pairs_per_s": args.requests / plain_secs, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                           "p99_ms": float(np.percentile(lat, 99) * 1e3), "form": "fft"},
+        "config": {"workload": "Poisson stream, sizes uniform over " + ", ".join(f"{w}x{h}" for h, w in shapes) +
+                   "; particle density U[0.01, 0.04], vortex or shear up to 12 px; 64->32->16 px @50%, median "
+                   "validation, 2 revalidated spring replacements, smoothn GCV; float32",
+                   "data": "synthetic (2 seeded pairs per size, reused)"},
+        "device_status": max(l.proc.status() for l in server.lanes.values()),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.serve:
+        run_serve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -120,11 +120,22 @@ int piv_plan_workspace_bytes(const piv_plan* plan, size_t* bytes);
  *                       in the last iteration (piv_gpu.val_locations); may be NULL.
  *   outliers:           [n_pairs][m][n] uint8, outliers left after replacement
  *                       (piv_gpu.outliers); may be NULL.
- * All kernels go to `stream`; with outputs_on_host the call returns after the
- * results are copied back, otherwise it returns without synchronising. */
+ * All kernels go to `stream`; with outputs_on_host = 1 the call returns after
+ * the results are copied back, with outputs_on_host = 2 the copies to host
+ * memory are queued on `stream` and the call returns at once (the caller
+ * synchronises the stream before reading them: lets a caller upload the next
+ * batch while this one runs), otherwise (device outputs) it returns without
+ * synchronising. */
 int piv_plan_run(piv_plan* plan, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host,
                  double* u, double* v, uint8_t* val_locations, uint8_t* outliers, int outputs_on_host,
                  void* stream);
+
+/* Device status word of the plan's bounded device-side waits (the tensor-core
+ * correlation's MMA completion waits, the spring solver's iteration cap):
+ * PIV_OK, or PIV_E_TIMEOUT when a wait gave up since the last call (the word
+ * is then reset). Synchronises `stream`. No counterpart in the reference,
+ * whose CuPy calls have no device-side waits. */
+int piv_plan_status(piv_plan* plan, int* status, void* stream);
 
 /* Per-iteration intermediates of the last piv_plan_run (device pointers owned
  * by the plan, valid until the next run): correlation output u/v (dtype of the

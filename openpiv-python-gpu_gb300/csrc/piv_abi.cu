@@ -607,7 +607,7 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
   if (val_locations) PIV_TRY(cuda_ok(cudaMemcpyAsync(val_locations, last.val0, cnt, ok, s), "result copy"));
   if (outliers) PIV_TRY(cuda_ok(cudaMemcpyAsync(outliers, p->outliers, cnt, ok, s), "result copy"));
   mark(n_stage_ids + 1);
-  if (outputs_on_host) PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
+  if (outputs_on_host == 1) PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
   return cuda_ok(cudaGetLastError(), "piv_plan_run");
 }
 
@@ -853,6 +853,17 @@ int piv_smoothn(int m, int n, int n_pairs, double* u, double* v, const uint8_t* 
   int rc = smoothn(m, n, n_pairs, u, v, u, v, field_mask, sp, p_out, scratch, s);
   cudaFreeAsync(scratch, s);
   return rc;
+}
+
+int piv_plan_status(piv_plan* plan, int* status, void* stream) {
+  if (!plan || !status) return set_error(PIV_E_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int word = 0;
+  PIV_TRY(cuda_ok(cudaMemcpyAsync(&word, plan->status, sizeof(int), cudaMemcpyDeviceToHost, s), "status copy"));
+  PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
+  if (word != PIV_OK) PIV_TRY(cuda_ok(cudaMemsetAsync(plan->status, 0, sizeof(int), s), "status reset"));
+  *status = word;
+  return PIV_OK;
 }
 
 }  // extern "C"

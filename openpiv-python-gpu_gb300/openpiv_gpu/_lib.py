@@ -69,6 +69,7 @@ _SIGNATURES = {
                              c_int, c_void_p]),
     "piv_plan_iteration_view": (c_int, [c_void_p, c_int, POINTER(PivIterationView)]),
     "piv_plan_destroy": (None, [c_void_p]),
+    "piv_plan_status": (c_int, [c_void_p, POINTER(c_int), c_void_p]),
     "piv_plan_graph_capture": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, POINTER(c_int), c_void_p]),
     "piv_plan_graph_launch": (c_int, [c_void_p, c_void_p]),

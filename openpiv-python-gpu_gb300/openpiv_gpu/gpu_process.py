@@ -425,8 +425,8 @@ class PIVGPU:
         return its
 
     # -- execution ------------------------------------------------------------
-    def _plan(self, pixel_type, n_pairs):
-        key = pixel_type
+    def _plan(self, pixel_type, n_pairs, slot=0):
+        key = (pixel_type, slot)
         entry = self._plans.get(key)
         if entry is not None and entry[1] >= n_pairs:
             return entry[0]
@@ -529,6 +529,68 @@ class PIVGPU:
         if self.max_iters == 1 and self.dtype_f == np.float32:
             u, v = u.float(), v.float()
         return u, v
+
+    def run_batches(self, batches):
+        """Pipelined run over an iterable of (frames_a, frames_b) batches of
+        host frames [B, H, W] (pinned memory gives the overlap): two plans on
+        two streams, so that one batch's upload and download overlap the
+        other's kernels. Yields (u, v) NumPy arrays per batch, in order; they
+        are views of pinned buffers that stay valid until two more batches
+        have been yielded (copy them to keep them longer).
+        """
+        torch = _torch()
+        lib = _lib.lib()
+        streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+        bufs = [None, None]
+        pending = [None, None]
+        m, n = self.piv_fields[-1].field_shape
+
+        def finish(slot):
+            B = pending[slot][0]  # the batch's frames stay referenced until its copies are done
+            streams[slot].synchronize()
+            pending[slot] = None
+            u, v, val, out = (t[:B] for t in bufs[slot][1:])
+            self.init_val_locations, self.val_locations = val.numpy().astype(bool), out.numpy().astype(bool)
+            u, v = u.numpy(), v.numpy()
+            if self.max_iters == 1 and self.dtype_f == np.float32:
+                u, v = u.astype(np.float32), v.astype(np.float32)
+            return u, v
+
+        k = 0
+        for frames_a, frames_b in batches:
+            slot = k % 2
+            if pending[slot] is not None:
+                yield finish(slot)
+            fa, pt_a, host_a = self._frames(frames_a)
+            fb, pt_b, host_b = self._frames(frames_b)
+            assert pt_a == pt_b and host_a == host_b, "both frames of a batch need the same type and location"
+            B = fa.shape[0]
+            assert tuple(fa.shape[1:]) == self.frame_shape and tuple(fb.shape) == tuple(fa.shape)
+            plan = self._plan(pt_a, B, slot)
+            if bufs[slot] is None or bufs[slot][0] < B:
+                bufs[slot] = (B,) + tuple(torch.empty((B, m, n), dtype=dt, pin_memory=True)
+                                          for dt in (torch.float64, torch.float64, torch.uint8, torch.uint8))
+            u, v, val, out = bufs[slot][1:]
+            pa = fa.ctypes.data if host_a else fa.data_ptr()
+            pb = fb.ctypes.data if host_b else fb.data_ptr()
+            _lib.check(lib.piv_plan_run(plan, B, pa, pb, host_a, u.data_ptr(), v.data_ptr(), val.data_ptr(),
+                                        out.data_ptr(), 2, streams[slot].cuda_stream))
+            pending[slot] = (B, fa, fb)
+            k += 1
+        for j in range(k, k + 2):
+            if pending[j % 2] is not None:
+                yield finish(j % 2)
+
+    def status(self):
+        """PIV_OK, or PIV_E_TIMEOUT when a bounded device-side wait of the
+        cached plans gave up since the last call (see piv_plan_status)."""
+        torch = _torch()
+        worst = 0
+        for plan, _ in self._plans.values():
+            st = ctypes.c_int(0)
+            _lib.check(_lib.lib().piv_plan_status(plan, ctypes.byref(st), torch.cuda.current_stream().cuda_stream))
+            worst = worst or st.value
+        return worst
 
     def plan_handle(self, frames, n_pairs):
         """The C plan used for frames like ``frames`` and up to n_pairs pairs."""

@@ -63,3 +63,33 @@ def test_graph_replay_equals_direct_run():
     s.synchronize()
     np.testing.assert_array_equal(u.cpu().numpy(), ud.cpu().numpy())
     np.testing.assert_array_equal(v.cpu().numpy(), vd.cpu().numpy())
+
+
+def test_pipelined_batches_equal_single_runs():
+    """PIVGPU.run_batches (two plans, two streams, asynchronous host copies)
+    returns, batch by batch and in order, the fields of separate run_batch
+    calls; the plans' device status stays PIV_OK."""
+    import torch
+
+    from openpiv_gpu import _build, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    _build.build()
+    torch.cuda.set_device(0)
+    kw = dict(synthetic.CONFIGS[2]["piv"])
+    mss = kw.pop("min_search_size")
+    batches = []
+    for b in range(5):
+        pairs = [synthetic.config_case(2, 3 * b + k, shape=(192, 224))[:2] for k in range(2)]
+        fa = torch.as_tensor(np.stack([p[0] for p in pairs])).pin_memory().numpy()
+        fb = torch.as_tensor(np.stack([p[1] for p in pairs])).pin_memory().numpy()
+        batches.append((fa, fb))
+    ref = PIVGPU((192, 224), mss, **kw, dft="tensor")
+    expect = [tuple(x.copy() for x in ref.run_batch(fa, fb, host_out=True)) for fa, fb in batches]
+    proc = PIVGPU((192, 224), mss, **kw, dft="tensor")
+    got = [(u.copy(), v.copy()) for u, v in proc.run_batches(iter(batches))]
+    assert len(got) == len(expect)
+    for (u, v), (ue, ve) in zip(got, expect):
+        np.testing.assert_array_equal(u, ue)
+        np.testing.assert_array_equal(v, ve)
+    assert proc.status() == 0 and ref.status() == 0

@@ -1,0 +1,39 @@
+"""Serving form: requests of mixed frame sizes go through the continuous-
+batching loop, and every request's result equals the result of processing its
+pair alone (bit for bit: a plan run treats the pairs of a batch independently)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_results_same_alone_and_in_the_mix():
+    import torch
+
+    from openpiv_gpu import _build, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+    from openpiv_gpu.serving import PIVServer
+
+    _build.build()
+    torch.cuda.set_device(0)
+    settings = dict(synthetic.CONFIGS[5]["piv"])
+    shapes = [(96, 128), (128, 160), (160, 96)]
+    pairs = [synthetic.config_case(5, k, shape=shapes[k % 3])[:2] for k in range(11)]
+    server = PIVServer(settings, max_batch=3, slots_per_shape=2, hbm_reserve=0)
+    reqs = []
+    for k, (a, b) in enumerate(pairs):
+        reqs.append(server.submit(a, b))
+        if k % 4 == 3:
+            server.step()  # later requests arrive while earlier ones run
+    done = server.drain()
+    assert len(done) == len(pairs)
+    stats = server.latency_stats()
+    assert stats["count"] == len(pairs) and stats["p99_ms"] >= stats["p50_ms"] > 0
+    kw = dict(settings)
+    mss = kw.pop("min_search_size")
+    for req, (a, b) in zip(reqs, pairs):
+        alone = PIVGPU(a.shape, mss, dft="tensor", **kw)
+        u, v = alone.run_batch(a[None], b[None], host_out=True)
+        np.testing.assert_array_equal(req.u, u[0])
+        np.testing.assert_array_equal(req.v, v[0])
