@@ -93,3 +93,31 @@ def test_pipelined_batches_equal_single_runs():
         np.testing.assert_array_equal(u, ue)
         np.testing.assert_array_equal(v, ve)
     assert proc.status() == 0 and ref.status() == 0
+
+
+def test_mixed_size_submission_equals_single_runs():
+    """PIVMixedBatch: pairs of three frame sizes in one submission, captured as
+    one CUDA graph over per-size plans on their own streams; every pair's result
+    equals processing it alone."""
+    import torch
+
+    from openpiv_gpu import _build, synthetic
+    from openpiv_gpu.batching import PIVMixedBatch
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    _build.build()
+    torch.cuda.set_device(0)
+    shapes = [(128, 160), (96, 96), (128, 160), (160, 224), (96, 96), (128, 160)]
+    pairs = [synthetic.config_case(4, k, shape=sh)[:2] for k, sh in enumerate(shapes)]
+    settings = dict(synthetic.CONFIGS[4]["piv"])
+    batch = PIVMixedBatch(shapes, settings, dft="tensor")
+    batch.load(pairs)
+    batch.capture()
+    batch.run()
+    got = batch.results()
+    kw = dict(settings)
+    mss = kw.pop("min_search_size")
+    for (a, b), (u, v) in zip(pairs, got):
+        ue, ve = PIVGPU(a.shape, mss, dft="tensor", **kw).run_batch(a[None], b[None], host_out=True)
+        np.testing.assert_array_equal(u, ue[0])
+        np.testing.assert_array_equal(v, ve[0])
