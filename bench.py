@@ -50,10 +50,13 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--pairs", type=int, default=128, help="pairs per step per GPU")
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--dft", choices=["fft", "tensor"], default="tensor", help="correlation engine of the chosen form")
+    ap.add_argument("--dft", choices=["fft", "tensor", "tensor_split"], default="tensor",
+                    help="correlation engine of the chosen form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
+    ap.add_argument("--no-split", action="store_true",
+                    help="skip timing the hi/lo split tensor form beside the fp16 tensor form")
     ap.add_argument("--serve", action="store_true",
                     help="serving form instead: Poisson arrivals of mixed-size pairs through the continuous-batching "
                          "loop, p50/p99 latency and pairs/s beside the plain per-pair path")
@@ -196,12 +199,13 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # Roofline helpers.
 # ---------------------------------------------------------------------------
-def tc_executed_flops(ss, N):
+def tc_executed_flops(ss, N, split=False):
     """FLOPs the tensor engine executes per window pair: packed real DFT along x
     (both frames), along y (both frames), complex inverse along f_r over N/2
-    packed columns, real inverse along f_c."""
+    packed columns, real inverse along f_c (three products per stage with
+    hi/lo split operands)."""
     macs = 2 * ss * ss * N + 2 * N * ss * N + (N // 2) * (2 * N) * (2 * N) + N * N * N
-    return 2 * macs
+    return 2 * macs * (3 if split else 1)
 
 
 def corr_flops(ss, N):
@@ -371,6 +375,18 @@ def run_gpu(args):
             ms_p = float(t.item())
         plain = {"pairs_per_s": B * world / (ms_p / args.steps * 1e-3), "ms_per_step": ms_p / args.steps}
         plain["chosen_over_plain"] = value / plain["pairs_per_s"]
+    split = None
+    proc_split = None
+    if args.dft == "tensor" and not args.no_split:
+        proc_split = make("tensor_split")
+        ms_s, _, _ = graph_time(proc_split)
+        if dist:
+            t = torch.tensor([ms_s], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_s = float(t.item())
+        split = {"pairs_per_s": B * world / (ms_s / args.steps * 1e-3), "ms_per_step": ms_s / args.steps}
+        if plain:
+            split["over_plain"] = split["pairs_per_s"] / plain["pairs_per_s"]
 
     # Stage breakdown (CUDA events inside the run, same stream).
     plan = proc.plan_handle(fa, B)
@@ -404,12 +420,14 @@ def run_gpu(args):
     achieved = flops / (corr[dom] * 1e-3) / 1e12
     peaks = measured_peaks()
     traffic_w = ncu_traffic()
-    on_tensor = args.dft == "tensor" and N == 2 * f.search_size and f.search_size in (16, 32, 64)
+    on_tensor = N == 2 * f.search_size and (
+        (args.dft == "tensor" and f.search_size in (16, 32, 64)) or
+        (args.dft == "tensor_split" and f.search_size in (16, 32)))
     if on_tensor:
         peak = peaks.get("bf16_tflops", 1900.0)
         unit, bound = "TFLOP/s", "tensor"
         src = "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in peaks else "fallback 1900 TFLOP/s"
-        key = f"correlate_tc_N{N}"
+        key = f"correlate_tc{'s' if args.dft == 'tensor_split' else ''}_N{N}"
     else:
         peak, unit, bound, src = sgemm_tflops(torch), "TFLOP/s", "fp32", "cuBLAS SGEMM (TF32 off) measured here"
         key = f"correlate_fft_N{N}"
@@ -421,7 +439,8 @@ def run_gpu(args):
                 "peak_source": src, "launch_ms": corr[dom],
                 "algorithmic_flops_per_window": corr_flops(f.search_size, N)}
     if on_tensor:
-        roofline["executed_tflops"] = n_win * tc_executed_flops(f.search_size, N) / (corr[dom] * 1e-3) / 1e12
+        roofline["executed_tflops"] = (n_win * tc_executed_flops(f.search_size, N, args.dft == "tensor_split")
+                                       / (corr[dom] * 1e-3) / 1e12)
 
     # End to end through the public API: pinned host frames in, fields out
     # (PIVGPU.run_batches: two plans on two streams, so that a batch's upload
@@ -460,6 +479,10 @@ def run_gpu(args):
             pu, pv = proc_plain.run_batch(fa[:1], fb[:1])
             pu, pv = pu[0].cpu().numpy(), pv[0].cpu().numpy()
             accuracy["plain_rms_px_vs_fp64_oracle"] = rms(pu, u64, pv, v64)
+        if proc_split is not None:
+            su, sv = proc_split.run_batch(fa[:1], fb[:1])
+            su, sv = su[0].cpu().numpy(), sv[0].cpu().numpy()
+            accuracy["split_rms_px_vs_fp64_oracle"] = rms(su, u64, sv, v64)
 
     cpu_baseline = None
     if cpu is not None:
@@ -479,7 +502,7 @@ def run_gpu(args):
                        "form": args.dft, "graph": True,
                        "l2": "inputs larger than L2 (B x 2 MiB frames + 8 MiB float frames per pair per pass)"},
             "windows_per_s": value * windows_per_pair, "windows_per_pair": windows_per_pair,
-            "plain_form": plain,
+            "plain_form": plain, "split_form": split,
             "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
             "device_status": device_status,

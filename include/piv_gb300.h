@@ -55,8 +55,13 @@ extern "C" {
 #define PIV_REPLACE_MEAN 2
 
 /* Correlation engines. */
-#define PIV_DFT_FFT32 0    /* in-shared-memory FFT in the correlation float type */
-#define PIV_DFT_TENSOR 1   /* tcgen05 tensor-core DFT (FP16 hi/lo split, FP32 accumulation) */
+#define PIV_DFT_FFT32 0          /* in-shared-memory FFT in the correlation float type */
+#define PIV_DFT_TENSOR 1         /* tcgen05 tensor-core DFT: FP16 operands, FP32 accumulation
+                                    (float32 passes with search 16, 32 or 64 px and n_fft 2;
+                                    other passes use the FFT) */
+#define PIV_DFT_TENSOR_SPLIT 2   /* as PIV_DFT_TENSOR with every operand split into FP16 hi and
+                                    lo parts and three products per stage (compensated);
+                                    search 16 or 32 px, other passes use the FFT */
 
 /* Settings of one PIV iteration, the per-pass tuple entries of
  * PIVGPU.__init__ (gpu_process.py:497-546) expanded per iteration as the

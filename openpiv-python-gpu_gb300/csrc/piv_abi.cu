@@ -266,6 +266,8 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
   if (cfg->max_pairs <= 0) return set_error(PIV_E_ARG, "max_pairs must be positive");
   if (pixel_bytes(cfg->pixel_type) == 0) return set_error(PIV_E_ARG, "unknown pixel_type %d", cfg->pixel_type);
   if (cfg->dtype != PIV_DTYPE_F32 && cfg->dtype != PIV_DTYPE_F64) return set_error(PIV_E_ARG, "unknown dtype");
+  if (cfg->dft_mode < PIV_DFT_FFT32 || cfg->dft_mode > PIV_DFT_TENSOR_SPLIT)
+    return set_error(PIV_E_ARG, "unknown dft_mode %d", cfg->dft_mode);
   if (!(cfg->dt > 0) || !(cfg->scaling_par > 0)) return set_error(PIV_E_ARG, "dt and scaling_par must be > 0");
   piv_plan* p = new piv_plan();
   p->cfg = *cfg;
@@ -540,8 +542,8 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
     c.scratch_bytes = p->corr_scratch_bytes;
     c.maps = nullptr;
     c.status = p->status;
-    if (cfg.dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
-      PIV_TRY(correlate_tensor(c, s));
+    if (correlate_tensor_supported(c, cfg.dft_mode)) {
+      PIV_TRY(correlate_tensor(c, cfg.dft_mode, s));
     } else {
       PIV_TRY(correlate_fft(c, s));
     }
@@ -697,10 +699,10 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
   c.maps = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t need = correlate_fft_scratch_bytes(fft_size, dtype);
-  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
+  if (correlate_tensor_supported(c, dft_mode)) {
     PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
-    int rc = correlate_tensor(c, s);
+    int rc = correlate_tensor(c, dft_mode, s);
     int st = 0;
     cudaMemcpyAsync(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(c.status, s);
@@ -751,10 +753,10 @@ int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a,
   c.v = (char*)u + cnt * tsz;
   c.maps = maps;
   int rc;
-  if (dft_mode == PIV_DFT_TENSOR && correlate_tensor_supported(c)) {
+  if (correlate_tensor_supported(c, dft_mode)) {
     PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
-    rc = correlate_tensor(c, s);
+    rc = correlate_tensor(c, dft_mode, s);
     cudaFreeAsync(c.status, s);
     cudaFreeAsync(u, s);
     return rc;

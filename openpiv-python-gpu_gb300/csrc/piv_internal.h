@@ -41,8 +41,9 @@ struct CorrArgs {
 
 int correlate_fft(const CorrArgs& a, cudaStream_t stream);
 size_t correlate_fft_scratch_bytes(int fft_size, int dtype);
-int correlate_tensor(const CorrArgs& a, cudaStream_t stream);
-bool correlate_tensor_supported(const CorrArgs& a);
+// dft_mode: PIV_DFT_TENSOR or PIV_DFT_TENSOR_SPLIT.
+int correlate_tensor(const CorrArgs& a, int dft_mode, cudaStream_t stream);
+bool correlate_tensor_supported(const CorrArgs& a, int dft_mode);
 
 // Deformation.
 struct DeformArgs {

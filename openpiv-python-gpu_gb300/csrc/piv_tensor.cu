@@ -37,21 +37,28 @@
 
 namespace piv {
 
-template <int SS>
+// SPLIT: every fp16 operand x is stored as hi = fp16(x) and lo = fp16(x - hi),
+// and each product runs as A_hi B_hi + A_hi B_lo + A_lo B_hi into the same
+// fp32 accumulator (compensated products): the operands then carry about 22
+// bits of mantissa instead of 11. The lo copy of each region sits right after
+// its hi copy.
+template <int SS, bool SPLIT = false>
 struct TcLayout {
   static constexpr int N = 2 * SS;           // DFT size
   static constexpr int HN = N / 2;
   static constexpr int W = 128 / SS;         // window pairs per tile
   static constexpr int TCOLS = 4 * N;        // TMEM columns (stage 2: two frames x two row tiles)
+  static constexpr int P = SPLIT ? 2 : 1;    // copies of every operand
+  static constexpr int NB1 = N * SS * 2, NB3 = 2 * N * 2 * N * 2, NB4 = N * N * 2, NOP = 1024 * SS;
   // Byte offsets in dynamic shared memory (16-byte aligned).
   static constexpr int B1 = 0;                          // F [N][SS] K-major (stages 1 and 2)
-  static constexpr int B3 = B1 + N * SS * 2;            // [2N][2N] K-major
-  static constexpr int B4 = B3 + 2 * N * 2 * N * 2;     // [N][N] K-major
+  static constexpr int B3 = B1 + P * NB1;               // [2N][2N] K-major
+  static constexpr int B4 = B3 + P * NB3;               // [N][N] K-major
   // Operand region, rewritten by each phase once the product that read it has
   // completed: A1 2 x [128][SS] K-major; A2 2 x 2 x [128][SS] MN-major; A3
   // [128][2N] K-major; A4 2 x [128][N] MN-major; then the peak-neighbour rows.
-  static constexpr int OP = B4 + N * N * 2;
-  static constexpr int STG = OP + 1024 * SS;            // next tile's float rows [frame][128][SS], 16-byte chunks swizzled
+  static constexpr int OP = B4 + P * NB4;
+  static constexpr int STG = OP + P * NOP;              // next tile's float rows [frame][128][SS], 16-byte chunks swizzled
   static constexpr int END = STG + 2 * 128 * SS * 4;
   static constexpr int A1_BYTES = 128 * SS * 2;
   static constexpr int A2_BYTES = 128 * SS * 2;
@@ -64,9 +71,17 @@ struct TcLayout {
   // the TMEM allows only two CTAs.
   static constexpr int TPL = SS == 32 ? 2 : 1;
   static constexpr int NT = 128 * TPL;
-  // CTAs per SM the register budget is compiled for.
-  static constexpr int LB_BLOCKS = MIN_BLOCKS;
+  // CTAs per SM the register budget is compiled for (shared memory limits the
+  // split form to 3 CTAs for ss 16 and 1 for ss 32).
+  static constexpr int LB_BLOCKS = !SPLIT ? MIN_BLOCKS : (SS == 16 ? 3 : 1);
+  // Operand scale: sum |2^e (a - mean)| below 2^(SCALE_BITS + 1).
+  static constexpr int SCALE_BITS = SPLIT ? 8 : 6;
 };
+
+// Eight fp32 values to fp16 at `off` and, with SPLIT, their fp16 remainders at
+// `off` of the lo copy `lo` bytes further on.
+template <bool SPLIT>
+PIV_D void st8s(unsigned char* base, int lo, uint32_t off, const float* v);
 
 // Swizzled chunk position of chunk c of staged row t: the eight rows a
 // quarter-warp reads together hit eight different 16-byte bank groups.
@@ -151,6 +166,43 @@ PIV_D void sth(unsigned char* base, uint32_t off, float v) {
   *reinterpret_cast<__half*>(base + off) = __float2half_rn(v);
 }
 
+template <bool SPLIT>
+PIV_D void st8s(unsigned char* base, int lo, uint32_t off, const float* v) {
+  st8(base, off, v);
+  if (SPLIT) {
+    float r[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = v[i] - __half2float(__float2half_rn(v[i]));
+    st8(base + lo, off, r);
+  }
+}
+
+template <bool SPLIT>
+PIV_D void sths(unsigned char* base, int lo, uint32_t off, float v) {
+  const __half h = __float2half_rn(v);
+  *reinterpret_cast<__half*>(base + off) = h;
+  if (SPLIT) *reinterpret_cast<__half*>(base + lo + off) = __float2half_rn(v - __half2float(h));
+}
+
+// D (+)= A B over `ks_n` k-steps, issued by one thread; with SPLIT also
+// A_hi B_lo and A_lo B_hi (a_lo / b_lo: byte distance to the lo copies).
+template <bool SPLIT>
+PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uint32_t a_lbo, uint32_t a_sbo,
+                     uint32_t b, uint32_t b_lo, uint32_t b_step, uint32_t b_lbo, uint32_t b_sbo, int ks_n,
+                     uint32_t id, bool acc_first) {
+  for (int ks = 0; ks < ks_n; ++ks)
+    tc::mma_f16(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo), id,
+                acc_first || ks > 0);
+  if (SPLIT) {
+    for (int ks = 0; ks < ks_n; ++ks)
+      tc::mma_f16(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + b_lo + ks * b_step, b_lbo, b_sbo),
+                  id, 1);
+    for (int ks = 0; ks < ks_n; ++ks)
+      tc::mma_f16(d, tc::sdesc(a + a_lo + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo),
+                  id, 1);
+  }
+}
+
 // 2^e for |e| <= 126.
 PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
 
@@ -207,9 +259,10 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
 // next tile's rows are then copied into shared memory with cp.async while the
 // current tile runs through its four products; otherwise each tile loads its
 // rows from global memory when it starts.
-template <int SS, bool ASYNC>
-__global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_corr_tc(CorrArgs a, int* status) {
-  using L = TcLayout<SS>;
+template <int SS, bool ASYNC, bool SPLIT>
+__global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::LB_BLOCKS)
+    k_corr_tc(CorrArgs a, int* status) {
+  using L = TcLayout<SS, SPLIT>;
   constexpr int N = L::N, HN = L::HN, W = L::W, CH = L::CH, TPL = L::TPL, NT = L::NT;
   constexpr int NPART = N / 32;      // warps per window in the epilogue
   extern __shared__ __align__(16) unsigned char sm[];
@@ -251,25 +304,29 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
     if (k == 0) v = 1.0f;
     else if (k == 1) v = ((x + p0) & 1) ? -1.0f : 1.0f;
     else v = (k & 1) ? tw_im[q] : tw_re[q];
-    sth(sm + L::B1, off_k(k, x, SS), v);
+    sths<SPLIT>(sm + L::B1, L::NB1, off_k(k, x, SS), v);
   }
+  // The split form keeps the inverse DFTs' 1/N out of B3 and B4 (their lo
+  // parts would fall below the fp16 normal range) and scales Q and U instead.
+  const float bscale = SPLIT ? 1.0f : inv_n;
   for (int e = tid; e < 4 * N * N; e += NT) {  // B3[n][kappa], kappa = (part, b, g)
     const int n = e / (2 * N), kap = e % (2 * N);
     const int part = kap / N, b = (kap % N) / HN, g = kap % HN;
     const int fr = b == 0 ? g : (g == 0 ? HN : N - g), r = n % N;
     const int q = (fr * r) % N;
-    const float cs = tw_re[q] * inv_n, sn = -tw_im[q] * inv_n;
+    const float cs = tw_re[q] * bscale, sn = -tw_im[q] * bscale;
     const float v = n < N ? (part == 0 ? cs : -sn) : (part == 0 ? sn : cs);
-    sth(sm + L::B3, off_k(n, kap, 2 * N), v);
+    sths<SPLIT>(sm + L::B3, L::NB3, off_k(n, kap, 2 * N), v);
   }
   for (int e = tid; e < N * N; e += NT) {  // B4[s][kappa], kappa = (part, c)
     const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
     const int q = (c * s_) % N;
     float v;
-    if (c == 0) v = part == 0 ? inv_n : ((s_ & 1) ? -inv_n : inv_n);
-    else v = part == 0 ? 2.0f * tw_re[q] * inv_n : 2.0f * tw_im[q] * inv_n;
-    sth(sm + L::B4, off_k(s_, kap, N), v);
+    if (c == 0) v = part == 0 ? bscale : ((s_ & 1) ? -bscale : bscale);
+    else v = part == 0 ? 2.0f * tw_re[q] * bscale : 2.0f * tw_im[q] * bscale;
+    sths<SPLIT>(sm + L::B4, L::NB4, off_k(s_, kap, N), v);
   }
+  const float oscale = SPLIT ? inv_n : 1.0f;  // applied to Q and U in the split form
   if (warp == 0) tc::tmem_alloc(&tmem_base_s, L::TCOLS);
   tc::fence_async_smem();
   tc::fence_before_sync();
@@ -383,13 +440,13 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
 #pragma unroll
         for (int o = 1; o < SS; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
         int e = 0;
-        if (l > 0.f) e = min(120, max(-120, 6 - ilogbf(l)));
+        if (l > 0.f) e = min(120, max(-120, L::SCALE_BITS - ilogbf(l)));
         const float s = pow2i(e);
 #pragma unroll
         for (int x = 0; x < SS; ++x) r[x] *= s;
         if (y == 0) sc_e[f][w] = e;
 #pragma unroll
-        for (int x = 0; x < SS; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, x, SS), r + x);
+        for (int x = 0; x < SS; x += 8) st8s<SPLIT>(sm + L::OP + f * L::A1_BYTES, L::NOP, off_k(t, x, SS), r + x);
       }
     }
     if (!sync_for_mma()) break;
@@ -403,12 +460,8 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
       const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
       for (int f = 0; f < 2; ++f)
-#pragma unroll
-        for (int ks = 0; ks < SS / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::OP + f * L::A1_BYTES + ks * 256, 128, SS * 16);
-          const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
-          tc::mma_f16(tmem + f * N, ad, bd, id, ks > 0);
-        }
+        mma_chain<SPLIT>(tmem + f * N, sbase + L::OP + f * L::A1_BYTES, L::NOP, 256, 128, SS * 16, sbase + L::B1,
+                         L::NB1, 256, 128, SS * 16, SS / 16, id, false);
       tc::mma_commit(&bar);
     }
     wait_mma();
@@ -434,7 +487,7 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
             float v8[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
-            st8(dst, off_mn(w * HN + c0, y, 128), v8);
+            st8s<SPLIT>(dst, L::NOP, off_mn(w * HN + c0, y, 128), v8);
           }
         }
       }
@@ -448,13 +501,8 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
       for (int rt = 0; rt < 2; ++rt)
 #pragma unroll
         for (int f = 0; f < 2; ++f)
-#pragma unroll
-          for (int ks = 0; ks < SS / 16; ++ks) {
-            const uint64_t ad =
-                tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
-            const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
-            tc::mma_f16(tmem + rt * 2 * N + f * N, ad, bd, id, ks > 0);
-          }
+          mma_chain<SPLIT>(tmem + rt * 2 * N + f * N, sbase + L::OP + (f * 2 + rt) * L::A2_BYTES, L::NOP, 32 * 128,
+                           128 * 16, 128, sbase + L::B1, L::NB1, 256, 128, SS * 16, SS / 16, id, false);
       tc::mma_commit(&bar);
     }
     wait_mma();
@@ -487,12 +535,12 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
             q = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
                              ob[2 * i], ob[2 * i + 1], special);
           }
-          qr0[i] = q.r0; qi0[i] = q.i0; qr1[i] = q.r1; qi1[i] = q.i1;
+          qr0[i] = q.r0 * oscale; qi0[i] = q.i0 * oscale; qr1[i] = q.r1 * oscale; qi1[i] = q.i1 * oscale;
         }
-        st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
-        st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
-        st8(dst, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
-        st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
     }
     if (!sync_for_mma()) break;
@@ -500,12 +548,8 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
     // ---- Stage 3: U = Q E / N -> TMEM cols [0, 2N).
     if (tid == 0) {
       const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
-#pragma unroll
-      for (int ks = 0; ks < 2 * N / 16; ++ks) {
-        const uint64_t ad = tc::sdesc(sbase + L::OP + ks * 256, 128, 2 * N * 16);
-        const uint64_t bd = tc::sdesc(sbase + L::B3 + ks * 256, 128, 2 * N * 16);
-        tc::mma_f16(tmem, ad, bd, id, ks > 0);
-      }
+      mma_chain<SPLIT>(tmem, sbase + L::OP, L::NOP, 256, 128, 2 * N * 16, sbase + L::B3, L::NB3, 256, 128,
+                       2 * N * 16, 2 * N / 16, id, false);
       tc::mma_commit(&bar);
     }
     wait_mma();
@@ -522,10 +566,14 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
           tc::tmem_ld16(tmem + lane_sel + part * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
+        if (SPLIT) {
+#pragma unroll
+          for (int r0 = 0; r0 < N; ++r0) v[r0] *= oscale;
+        }
 #pragma unroll
         for (int r0 = 0; r0 < N; r0 += 8) {
           const int m = w * N + r0;
-          st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
+          st8s<SPLIT>(sm + L::OP + (m >> 7) * L::A4_BYTES, L::NOP, off_mn(m & 127, part * HN + c, 128), v + r0);
         }
       }
     }
@@ -536,12 +584,8 @@ __global__ void __launch_bounds__(TcLayout<SS>::NT, TcLayout<SS>::LB_BLOCKS) k_c
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt)
-#pragma unroll
-        for (int ks = 0; ks < N / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
-          const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16);
-          tc::mma_f16(tmem + rt * N, ad, bd, id, ks > 0);
-        }
+        mma_chain<SPLIT>(tmem + rt * N, sbase + L::OP + rt * L::A4_BYTES, L::NOP, 32 * 128, 128 * 16, 128,
+                         sbase + L::B4, L::NB4, 256, 128, N * 16, N / 16, id, false);
       tc::mma_commit(&bar);
     }
     wait_mma();
@@ -1151,9 +1195,10 @@ static int launch_tc64(const CorrArgs& a, cudaStream_t stream) {
   return aligned ? launch_tc64_t<true>(a, stream) : launch_tc64_t<false>(a, stream);
 }
 
-bool correlate_tensor_supported(const CorrArgs& a) {
+bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
+  if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT) return false;
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
-         (a.ss == 16 || a.ss == 32 || a.ss == 64);
+         (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode == PIV_DFT_TENSOR));
 }
 
 // CTAs per SM and the dynamic shared memory that makes exactly that many fit:
@@ -1164,13 +1209,13 @@ struct TcLaunch {
   size_t smem = 0;
 };
 
-template <int SS, bool ASYNC>
+template <int SS, bool ASYNC, bool SPLIT>
 static int tc_launch_config(TcLaunch& out) {
-  using L = TcLayout<SS>;
+  using L = TcLayout<SS, SPLIT>;
   int dev = 0;
   cudaGetDevice(&dev);
   cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, k_corr_tc<SS, ASYNC>);
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_corr_tc<SS, ASYNC, SPLIT>);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncGetAttributes(k_corr_tc)");
   int smem_sm = 0, smem_optin = 0, resv = 0, regs_sm = 0;
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -1188,9 +1233,9 @@ static int tc_launch_config(TcLaunch& out) {
   smem = std::min(smem, (size_t)smem_optin - fa.sharedSizeBytes);
   smem = std::max(smem, L::SMEM) & ~(size_t)15;
   if (smem < L::SMEM) smem = L::SMEM;
-  e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc)");
   out.per_sm = per_sm;
@@ -1198,9 +1243,9 @@ static int tc_launch_config(TcLaunch& out) {
   return PIV_OK;
 }
 
-template <int SS, bool ASYNC>
+template <int SS, bool ASYNC, bool SPLIT>
 static int launch_tc_t(const CorrArgs& a, cudaStream_t stream) {
-  using L = TcLayout<SS>;
+  using L = TcLayout<SS, SPLIT>;
   const long long total = (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + L::W - 1) / L::W);
   static thread_local int configured_dev = -1;
@@ -1208,18 +1253,18 @@ static int launch_tc_t(const CorrArgs& a, cudaStream_t stream) {
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_dev != dev) {
-    const int rc = tc_launch_config<SS, ASYNC>(cfg);
+    const int rc = tc_launch_config<SS, ASYNC, SPLIT>(cfg);
     if (rc != PIV_OK) return rc;
     configured_dev = dev;
   }
   int grid = sm_count() * cfg.per_sm;
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc<SS, ASYNC><<<grid, L::NT, cfg.smem, stream>>>(a, a.status);
+  k_corr_tc<SS, ASYNC, SPLIT><<<grid, L::NT, cfg.smem, stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
 }
 
-template <int SS>
+template <int SS, bool SPLIT>
 static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
   const long long total = (long long)a.n_pairs * a.m * a.n;
   if (total == 0) return PIV_OK;
@@ -1229,13 +1274,16 @@ static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
   const bool aligned = a.pixel_type == PIV_PIXEL_F32 && ((uintptr_t)a.frame_a % 16) == 0 &&
                        ((uintptr_t)a.frame_b % 16) == 0 && a.width % 4 == 0 && a.x_offset % 4 == 0 &&
                        a.spacing % 4 == 0;
-  return aligned ? launch_tc_t<SS, true>(a, stream) : launch_tc_t<SS, false>(a, stream);
+  return aligned ? launch_tc_t<SS, true, SPLIT>(a, stream) : launch_tc_t<SS, false, SPLIT>(a, stream);
 }
 
-int correlate_tensor(const CorrArgs& a, cudaStream_t stream) {
-  if (!correlate_tensor_supported(a)) return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
+int correlate_tensor(const CorrArgs& a, int dft_mode, cudaStream_t stream) {
+  if (!correlate_tensor_supported(a, dft_mode))
+    return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
+  if (dft_mode == PIV_DFT_TENSOR_SPLIT)
+    return a.ss == 16 ? launch_tc<16, true>(a, stream) : launch_tc<32, true>(a, stream);
   if (a.ss == 64) return launch_tc64(a, stream);
-  return a.ss == 16 ? launch_tc<16>(a, stream) : launch_tc<32>(a, stream);
+  return a.ss == 16 ? launch_tc<16, false>(a, stream) : launch_tc<32, false>(a, stream);
 }
 
 }  // namespace piv

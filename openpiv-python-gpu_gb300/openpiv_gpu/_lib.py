@@ -25,7 +25,7 @@ DTYPE = {"float32": 0, "float64": 1}
 SUBPIXEL = {"gaussian": 0, "parabolic": 1, "centroid": 2}
 S2N = {"peak2peak": 0, "peak2mean": 1, "peak2energy": 2}
 REPLACE = {"spring": 0, "median": 1, "mean": 2}
-DFT = {"fft": 0, "tensor": 1}
+DFT = {"fft": 0, "tensor": 1, "tensor_split": 2}
 STAGES = ("predictor", "deform", "correlate", "validate", "replace", "smooth")
 
 HEADER = os.path.join(os.path.dirname(_build.ROOT), "include", "piv_gb300.h")

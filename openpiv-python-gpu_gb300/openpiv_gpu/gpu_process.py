@@ -306,7 +306,9 @@ class PIVGPU:
     deformation; any other order is the reference's bilinear deformation.
     ``batch_size`` is accepted and has no effect (every window of a pass runs
     in one launch). ``dft`` selects the correlation engine: "fft" (plain
-    float FFT) or "tensor" (tcgen05 DFT where available).
+    float FFT), "tensor" (tcgen05 DFT on fp16 operands where available) or
+    "tensor_split" (tcgen05 DFT on fp16 hi/lo operand pairs, three products
+    per stage, for 16 and 32 px passes; the FFT elsewhere).
     """
 
     def __init__(self, frame_shape, min_search_size, search_size_iters=SEARCH_SIZE_ITERS,
@@ -358,6 +360,8 @@ class PIVGPU:
         self.scaling_par = scaling_par
         self.mask = np.asarray(mask).astype(bool) if mask is not None else None
         self.dtype_f = np.float32 if dtype_f == "float32" else DTYPE_f
+        if dft not in _lib.DFT:
+            raise ValueError(f"dft must be one of {sorted(_lib.DFT)}, not {dft!r}")
         self.dft = dft
         self.init_val_locations = self.val_locations = None
         self.piv_fields = None
@@ -730,6 +734,8 @@ class CorrelationGPU:
         self.subpixel_method = subpixel_method
         self.s2n_method = s2n_method
         self.s2n_size = s2n_size
+        if dft not in _lib.DFT:
+            raise ValueError(f"dft must be one of {sorted(_lib.DFT)}, not {dft!r}")
         self.dft = dft
         self.sig2noise = None
         self._args = None
