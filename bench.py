@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default correlation launch variants instead of autotuning them per pass")
     ap.add_argument("--no-split", action="store_true",
                     help="skip timing the hi/lo split tensor form beside the fp16 tensor form")
     ap.add_argument("--serve", action="store_true",
@@ -317,7 +319,7 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
 
     def make(dft):
-        proc = PIVGPU(FRAME, mss, **kw, dft=dft)
+        proc = PIVGPU(FRAME, mss, **kw, dft=dft, autotune=not args.no_autotune)
         with torch.cuda.stream(stream):
             for _ in range(max(1, args.warmup)):
                 proc.run_batch(fa, fb)
@@ -503,6 +505,11 @@ def run_gpu(args):
                        "l2": "inputs larger than L2 (B x 2 MiB frames + 8 MiB float frames per pair per pass)"},
             "windows_per_s": value * windows_per_pair, "windows_per_pair": windows_per_pair,
             "plain_form": plain, "split_form": split,
+            "tuning": {"form": [t["name"] for t in proc.tuning()],
+                       "default_ms": [t["ms"][0] for t in proc.tuning()],
+                       "tuned_ms": [None if t["ms"][t["variant"]] is None else t["ms"][t["variant"]]
+                                    for t in proc.tuning()],
+                       "plain": [t["name"] for t in proc_plain.tuning()] if proc_plain is not None else None},
             "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
             "device_status": device_status,

@@ -142,6 +142,31 @@ int piv_plan_run(piv_plan* plan, int n_pairs, const void* frames_a, const void* 
  * whose CuPy calls have no device-side waits. */
 int piv_plan_status(piv_plan* plan, int* status, void* stream);
 
+/* Autotuner (no counterpart in the reference, whose correlation is one cuFFT
+ * call per pass). Runs the plan once on the given frames, then times every
+ * launch variant of each pass's correlation engine on that pass's own inputs
+ * (`reps` launches each after one warm-up, CUDA events on `stream`) and keeps
+ * the fastest for later runs. Variants of the FFT engine differ in radix split
+ * and tile shape (windows per CTA, threads per CTA) and agree up to rounding;
+ * variants of the tensor engines differ in CTAs per SM and staging and give
+ * identical results. Results are shared by the plans of the process (same
+ * engine, sizes, pixel type, alignment and order of magnitude of windows skip
+ * the timing). A captured graph of the plan is released. Synchronises
+ * `stream`. */
+int piv_plan_autotune(piv_plan* plan, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host,
+                      int reps, void* stream);
+/* Chosen variant of iteration `iter`, the number of variants of its engine
+ * (0 before the first run) and the autotuner's time per variant in ms (-1 where
+ * not timed), up to `capacity` entries. */
+int piv_plan_tuning(const piv_plan* plan, int iter, int* variant, int* n_variants, float* ms, int capacity);
+/* Human-readable description of variant `variant` of iteration `iter` (after a run). */
+int piv_plan_variant_name(const piv_plan* plan, int iter, int variant, char* buf, size_t len);
+/* Sets the variant of iteration `iter` (e.g. a choice saved from an earlier
+ * autotune); an out-of-range variant is an error once the plan has run. */
+int piv_plan_set_variant(piv_plan* plan, int iter, int variant);
+/* Forgets the process-wide autotuner results. */
+void piv_autotune_cache_clear(void);
+
 /* Per-iteration intermediates of the last piv_plan_run (device pointers owned
  * by the plan, valid until the next run): correlation output u/v (dtype of the
  * correlation), predictor on the iteration's grid, fields after validation and

@@ -30,10 +30,10 @@ def main():
         ref = np.exp(-2j * np.pi * k / 256)
         assert abs(vals[k][0] - ref.real) < 1e-15 and abs(vals[k][1] - ref.imag) < 1e-15, k
     lines = ["// Generated by gen_twiddles.py: W_256^k = exp(-2 pi i k / 256).", "#pragma once", ""]
-    lines.append("__constant__ double2 c_tw256_d[256] = {")
+    lines.append("static __constant__ double2 c_tw256_d[256] = {")
     lines += [f"  {{{c!r}, {s!r}}}," for c, s in vals]
     lines.append("};")
-    lines.append("__constant__ float2 c_tw256_f[256] = {")
+    lines.append("static __constant__ float2 c_tw256_f[256] = {")
     lines += [f"  {{{float(np.float32(c))!r}f, {float(np.float32(s))!r}f}}," for c, s in vals]
     lines.append("};")
     with open(os.path.join(here, "twiddles.h"), "w") as fh:

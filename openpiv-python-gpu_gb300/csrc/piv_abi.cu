@@ -19,6 +19,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <array>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -120,6 +122,13 @@ struct IterState {
   int* peak_j = nullptr;
   void* s2n = nullptr;
   uint8_t* field_mask = nullptr;
+  // Correlation launch variant (0 = default; set by piv_plan_autotune or
+  // piv_plan_set_variant), the pass's arguments of the last run, and the
+  // autotuner's per-variant times (ms, -1 = not timed).
+  int corr_variant = 0;
+  CorrArgs corr{};
+  bool corr_valid = false;
+  std::vector<float> tune_ms;
 };
 
 struct piv_plan {
@@ -192,6 +201,40 @@ static int plan_alloc_t(piv_plan* p, Ptr** ptr, size_t count) {
 }
 
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+// The correlation engine of a pass and its launch variants.
+static int run_corr(int dft_mode, const CorrArgs& c, int variant, cudaStream_t s) {
+  if (correlate_tensor_supported(c, dft_mode)) return correlate_tensor(c, dft_mode, variant, s);
+  return correlate_fft(c, variant, s);
+}
+
+static int corr_variant_count(int dft_mode, const CorrArgs& c) {
+  const int n = correlate_tensor_supported(c, dft_mode) ? correlate_tensor_variant_count(c, dft_mode)
+                                                        : correlate_fft_variant_count(c.fft_size, c.dtype);
+  return n > 0 ? n : 1;
+}
+
+// Autotuner results shared by the plans of a process: a pass with the same
+// engine, transform size, float type, window sizes, pixel type, row alignment
+// and order of magnitude of windows reuses the choice without timing again.
+using TuneKey = std::array<long long, 11>;
+static std::mutex g_tune_mu;
+static std::map<TuneKey, int> g_tune_cache;
+
+static TuneKey tune_key(int dft_mode, const CorrArgs& c) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const long long wins = (long long)c.n_pairs * c.m * c.n;
+  int bucket = 0;
+  while ((1LL << bucket) < wins) ++bucket;
+  const int engine = correlate_tensor_supported(c, dft_mode) ? dft_mode : PIV_DFT_FFT32;
+  const long long align = ((uintptr_t)c.frame_a % 16 == 0 && (uintptr_t)c.frame_b % 16 == 0 ? 1 : 0) |
+                          (c.width % 4 == 0 ? 2 : 0) | (c.width % 16 == 0 ? 4 : 0) |
+                          (c.x_offset % 4 == 0 && c.spacing % 4 == 0 ? 8 : 0) |
+                          (c.x_offset % 16 == 0 && c.spacing % 16 == 0 ? 16 : 0);
+  return TuneKey{dev, engine, c.fft_size, c.dtype, c.ss, c.ws, c.pixel_type, align, bucket, c.s2n ? 1 : 0,
+                 c.win_mask ? 1 : 0};
+}
 
 extern "C" {
 
@@ -542,11 +585,9 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
     c.scratch_bytes = p->corr_scratch_bytes;
     c.maps = nullptr;
     c.status = p->status;
-    if (correlate_tensor_supported(c, cfg.dft_mode)) {
-      PIV_TRY(correlate_tensor(c, cfg.dft_mode, s));
-    } else {
-      PIV_TRY(correlate_fft(c, s));
-    }
+    st.corr = c;
+    st.corr_valid = true;
+    PIV_TRY(run_corr(cfg.dft_mode, c, st.corr_variant, s));
     mark(k * PIV_STAGES + 2);
     PIV_TRY(combine_fields(cnt, st.u_corr, st.v_corr, cfg.dtype, st.up, st.vp, st.fp32, st.u_rep, st.v_rep, s));
     ValArgs va;
@@ -702,7 +743,7 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
   if (correlate_tensor_supported(c, dft_mode)) {
     PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
-    int rc = correlate_tensor(c, dft_mode, s);
+    int rc = correlate_tensor(c, dft_mode, 0, s);
     int st = 0;
     cudaMemcpyAsync(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(c.status, s);
@@ -714,7 +755,7 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
     PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
     c.scratch_bytes = need;
   }
-  int rc = correlate_fft(c, s);
+  int rc = correlate_fft(c, 0, s);
   if (c.scratch) cudaFreeAsync(c.scratch, s);
   return rc;
 }
@@ -756,7 +797,7 @@ int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a,
   if (correlate_tensor_supported(c, dft_mode)) {
     PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
-    rc = correlate_tensor(c, dft_mode, s);
+    rc = correlate_tensor(c, dft_mode, 0, s);
     cudaFreeAsync(c.status, s);
     cudaFreeAsync(u, s);
     return rc;
@@ -766,7 +807,7 @@ int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a,
     PIV_TRY(cuda_ok(cudaMallocAsync(&c.scratch, need, s), "cudaMallocAsync"));
     c.scratch_bytes = need;
   }
-  rc = correlate_fft(c, s);
+  rc = correlate_fft(c, 0, s);
   if (c.scratch) cudaFreeAsync(c.scratch, s);
   cudaFreeAsync(u, s);
   return rc;
@@ -866,6 +907,127 @@ int piv_plan_status(piv_plan* plan, int* status, void* stream) {
   if (word != PIV_OK) PIV_TRY(cuda_ok(cudaMemsetAsync(plan->status, 0, sizeof(int), s), "status reset"));
   *status = word;
   return PIV_OK;
+}
+
+int piv_plan_autotune(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host,
+                      int reps, void* stream_ptr) {
+  if (!p || !frames_a || !frames_b) return set_error(PIV_E_ARG, "NULL argument");
+  if (n_pairs <= 0 || n_pairs > p->cfg.max_pairs)
+    return set_error(PIV_E_ARG, "n_pairs %d outside [1, max_pairs=%d]", n_pairs, p->cfg.max_pairs);
+  if (reps <= 0) reps = 5;
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  // One run, so that every pass's inputs (the deformed frames of later
+  // passes) are those of these frames.
+  const size_t cnt = p->st.back().mn * (size_t)n_pairs;
+  double* uv = nullptr;
+  PIV_TRY(cuda_ok(cudaMallocAsync((void**)&uv, 2 * cnt * sizeof(double), s), "cudaMallocAsync"));
+  int rc = piv_plan_run(p, n_pairs, frames_a, frames_b, frames_on_host, uv, uv + cnt, nullptr, nullptr, 0, stream_ptr);
+  cudaFreeAsync(uv, s);
+  if (rc != PIV_OK) return rc;
+  PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PIV_TRY(cuda_ok(cudaEventCreate(&e0), "cudaEventCreate"));
+  rc = cuda_ok(cudaEventCreate(&e1), "cudaEventCreate");
+  for (size_t k = 0; rc == PIV_OK && k < p->st.size(); ++k) {
+    IterState& st = p->st[k];
+    const CorrArgs& c = st.corr;
+    const int nv = corr_variant_count(p->cfg.dft_mode, c);
+    st.tune_ms.assign(nv, -1.0f);
+    const TuneKey key = tune_key(p->cfg.dft_mode, c);
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto f = g_tune_cache.find(key);
+      if (f != g_tune_cache.end() && f->second < nv) {
+        st.corr_variant = f->second;
+        continue;
+      }
+    }
+    int best = 0;
+    float best_ms = 0;
+    for (int v = 0; v < nv && rc == PIV_OK; ++v) {
+      rc = run_corr(p->cfg.dft_mode, c, v, s);  // warm-up, first-use configuration
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && rc == PIV_OK; ++r) rc = run_corr(p->cfg.dft_mode, c, v, s);
+      cudaEventRecord(e1, s);
+      if (rc == PIV_OK) rc = cuda_ok(cudaEventSynchronize(e1), "autotune");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      st.tune_ms[v] = ms;
+      if (v == 0 || ms < best_ms) {
+        best_ms = ms;
+        best = v;
+      }
+    }
+    if (rc != PIV_OK) break;
+    st.corr_variant = best;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = best;
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc != PIV_OK) return rc;
+  int status = 0;
+  PIV_TRY(piv_plan_status(p, &status, stream_ptr));
+  if (status != PIV_OK) return set_error(status, "autotune: a bounded device-side wait gave up");
+  if (p->graph_exec) {  // a captured run would keep the old variants
+    cudaGraphExecDestroy(p->graph_exec);
+    p->graph_exec = nullptr;
+  }
+  return PIV_OK;
+}
+
+int piv_plan_tuning(const piv_plan* p, int iter, int* variant, int* n_variants, float* ms, int capacity) {
+  if (!p || !variant || !n_variants) return set_error(PIV_E_ARG, "NULL argument");
+  if (iter < 0 || iter >= (int)p->st.size()) return set_error(PIV_E_ARG, "iteration %d out of range", iter);
+  const IterState& st = p->st[iter];
+  *variant = st.corr_variant;
+  *n_variants = st.corr_valid ? corr_variant_count(p->cfg.dft_mode, st.corr) : 0;
+  for (int v = 0; ms && v < capacity && v < *n_variants; ++v)
+    ms[v] = v < (int)st.tune_ms.size() ? st.tune_ms[v] : -1.0f;
+  return PIV_OK;
+}
+
+int piv_plan_variant_name(const piv_plan* p, int iter, int variant, char* buf, size_t len) {
+  if (!p || !buf || len == 0) return set_error(PIV_E_ARG, "NULL argument");
+  if (iter < 0 || iter >= (int)p->st.size()) return set_error(PIV_E_ARG, "iteration %d out of range", iter);
+  const IterState& st = p->st[iter];
+  if (!st.corr_valid) return set_error(PIV_E_ARG, "the plan has not run yet");
+  const CorrArgs& c = st.corr;
+  if (correlate_tensor_supported(c, p->cfg.dft_mode)) {
+    int per_sm = 0, async = 0;
+    if (correlate_tensor_variant_describe(c, p->cfg.dft_mode, variant, &per_sm, &async) != PIV_OK)
+      return set_error(PIV_E_ARG, "variant %d out of range", variant);
+    snprintf(buf, len, "tensor%s ss=%d N=%d, %d CTA/SM, %s staging",
+             p->cfg.dft_mode == PIV_DFT_TENSOR_SPLIT ? " hi/lo" : "", c.ss, c.fft_size, per_sm,
+             async ? "async" : "sync");
+  } else {
+    int r1 = 0, r2 = 0, wpc = 0, nt = 0;
+    if (correlate_fft_variant_describe(c.fft_size, c.dtype, variant, &r1, &r2, &wpc, &nt) != PIV_OK)
+      return set_error(PIV_E_ARG, "variant %d out of range", variant);
+    snprintf(buf, len, "fft%s N=%d, radix %dx%d, %d windows/CTA, %d threads", c.dtype == PIV_DTYPE_F64 ? "64" : "32",
+             c.fft_size, r1, r2, wpc, nt);
+  }
+  return PIV_OK;
+}
+
+int piv_plan_set_variant(piv_plan* p, int iter, int variant) {
+  if (!p) return set_error(PIV_E_ARG, "NULL plan");
+  if (iter < 0 || iter >= (int)p->st.size()) return set_error(PIV_E_ARG, "iteration %d out of range", iter);
+  IterState& st = p->st[iter];
+  if (variant < 0 || (st.corr_valid && variant >= corr_variant_count(p->cfg.dft_mode, st.corr)))
+    return set_error(PIV_E_ARG, "variant %d out of range", variant);
+  st.corr_variant = variant;
+  if (p->graph_exec) {
+    cudaGraphExecDestroy(p->graph_exec);
+    p->graph_exec = nullptr;
+  }
+  return PIV_OK;
+}
+
+void piv_autotune_cache_clear(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache.clear();
 }
 
 }  // extern "C"

@@ -39,11 +39,17 @@ struct CorrArgs {
   int* status;          // device word set to PIV_E_TIMEOUT when a bounded wait gives up (tensor engine)
 };
 
-int correlate_fft(const CorrArgs& a, cudaStream_t stream);
-size_t correlate_fft_scratch_bytes(int fft_size, int dtype);
+// Launch variants (tile shape, radix split, CTAs per SM, staging) of the two
+// engines; variant 0 is the default, and an out-of-range variant runs it.
+int correlate_fft(const CorrArgs& a, int variant, cudaStream_t stream);
+int correlate_fft_variant_count(int fft_size, int dtype);
+int correlate_fft_variant_describe(int fft_size, int dtype, int variant, int* r1, int* r2, int* wpc, int* nt);
+size_t correlate_fft_scratch_bytes(int fft_size, int dtype);  // the largest over the variants
 // dft_mode: PIV_DFT_TENSOR or PIV_DFT_TENSOR_SPLIT.
-int correlate_tensor(const CorrArgs& a, int dft_mode, cudaStream_t stream);
+int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream);
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode);
+int correlate_tensor_variant_count(const CorrArgs& a, int dft_mode);
+int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int variant, int* per_sm, int* async);
 
 // Deformation.
 struct DeformArgs {

@@ -1162,6 +1162,12 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
 }
 
+#define PIV_TRY_TC(expr)             \
+  do {                               \
+    const int _rc = (expr);          \
+    if (_rc != PIV_OK) return _rc;   \
+  } while (0)
+
 template <bool ASYNC>
 static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
   const long long total = (long long)a.n_pairs * a.m * a.n;
@@ -1185,14 +1191,18 @@ static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc64 launch");
 }
 
-static int launch_tc64(const CorrArgs& a, cudaStream_t stream) {
-  const long long total = (long long)a.n_pairs * a.m * a.n;
-  if (total == 0) return PIV_OK;
-  if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
-  const bool aligned = a.pixel_type == PIV_PIXEL_U8 && ((uintptr_t)a.frame_a % 16) == 0 &&
-                       ((uintptr_t)a.frame_b % 16) == 0 && a.width % 16 == 0 && a.x_offset % 16 == 0 &&
-                       a.spacing % 16 == 0;
-  return aligned ? launch_tc64_t<true>(a, stream) : launch_tc64_t<false>(a, stream);
+// Rows of 8-bit frames start on 16-byte boundaries (asynchronous staging of
+// the 64-px engine).
+static bool tc64_aligned(const CorrArgs& a) {
+  return a.pixel_type == PIV_PIXEL_U8 && ((uintptr_t)a.frame_a % 16) == 0 && ((uintptr_t)a.frame_b % 16) == 0 &&
+         a.width % 16 == 0 && a.x_offset % 16 == 0 && a.spacing % 16 == 0;
+}
+
+// Rows of float frames start on 16-byte boundaries (asynchronous staging of
+// the 16/32-px engine).
+static bool tc_aligned(const CorrArgs& a) {
+  return a.pixel_type == PIV_PIXEL_F32 && ((uintptr_t)a.frame_a % 16) == 0 && ((uintptr_t)a.frame_b % 16) == 0 &&
+         a.width % 4 == 0 && a.x_offset % 4 == 0 && a.spacing % 4 == 0;
 }
 
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
@@ -1201,12 +1211,14 @@ bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
          (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode == PIV_DFT_TENSOR));
 }
 
-// CTAs per SM and the dynamic shared memory that makes exactly that many fit:
-// the occupancy API does not know about TMEM, so the shared-memory request is
-// padded until no more CTAs than the TMEM holds can be resident on one SM.
+// Resident CTAs per SM the 16/32-px engine allows (TMEM, registers, shared
+// memory), and the device limits the shared-memory padding is computed from:
+// the occupancy API does not know about TMEM, so a launch pads its dynamic
+// shared memory until no more than the chosen number of CTAs fits on an SM.
 struct TcLaunch {
-  int per_sm = 0;
-  size_t smem = 0;
+  int max_per_sm = 0;
+  size_t static_smem = 0;
+  int smem_sm = 0, smem_optin = 0, resv = 0;
 };
 
 template <int SS, bool ASYNC, bool SPLIT>
@@ -1229,61 +1241,119 @@ static int tc_launch_config(TcLaunch& out) {
   const int by_regs = regs_cta > 0 ? regs_sm / regs_cta : per_sm;
   per_sm = std::min(per_sm, std::min(by_smem, by_regs));
   if (per_sm < 1) return set_error(PIV_E_UNSUPPORTED, "tensor correlation does not fit on an SM");
-  size_t smem = (size_t)smem_sm / per_sm - fa.sharedSizeBytes - resv;
-  smem = std::min(smem, (size_t)smem_optin - fa.sharedSizeBytes);
-  smem = std::max(smem, L::SMEM) & ~(size_t)15;
-  if (smem < L::SMEM) smem = L::SMEM;
-  e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(smem_optin - fa.sharedSizeBytes));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_corr_tc<SS, ASYNC, SPLIT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_corr_tc)");
-  out.per_sm = per_sm;
-  out.smem = smem;
+  out.max_per_sm = per_sm;
+  out.static_smem = fa.sharedSizeBytes;
+  out.smem_sm = smem_sm;
+  out.smem_optin = smem_optin;
+  out.resv = resv;
   return PIV_OK;
 }
 
+// Dynamic shared memory that makes exactly k CTAs resident per SM.
+static size_t tc_smem_for(const TcLaunch& c, int k, size_t need) {
+  size_t smem = (size_t)c.smem_sm / k - c.static_smem - c.resv;
+  smem = std::min(smem, (size_t)c.smem_optin - c.static_smem);
+  smem = std::max(smem, need) & ~(size_t)15;
+  return smem < need ? need : smem;
+}
+
 template <int SS, bool ASYNC, bool SPLIT>
-static int launch_tc_t(const CorrArgs& a, cudaStream_t stream) {
-  using L = TcLayout<SS, SPLIT>;
-  const long long total = (long long)a.n_pairs * a.m * a.n;
-  const int n_tiles = (int)((total + L::W - 1) / L::W);
+static int tc_config_cached(TcLaunch*& cfg) {
   static thread_local int configured_dev = -1;
-  static thread_local TcLaunch cfg;
+  static thread_local TcLaunch c;
   int dev = 0;
   cudaGetDevice(&dev);
   if (configured_dev != dev) {
-    const int rc = tc_launch_config<SS, ASYNC, SPLIT>(cfg);
+    const int rc = tc_launch_config<SS, ASYNC, SPLIT>(c);
     if (rc != PIV_OK) return rc;
     configured_dev = dev;
   }
-  int grid = sm_count() * cfg.per_sm;
+  cfg = &c;
+  return PIV_OK;
+}
+
+// per_sm <= 0: as many CTAs per SM as fit.
+template <int SS, bool ASYNC, bool SPLIT>
+static int launch_tc_t(const CorrArgs& a, int per_sm, cudaStream_t stream) {
+  using L = TcLayout<SS, SPLIT>;
+  const long long total = (long long)a.n_pairs * a.m * a.n;
+  const int n_tiles = (int)((total + L::W - 1) / L::W);
+  TcLaunch* cfg = nullptr;
+  PIV_TRY_TC((tc_config_cached<SS, ASYNC, SPLIT>(cfg)));
+  const int k = per_sm <= 0 || per_sm > cfg->max_per_sm ? cfg->max_per_sm : per_sm;
+  int grid = sm_count() * k;
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc<SS, ASYNC, SPLIT><<<grid, L::NT, cfg.smem, stream>>>(a, a.status);
+  k_corr_tc<SS, ASYNC, SPLIT><<<grid, L::NT, tc_smem_for(*cfg, k, L::SMEM), stream>>>(a, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
 }
 
 template <int SS, bool SPLIT>
-static int launch_tc(const CorrArgs& a, cudaStream_t stream) {
+static int max_per_sm(bool async, int* out) {
+  TcLaunch* cfg = nullptr;
+  const int rc = async ? tc_config_cached<SS, true, SPLIT>(cfg) : tc_config_cached<SS, false, SPLIT>(cfg);
+  *out = rc == PIV_OK ? cfg->max_per_sm : 0;
+  return rc;
+}
+
+// Launch variants of a tensor pass. The 16/32-px engine: variant v runs
+// (max_per_sm - v / S) CTAs per SM with asynchronous staging when S = 2 and v
+// is even (S = 2 when the rows allow asynchronous staging, else 1). The
+// 64-px engine: one CTA per SM; variant 1 loads synchronously. Variant 0 is
+// the default; all variants give identical results.
+int correlate_tensor_variant_count(const CorrArgs& a, int dft_mode) {
+  if (!correlate_tensor_supported(a, dft_mode)) return 0;
+  if (a.ss == 64) return tc64_aligned(a) ? 2 : 1;
+  const bool al = tc_aligned(a);
+  const bool split = dft_mode == PIV_DFT_TENSOR_SPLIT;
+  int m = 0;
+  if (a.ss == 16) split ? max_per_sm<16, true>(al, &m) : max_per_sm<16, false>(al, &m);
+  else split ? max_per_sm<32, true>(al, &m) : max_per_sm<32, false>(al, &m);
+  return m * (al ? 2 : 1);
+}
+
+int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int variant, int* per_sm, int* async) {
+  const int n = correlate_tensor_variant_count(a, dft_mode);
+  if (variant < 0 || variant >= n) return PIV_E_ARG;
+  if (a.ss == 64) {
+    *per_sm = 1;
+    *async = tc64_aligned(a) && variant == 0;
+    return PIV_OK;
+  }
+  const int S = tc_aligned(a) ? 2 : 1;
+  *per_sm = n / S - variant / S;
+  *async = S == 2 && variant % 2 == 0;
+  return PIV_OK;
+}
+
+int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream) {
+  if (!correlate_tensor_supported(a, dft_mode))
+    return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
   const long long total = (long long)a.n_pairs * a.m * a.n;
   if (total == 0) return PIV_OK;
   if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
-  // Row starts on 16-byte boundaries: float frames, 16-byte aligned buffers,
-  // and widths, offsets and spacings that are multiples of four pixels.
-  const bool aligned = a.pixel_type == PIV_PIXEL_F32 && ((uintptr_t)a.frame_a % 16) == 0 &&
-                       ((uintptr_t)a.frame_b % 16) == 0 && a.width % 4 == 0 && a.x_offset % 4 == 0 &&
-                       a.spacing % 4 == 0;
-  return aligned ? launch_tc_t<SS, true, SPLIT>(a, stream) : launch_tc_t<SS, false, SPLIT>(a, stream);
-}
-
-int correlate_tensor(const CorrArgs& a, int dft_mode, cudaStream_t stream) {
-  if (!correlate_tensor_supported(a, dft_mode))
-    return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
-  if (dft_mode == PIV_DFT_TENSOR_SPLIT)
-    return a.ss == 16 ? launch_tc<16, true>(a, stream) : launch_tc<32, true>(a, stream);
-  if (a.ss == 64) return launch_tc64(a, stream);
-  return a.ss == 16 ? launch_tc<16, false>(a, stream) : launch_tc<32, false>(a, stream);
+  if (a.ss == 64) {
+    const bool async = tc64_aligned(a) && variant <= 0;
+    return async ? launch_tc64_t<true>(a, stream) : launch_tc64_t<false>(a, stream);
+  }
+  int per_sm = 0, async = tc_aligned(a);
+  if (variant > 0 && correlate_tensor_variant_describe(a, dft_mode, variant, &per_sm, &async) != PIV_OK) {
+    per_sm = 0;
+    async = tc_aligned(a);
+  }
+  const bool split = dft_mode == PIV_DFT_TENSOR_SPLIT;
+  if (a.ss == 16) {
+    if (split) return async ? launch_tc_t<16, true, true>(a, per_sm, stream) : launch_tc_t<16, false, true>(a, per_sm, stream);
+    return async ? launch_tc_t<16, true, false>(a, per_sm, stream) : launch_tc_t<16, false, false>(a, per_sm, stream);
+  }
+  if (split) return async ? launch_tc_t<32, true, true>(a, per_sm, stream) : launch_tc_t<32, false, true>(a, per_sm, stream);
+  return async ? launch_tc_t<32, true, false>(a, per_sm, stream) : launch_tc_t<32, false, false>(a, per_sm, stream);
 }
 
 }  // namespace piv

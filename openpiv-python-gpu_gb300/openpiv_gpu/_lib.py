@@ -70,6 +70,11 @@ _SIGNATURES = {
     "piv_plan_iteration_view": (c_int, [c_void_p, c_int, POINTER(PivIterationView)]),
     "piv_plan_destroy": (None, [c_void_p]),
     "piv_plan_status": (c_int, [c_void_p, POINTER(c_int), c_void_p]),
+    "piv_plan_autotune": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "piv_plan_tuning": (c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(ctypes.c_float), c_int]),
+    "piv_plan_variant_name": (c_int, [c_void_p, c_int, c_int, ctypes.c_char_p, c_size_t]),
+    "piv_plan_set_variant": (c_int, [c_void_p, c_int, c_int]),
+    "piv_autotune_cache_clear": (None, []),
     "piv_plan_graph_capture": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, POINTER(c_int), c_void_p]),
     "piv_plan_graph_launch": (c_int, [c_void_p, c_void_p]),

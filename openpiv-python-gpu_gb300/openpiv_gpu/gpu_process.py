@@ -308,7 +308,11 @@ class PIVGPU:
     in one launch). ``dft`` selects the correlation engine: "fft" (plain
     float FFT), "tensor" (tcgen05 DFT on fp16 operands where available) or
     "tensor_split" (tcgen05 DFT on fp16 hi/lo operand pairs, three products
-    per stage, for 16 and 32 px passes; the FFT elsewhere).
+    per stage, for 16 and 32 px passes; the FFT elsewhere). With
+    ``autotune=True`` the first run of each plan times every launch variant
+    of each pass's correlation engine on that run's frames (radix split and
+    tile shape of the FFT engine, CTAs per SM and staging of the tensor
+    engines) and keeps the fastest; ``tuning()`` reports the choices.
     """
 
     def __init__(self, frame_shape, min_search_size, search_size_iters=SEARCH_SIZE_ITERS,
@@ -319,7 +323,7 @@ class PIVGPU:
                  mean_tol=MEAN_TOL, rms_tol=RMS_TOL, num_replacing_iters=NUM_REPLACING_ITERS,
                  replacing_method=REPLACING_METHOD, replacing_size=REPLACING_SIZE, revalidate=REVALIDATE,
                  smooth=SMOOTH, smoothing_par=SMOOTHING_PAR, dt=1, scaling_par=1, mask=None, dtype_f=DTYPE_f,
-                 dft="fft", **aliases):
+                 dft="fft", autotune=False, **aliases):
         aliases = _apply_aliases(dict(aliases))
         if "search_size_iters" in aliases:
             search_size_iters = aliases.pop("search_size_iters")
@@ -369,6 +373,8 @@ class PIVGPU:
         self._iterations = self._build_iterations()
         self._plans = {}
         self._last = None
+        self.autotune = bool(autotune)
+        self._tuned = set()
 
     # -- geometry -------------------------------------------------------------
     def get_geom_settings(self):
@@ -518,6 +524,7 @@ class PIVGPU:
         pa = fa.ctypes.data if host_a else fa.data_ptr()
         pb = fb.ctypes.data if host_b else fb.data_ptr()
         stream = torch.cuda.current_stream().cuda_stream
+        self._maybe_tune(plan, B, pa, pb, host_a, stream)
         _lib.check(_lib.lib().piv_plan_run(plan, B, pa, pb, host_a, u.data_ptr(), v.data_ptr(), val.data_ptr(),
                                            out.data_ptr(), int(bool(host_out)), stream))
         self._last = (plan, B, fa, fb)
@@ -577,6 +584,7 @@ class PIVGPU:
             u, v, val, out = bufs[slot][1:]
             pa = fa.ctypes.data if host_a else fa.data_ptr()
             pb = fb.ctypes.data if host_b else fb.data_ptr()
+            self._maybe_tune(plan, B, pa, pb, host_a, streams[slot].cuda_stream)
             _lib.check(lib.piv_plan_run(plan, B, pa, pb, host_a, u.data_ptr(), v.data_ptr(), val.data_ptr(),
                                         out.data_ptr(), 2, streams[slot].cuda_stream))
             pending[slot] = (B, fa, fb)
@@ -584,6 +592,49 @@ class PIVGPU:
         for j in range(k, k + 2):
             if pending[j % 2] is not None:
                 yield finish(j % 2)
+
+    def _maybe_tune(self, plan, n_pairs, pa, pb, on_host, stream):
+        if self.autotune and plan.value not in self._tuned:
+            _lib.check(_lib.lib().piv_plan_autotune(plan, n_pairs, pa, pb, on_host, 5, stream))
+            self._tuned.add(plan.value)
+
+    def tune(self, frames_a, frames_b, reps=5):
+        """Autotunes the plan for batches like (frames_a, frames_b) [B, H, W]
+        now (see ``autotune``); returns ``tuning()``."""
+        torch = _torch()
+        fa, pt, host = self._frames(frames_a)
+        fb, _, _ = self._frames(frames_b)
+        plan = self._plan(pt, fa.shape[0])
+        pa = fa.ctypes.data if host else fa.data_ptr()
+        pb = fb.ctypes.data if host else fb.data_ptr()
+        _lib.check(_lib.lib().piv_plan_autotune(plan, fa.shape[0], pa, pb, host, int(reps),
+                                                torch.cuda.current_stream().cuda_stream))
+        self._tuned.add(plan.value)
+        return self.tuning(plan)
+
+    def tuning(self, plan=None):
+        """Per pass of a plan (the last one run by default): the chosen
+        correlation variant, its description, and the autotuner's time of every
+        variant in ms (None where it was not timed)."""
+        if plan is None:
+            if self._last is None:
+                return []
+            plan = self._last[0]
+        lib = _lib.lib()
+        out = []
+        for k in range(len(self._iterations)):
+            var, nv = ctypes.c_int(0), ctypes.c_int(0)
+            ms = (ctypes.c_float * 64)()
+            _lib.check(lib.piv_plan_tuning(plan, k, ctypes.byref(var), ctypes.byref(nv), ms, 64))
+            names = []
+            for j in range(nv.value):
+                buf = ctypes.create_string_buffer(128)
+                _lib.check(lib.piv_plan_variant_name(plan, k, j, buf, 128))
+                names.append(buf.value.decode())
+            times = [None if ms[j] < 0 else float(ms[j]) for j in range(min(nv.value, 64))]
+            out.append({"variant": var.value, "name": names[var.value] if names else None, "variants": names,
+                        "ms": times})
+        return out
 
     def status(self):
         """PIV_OK, or PIV_E_TIMEOUT when a bounded device-side wait of the
