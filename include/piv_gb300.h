@@ -167,6 +167,43 @@ int piv_plan_set_variant(piv_plan* plan, int iter, int variant);
 /* Forgets the process-wide autotuner results. */
 void piv_autotune_cache_clear(void);
 
+/* Multi-size batch: a submission of pairs of several frame sizes processed
+ * together (the reference processes one pair per PIVGPU call,
+ * gpu_process.py:564-647). One plan per frame size (configs[g]; every
+ * configuration has the same passes: search, window and transform sizes,
+ * normalisation, subpixel and S2N method, plus the same dtype and dft_mode).
+ * A run gives each size group its own stream for its stages; a pass on a
+ * tensor engine joins the groups and runs ONE correlation launch over the
+ * windows of every pair of every size (a segment table of up to 8 sizes per
+ * launch travels in the kernel parameters), then forks them again. Results
+ * equal each group's piv_plan_run. */
+typedef struct piv_batch piv_batch;
+int piv_batch_create(const piv_config* configs, int n_configs, piv_batch** out);
+void piv_batch_destroy(piv_batch* batch);
+/* The plan of size group `group` (iteration views, tuning, status). */
+int piv_batch_plan(piv_batch* batch, int group, piv_plan** plan);
+/* Enqueues one run on `stream` with device frames and device outputs per
+ * group (n_pairs[g] = 0 skips group g; val_locations / outliers may be NULL
+ * or hold NULL entries). Does not synchronise. */
+int piv_batch_run(piv_batch* batch, const int* n_pairs, const void* const* frames_a, const void* const* frames_b,
+                  double* const* u, double* const* v, uint8_t* const* val_locations, uint8_t* const* outliers,
+                  void* stream);
+/* Captures one run as a CUDA graph (fixed pointers and pair counts);
+ * kernel_nodes receives the number of kernel nodes. */
+int piv_batch_graph_capture(piv_batch* batch, const int* n_pairs, const void* const* frames_a,
+                            const void* const* frames_b, double* const* u, double* const* v,
+                            uint8_t* const* val_locations, uint8_t* const* outliers, int* kernel_nodes,
+                            void* stream);
+int piv_batch_graph_launch(piv_batch* batch, void* stream);
+/* Schedule of the correlation: joint = 1 (default) launches one correlation
+ * per pass over every size on the tensor engines, after joining the size
+ * groups' streams; joint = 0 keeps every size group on its own stream for
+ * the whole run (one correlation launch per size and pass, overlapping the
+ * other groups' stages). Results are the same; a captured graph is released. */
+int piv_batch_set_schedule(piv_batch* batch, int joint);
+/* Worst status word of the groups' plans (see piv_plan_status). */
+int piv_batch_status(piv_batch* batch, int* status, void* stream);
+
 /* Per-iteration intermediates of the last piv_plan_run (device pointers owned
  * by the plan, valid until the next run): correlation output u/v (dtype of the
  * correlation), predictor on the iteration's grid, fields after validation and

@@ -168,6 +168,16 @@ struct piv_plan {
   cudaGraphExec_t graph_exec = nullptr;
 };
 
+struct piv_batch {
+  std::vector<piv_plan*> plans;       // one per frame size
+  std::vector<cudaStream_t> streams;  // one per frame size
+  std::vector<cudaEvent_t> done;      // one per frame size
+  cudaEvent_t fork = nullptr;
+  std::vector<int> corr_variant;      // per pass: launch variant of the joint correlation
+  int joint = 1;                      // one correlation launch per pass over all sizes (tensor engines)
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
 static cudaEvent_t take_event(piv_plan* p) {
   if (!p->event_pool.empty()) {
     cudaEvent_t e = p->event_pool.back();
@@ -468,39 +478,49 @@ __global__ void k_mask_frames(long long npix, int n_pairs, int pixel_bytes, cons
   for (int k = 0; k < pixel_bytes; ++k) { pa[k] = 0; pb[k] = 0; }
 }
 
-int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host, double* u,
-                 double* v, uint8_t* val_locations, uint8_t* outliers, int outputs_on_host, void* stream_ptr) {
-  if (!p || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
-  if (n_pairs <= 0 || n_pairs > p->cfg.max_pairs)
-    return set_error(PIV_E_ARG, "n_pairs %d outside [1, max_pairs=%d]", n_pairs, p->cfg.max_pairs);
-  cudaStream_t s = (cudaStream_t)stream_ptr;
-  const piv_config& cfg = p->cfg;
-  const int H = cfg.height, W = cfg.width;
-  const size_t hw = (size_t)H * W;
-  const size_t pb = pixel_bytes(cfg.pixel_type);
-  const int n_stage_ids = (int)p->st.size() * PIV_STAGES;
+// One run of a plan, split into the pieces a multi-size batch interleaves:
+// run_begin (frame copies, masking), run_pre (predictor and deformation of
+// pass k; fills the pass's correlation arguments), the correlation, run_post
+// (validation, replacement, smoothing of pass k) and run_end (scaling, result
+// copies). piv_plan_run calls them in order on one stream.
+struct RunCtx {
+  int n_pairs = 0;
+  const void* fa = nullptr;
+  const void* fb = nullptr;
+  bool coef_ready = false;
   piv_plan::TimedRun* tr = nullptr;
+};
+
+static void mark(piv_plan* p, RunCtx& x, int id, cudaStream_t s) {
+  if (!x.tr) return;
+  cudaEvent_t e = take_event(p);
+  cudaEventRecord(e, s);
+  x.tr->ids.push_back(id);
+  x.tr->ev.push_back(e);
+}
+
+static int run_begin(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host,
+                     cudaStream_t s, RunCtx& x) {
+  const piv_config& cfg = p->cfg;
+  const size_t hw = (size_t)cfg.height * cfg.width;
+  const size_t pb = pixel_bytes(cfg.pixel_type);
+  x.n_pairs = n_pairs;
+  x.coef_ready = false;
+  x.tr = nullptr;
   if (p->timing) {
     p->timed.emplace_back();
-    tr = &p->timed.back();
-    tr->start = take_event(p);
-    cudaEventRecord(tr->start, s);
+    x.tr = &p->timed.back();
+    x.tr->start = take_event(p);
+    cudaEventRecord(x.tr->start, s);
   }
-  auto mark = [&](int id) {
-    if (!tr) return;
-    cudaEvent_t e = take_event(p);
-    cudaEventRecord(e, s);
-    tr->ids.push_back(id);
-    tr->ev.push_back(e);
-  };
-  const void* fa = frames_a;
-  const void* fb = frames_b;
+  x.fa = frames_a;
+  x.fb = frames_b;
   if (frames_on_host || p->frame_mask) {
     const cudaMemcpyKind kind = frames_on_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     PIV_TRY(cuda_ok(cudaMemcpyAsync(p->stage_a, frames_a, n_pairs * hw * pb, kind, s), "frame copy"));
     PIV_TRY(cuda_ok(cudaMemcpyAsync(p->stage_b, frames_b, n_pairs * hw * pb, kind, s), "frame copy"));
-    fa = p->stage_a;
-    fb = p->stage_b;
+    x.fa = p->stage_a;
+    x.fb = p->stage_b;
     if (p->frame_mask) {
       // mask_frames (gpu_process.py:682-688)
       const long long tot = (long long)hw * n_pairs;
@@ -509,134 +529,152 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
       PIV_TRY(cuda_ok(cudaGetLastError(), "k_mask_frames"));
     }
   }
-  mark(n_stage_ids);
-  bool coef_ready = false;
-  const int n_it = (int)p->st.size();
-  for (int k = 0; k < n_it; ++k) {
-    IterState& st = p->st[k];
-    const piv_iteration& it = st.it;
-    const int cnt = (int)(st.mn * n_pairs);
-    const void* ca = fa;
-    const void* cb = fb;
-    int c_pixel = cfg.pixel_type;
-    if (k > 0) {
-      IterState& pr = p->st[k - 1];
-      if (pr.g.search_size != st.g.search_size) {
-        PIV_TRY(regrid(pr.g, st.g, n_pairs, pr.u_out, pr.v_out, st.up, st.vp, s));
-      } else {
-        PIV_TRY(cuda_ok(cudaMemcpyAsync(st.up, pr.u_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
-        PIV_TRY(cuda_ok(cudaMemcpyAsync(st.vp, pr.v_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
-      }
-      mark(k * PIV_STAGES + 0);
-      if (it.deforming_order == 3 && !coef_ready) {
-        PIV_TRY(spline_prefilter(H, W, n_pairs, fa, cfg.pixel_type, p->coef, s));
-        PIV_TRY(spline_prefilter(H, W, n_pairs, fb, cfg.pixel_type, p->coef + (size_t)cfg.max_pairs * hw, s));
-        coef_ready = true;
-      }
-      DeformArgs d;
-      d.geom = st.g;
-      d.n_pairs = n_pairs;
-      d.frames_a = fa;
-      d.frames_b = fb;
-      d.pixel_type = cfg.pixel_type;
-      d.up = st.up;
-      d.vp = st.vp;
-      d.deforming_par = it.deforming_par;
-      d.order = it.deforming_order == 3 ? 3 : 1;
-      d.coef_a = p->coef;
-      d.coef_b = p->coef ? p->coef + (size_t)cfg.max_pairs * hw : nullptr;
-      d.frame_mask = p->frame_mask;
-      d.dtype = cfg.dtype;
-      d.out_a = p->def_a;
-      d.out_b = p->def_b;
-      PIV_TRY(deform(d, s));
-      mark(k * PIV_STAGES + 1);
-      ca = p->def_a;
-      cb = p->def_b;
-      c_pixel = cfg.dtype == PIV_DTYPE_F64 ? PIV_PIXEL_F64 : PIV_PIXEL_F32;
+  mark(p, x, (int)p->st.size() * PIV_STAGES, s);
+  return PIV_OK;
+}
+
+static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
+  const piv_config& cfg = p->cfg;
+  const int H = cfg.height, W = cfg.width;
+  const size_t hw = (size_t)H * W;
+  const int n_pairs = x.n_pairs;
+  IterState& st = p->st[k];
+  const piv_iteration& it = st.it;
+  const int cnt = (int)(st.mn * n_pairs);
+  const void* ca = x.fa;
+  const void* cb = x.fb;
+  int c_pixel = cfg.pixel_type;
+  if (k > 0) {
+    IterState& pr = p->st[k - 1];
+    if (pr.g.search_size != st.g.search_size) {
+      PIV_TRY(regrid(pr.g, st.g, n_pairs, pr.u_out, pr.v_out, st.up, st.vp, s));
+    } else {
+      PIV_TRY(cuda_ok(cudaMemcpyAsync(st.up, pr.u_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
+      PIV_TRY(cuda_ok(cudaMemcpyAsync(st.vp, pr.v_out, cnt * 8, cudaMemcpyDeviceToDevice, s), "predictor copy"));
     }
-    CorrArgs c{};
-    c.frame_a = ca;
-    c.frame_b = cb;
-    c.pixel_type = c_pixel;
-    c.height = H;
-    c.width = W;
-    c.ss = st.g.search_size;
-    c.ws = st.g.window_size;
-    c.spacing = st.g.spacing;
-    c.m = st.g.m;
-    c.n = st.g.n;
-    c.x_offset = st.g.x_offset;
-    c.y_offset = st.g.y_offset;
-    c.n_pairs = n_pairs;
-    c.fft_size = it.fft_size;
-    c.normalize = it.normalize;
-    c.subpixel = it.subpixel_method;
-    c.dtype = cfg.dtype;
-    c.win_mask = st.field_mask;
-    c.u = st.u_corr;
-    c.v = st.v_corr;
-    c.peak_i = st.peak_i;
-    c.peak_j = st.peak_j;
-    c.s2n = st.s2n;
-    c.s2n_method = it.s2n_method;
-    c.s2n_size = it.s2n_size;
-    c.scratch = p->corr_scratch;
-    c.scratch_bytes = p->corr_scratch_bytes;
-    c.maps = nullptr;
-    c.status = p->status;
-    st.corr = c;
-    st.corr_valid = true;
-    PIV_TRY(run_corr(cfg.dft_mode, c, st.corr_variant, s));
-    mark(k * PIV_STAGES + 2);
-    PIV_TRY(combine_fields(cnt, st.u_corr, st.v_corr, cfg.dtype, st.up, st.vp, st.fp32, st.u_rep, st.v_rep, s));
-    ValArgs va;
-    va.m = st.g.m;
-    va.n = st.g.n;
-    va.n_pairs = n_pairs;
+    mark(p, x, k * PIV_STAGES + 0, s);
+    if (it.deforming_order == 3 && !x.coef_ready) {
+      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fa, cfg.pixel_type, p->coef, s));
+      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fb, cfg.pixel_type, p->coef + (size_t)cfg.max_pairs * hw, s));
+      x.coef_ready = true;
+    }
+    DeformArgs d;
+    d.geom = st.g;
+    d.n_pairs = n_pairs;
+    d.frames_a = x.fa;
+    d.frames_b = x.fb;
+    d.pixel_type = cfg.pixel_type;
+    d.up = st.up;
+    d.vp = st.vp;
+    d.deforming_par = it.deforming_par;
+    d.order = it.deforming_order == 3 ? 3 : 1;
+    d.coef_a = p->coef;
+    d.coef_b = p->coef ? p->coef + (size_t)cfg.max_pairs * hw : nullptr;
+    d.frame_mask = p->frame_mask;
+    d.dtype = cfg.dtype;
+    d.out_a = p->def_a;
+    d.out_b = p->def_b;
+    PIV_TRY(deform(d, s));
+    mark(p, x, k * PIV_STAGES + 1, s);
+    ca = p->def_a;
+    cb = p->def_b;
+    c_pixel = cfg.dtype == PIV_DTYPE_F64 ? PIV_PIXEL_F64 : PIV_PIXEL_F32;
+  }
+  c = CorrArgs{};
+  c.frame_a = ca;
+  c.frame_b = cb;
+  c.pixel_type = c_pixel;
+  c.height = H;
+  c.width = W;
+  c.ss = st.g.search_size;
+  c.ws = st.g.window_size;
+  c.spacing = st.g.spacing;
+  c.m = st.g.m;
+  c.n = st.g.n;
+  c.x_offset = st.g.x_offset;
+  c.y_offset = st.g.y_offset;
+  c.n_pairs = n_pairs;
+  c.fft_size = it.fft_size;
+  c.normalize = it.normalize;
+  c.subpixel = it.subpixel_method;
+  c.dtype = cfg.dtype;
+  c.win_mask = st.field_mask;
+  c.u = st.u_corr;
+  c.v = st.v_corr;
+  c.peak_i = st.peak_i;
+  c.peak_j = st.peak_j;
+  c.s2n = st.s2n;
+  c.s2n_method = it.s2n_method;
+  c.s2n_size = it.s2n_size;
+  c.scratch = p->corr_scratch;
+  c.scratch_bytes = p->corr_scratch_bytes;
+  c.maps = nullptr;
+  c.status = p->status;
+  st.corr = c;
+  st.corr_valid = true;
+  return PIV_OK;
+}
+
+static int run_post(piv_plan* p, int k, RunCtx& x, cudaStream_t s) {
+  const piv_config& cfg = p->cfg;
+  const int n_pairs = x.n_pairs;
+  const int n_it = (int)p->st.size();
+  IterState& st = p->st[k];
+  const piv_iteration& it = st.it;
+  const int cnt = (int)(st.mn * n_pairs);
+  PIV_TRY(combine_fields(cnt, st.u_corr, st.v_corr, cfg.dtype, st.up, st.vp, st.fp32, st.u_rep, st.v_rep, s));
+  ValArgs va;
+  va.m = st.g.m;
+  va.n = st.g.n;
+  va.n_pairs = n_pairs;
+  va.u = st.u_rep;
+  va.v = st.v_rep;
+  va.s2n = st.s2n;
+  va.s2n_dtype = cfg.dtype;
+  va.size = it.validation_size;
+  va.s2n_tol = it.s2n_tol;
+  va.median_tol = it.median_tol;
+  va.mad_tol = it.mad_tol;
+  va.mean_tol = it.mean_tol;
+  va.rms_tol = it.rms_tol;
+  va.field_mask = st.field_mask;
+  va.exclude = nullptr;
+  va.fp32 = st.fp32;
+  PIV_TRY(validate(va, st.val0, p->rms_stats, s));
+  PIV_TRY(cuda_ok(cudaMemcpyAsync(st.val, st.val0, cnt, cudaMemcpyDeviceToDevice, s), "val copy"));
+  mark(p, x, k * PIV_STAGES + 3, s);
+  RepArgs ra;
+  ra.val = va;
+  ra.u = st.u_rep;
+  ra.v = st.v_rep;
+  ra.val_mask = st.val;
+  ra.n_iters = it.num_replacing_iters;
+  ra.method = it.replacing_method;
+  ra.size = it.replacing_size;
+  ra.revalidate = it.revalidate;
+  ra.dtype = cfg.dtype;
+  ra.scratch = p->rep_scratch;
+  ra.status = p->status;
+  PIV_TRY(replace(ra, s));
+  if (k == n_it - 1) {
     va.u = st.u_rep;
     va.v = st.v_rep;
-    va.s2n = st.s2n;
-    va.s2n_dtype = cfg.dtype;
-    va.size = it.validation_size;
-    va.s2n_tol = it.s2n_tol;
-    va.median_tol = it.median_tol;
-    va.mad_tol = it.mad_tol;
-    va.mean_tol = it.mean_tol;
-    va.rms_tol = it.rms_tol;
-    va.field_mask = st.field_mask;
-    va.exclude = nullptr;
-    va.fp32 = st.fp32;
-    PIV_TRY(validate(va, st.val0, p->rms_stats, s));
-    PIV_TRY(cuda_ok(cudaMemcpyAsync(st.val, st.val0, cnt, cudaMemcpyDeviceToDevice, s), "val copy"));
-    mark(k * PIV_STAGES + 3);
-    RepArgs ra;
-    ra.val = va;
-    ra.u = st.u_rep;
-    ra.v = st.v_rep;
-    ra.val_mask = st.val;
-    ra.n_iters = it.num_replacing_iters;
-    ra.method = it.replacing_method;
-    ra.size = it.replacing_size;
-    ra.revalidate = it.revalidate;
-    ra.dtype = cfg.dtype;
-    ra.scratch = p->rep_scratch;
-    ra.status = p->status;
-    PIV_TRY(replace(ra, s));
-    if (k == n_it - 1) {
-      va.u = st.u_rep;
-      va.v = st.v_rep;
-      PIV_TRY(validate(va, p->outliers, p->rms_stats, s));
-    }
-    mark(k * PIV_STAGES + 4);
-    if (k != n_it - 1) {
-      PIV_TRY(smoothn(st.g.m, st.g.n, n_pairs, st.u_rep, st.v_rep, st.u_out, st.v_out, st.field_mask,
-                      it.smoothing_par, st.smooth_p, p->smooth_scratch, s));
-      mark(k * PIV_STAGES + 5);
-    }
+    PIV_TRY(validate(va, p->outliers, p->rms_stats, s));
   }
+  mark(p, x, k * PIV_STAGES + 4, s);
+  if (k != n_it - 1) {
+    PIV_TRY(smoothn(st.g.m, st.g.n, n_pairs, st.u_rep, st.v_rep, st.u_out, st.v_out, st.field_mask,
+                    it.smoothing_par, st.smooth_p, p->smooth_scratch, s));
+    mark(p, x, k * PIV_STAGES + 5, s);
+  }
+  return PIV_OK;
+}
+
+static int run_end(piv_plan* p, RunCtx& x, double* u, double* v, uint8_t* val_locations, uint8_t* outliers,
+                   int outputs_on_host, cudaStream_t s) {
+  const piv_config& cfg = p->cfg;
   IterState& last = p->st.back();
-  const int cnt = (int)(last.mn * n_pairs);
+  const int cnt = (int)(last.mn * x.n_pairs);
   const double* ru = last.u_rep;
   const double* rv = last.v_rep;
   if (cfg.dt != 1 || cfg.scaling_par != 1) {
@@ -649,7 +687,26 @@ int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* fra
   PIV_TRY(cuda_ok(cudaMemcpyAsync(v, rv, cnt * 8, ok, s), "result copy"));
   if (val_locations) PIV_TRY(cuda_ok(cudaMemcpyAsync(val_locations, last.val0, cnt, ok, s), "result copy"));
   if (outliers) PIV_TRY(cuda_ok(cudaMemcpyAsync(outliers, p->outliers, cnt, ok, s), "result copy"));
-  mark(n_stage_ids + 1);
+  mark(p, x, (int)p->st.size() * PIV_STAGES + 1, s);
+  return PIV_OK;
+}
+
+int piv_plan_run(piv_plan* p, int n_pairs, const void* frames_a, const void* frames_b, int frames_on_host, double* u,
+                 double* v, uint8_t* val_locations, uint8_t* outliers, int outputs_on_host, void* stream_ptr) {
+  if (!p || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (n_pairs <= 0 || n_pairs > p->cfg.max_pairs)
+    return set_error(PIV_E_ARG, "n_pairs %d outside [1, max_pairs=%d]", n_pairs, p->cfg.max_pairs);
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  RunCtx x;
+  PIV_TRY(run_begin(p, n_pairs, frames_a, frames_b, frames_on_host, s, x));
+  for (int k = 0; k < (int)p->st.size(); ++k) {
+    CorrArgs c;
+    PIV_TRY(run_pre(p, k, x, s, c));
+    PIV_TRY(run_corr(p->cfg.dft_mode, c, p->st[k].corr_variant, s));
+    mark(p, x, k * PIV_STAGES + 2, s);
+    PIV_TRY(run_post(p, k, x, s));
+  }
+  PIV_TRY(run_end(p, x, u, v, val_locations, outliers, outputs_on_host, s));
   if (outputs_on_host == 1) PIV_TRY(cuda_ok(cudaStreamSynchronize(s), "stream synchronize"));
   return cuda_ok(cudaGetLastError(), "piv_plan_run");
 }
@@ -1028,6 +1085,217 @@ int piv_plan_set_variant(piv_plan* p, int iter, int variant) {
 void piv_autotune_cache_clear(void) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   g_tune_cache.clear();
+}
+
+// ---------------------------------------------------------------------------
+// Multi-size batches.
+// ---------------------------------------------------------------------------
+int piv_batch_create(const piv_config* cfgs, int n_cfgs, piv_batch** out) {
+  if (!cfgs || !out || n_cfgs <= 0) return set_error(PIV_E_ARG, "NULL argument or no configuration");
+  *out = nullptr;
+  const piv_config& c0 = cfgs[0];
+  for (int g = 1; g < n_cfgs; ++g) {
+    const piv_config& c = cfgs[g];
+    if (c.n_iters != c0.n_iters || c.dtype != c0.dtype || c.dft_mode != c0.dft_mode)
+      return set_error(PIV_E_ARG, "batch configuration %d differs in passes, dtype or dft_mode", g);
+    for (int k = 0; k < c0.n_iters; ++k) {
+      const piv_iteration &a = c0.iters[k], &b = c.iters[k];
+      if (a.search_size != b.search_size || a.window_size != b.window_size || a.fft_size != b.fft_size ||
+          a.normalize != b.normalize || a.subpixel_method != b.subpixel_method || a.s2n_method != b.s2n_method)
+        return set_error(PIV_E_ARG, "batch configuration %d differs from configuration 0 in pass %d", g, k);
+    }
+  }
+  piv_batch* b = new piv_batch();
+  int rc = PIV_OK;
+  for (int g = 0; g < n_cfgs && rc == PIV_OK; ++g) {
+    piv_plan* p = nullptr;
+    rc = piv_plan_create(&cfgs[g], &p);
+    if (rc == PIV_OK) b->plans.push_back(p);
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (rc == PIV_OK) rc = cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (rc == PIV_OK) b->streams.push_back(st);
+    if (rc == PIV_OK) rc = cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+    if (rc == PIV_OK) b->done.push_back(ev);
+  }
+  if (rc == PIV_OK) rc = cuda_ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
+  if (rc != PIV_OK) {
+    piv_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return PIV_OK;
+}
+
+void piv_batch_destroy(piv_batch* b) {
+  if (!b) return;
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  for (piv_plan* p : b->plans) piv_plan_destroy(p);
+  for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : b->done) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  delete b;
+}
+
+int piv_batch_plan(piv_batch* b, int group, piv_plan** plan) {
+  if (!b || !plan) return set_error(PIV_E_ARG, "NULL argument");
+  if (group < 0 || group >= (int)b->plans.size()) return set_error(PIV_E_ARG, "group %d out of range", group);
+  *plan = b->plans[group];
+  return PIV_OK;
+}
+
+// Enqueues one batch run: every size group runs its stages on its own stream;
+// a pass on a tensor engine joins the groups, launches one correlation over
+// all their windows (up to kMaxCorrSegs sizes per launch) on `s` and forks
+// again.
+static int batch_enqueue(piv_batch* b, const int* n_pairs, const void* const* frames_a,
+                         const void* const* frames_b, double* const* u, double* const* v,
+                         uint8_t* const* val_locations, uint8_t* const* outliers, cudaStream_t s) {
+  const int G = (int)b->plans.size();
+  std::vector<int> act;  // groups with pairs in this run
+  for (int g = 0; g < G; ++g) {
+    if (n_pairs[g] < 0 || n_pairs[g] > b->plans[g]->cfg.max_pairs)
+      return set_error(PIV_E_ARG, "group %d: n_pairs %d outside [0, %d]", g, n_pairs[g], b->plans[g]->cfg.max_pairs);
+    if (n_pairs[g] == 0) continue;
+    if (!frames_a[g] || !frames_b[g] || !u[g] || !v[g]) return set_error(PIV_E_ARG, "group %d: NULL argument", g);
+    act.push_back(g);
+  }
+  if (act.empty()) return PIV_OK;
+  std::vector<RunCtx> x(G);
+  PIV_TRY(cuda_ok(cudaEventRecord(b->fork, s), "cudaEventRecord"));
+  for (int g : act) {
+    PIV_TRY(cuda_ok(cudaStreamWaitEvent(b->streams[g], b->fork, 0), "cudaStreamWaitEvent"));
+    PIV_TRY(run_begin(b->plans[g], n_pairs[g], frames_a[g], frames_b[g], 0, b->streams[g], x[g]));
+  }
+  const int n_it = (int)b->plans[0]->st.size();
+  const int mode = b->plans[0]->cfg.dft_mode;
+  for (int k = 0; k < n_it; ++k) {
+    std::vector<CorrArgs> cs(G);
+    bool joint = b->joint != 0;
+    for (int g : act) {
+      PIV_TRY(run_pre(b->plans[g], k, x[g], b->streams[g], cs[g]));
+      joint = joint && correlate_tensor_supported(cs[g], mode) && cs[g].pixel_type == cs[act[0]].pixel_type;
+    }
+    if (joint) {
+      for (int g : act) {
+        PIV_TRY(cuda_ok(cudaEventRecord(b->done[g], b->streams[g]), "cudaEventRecord"));
+        PIV_TRY(cuda_ok(cudaStreamWaitEvent(s, b->done[g], 0), "cudaStreamWaitEvent"));
+      }
+      for (size_t c0 = 0; c0 < act.size(); c0 += kMaxCorrSegs) {
+        CorrArgs m = cs[act[c0]];
+        m.n_segs = 0;
+        m.seg_windows = 0;
+        for (size_t j = c0; j < act.size() && j < c0 + kMaxCorrSegs; ++j) {
+          const CorrArgs& c = cs[act[j]];
+          CorrSeg& q = m.segs[m.n_segs++];
+          q.frame_a = c.frame_a;
+          q.frame_b = c.frame_b;
+          q.u = c.u;
+          q.v = c.v;
+          q.peak_i = c.peak_i;
+          q.peak_j = c.peak_j;
+          q.win_mask = c.win_mask;
+          q.win0 = m.seg_windows;
+          q.height = c.height;
+          q.width = c.width;
+          q.spacing = c.spacing;
+          q.m = c.m;
+          q.n = c.n;
+          q.x_offset = c.x_offset;
+          q.y_offset = c.y_offset;
+          q.n_pairs = c.n_pairs;
+          m.seg_windows += (long long)c.n_pairs * c.m * c.n;
+        }
+        const int var = k < (int)b->corr_variant.size() ? b->corr_variant[k] : 0;
+        PIV_TRY(run_corr(mode, m, var, s));
+      }
+      PIV_TRY(cuda_ok(cudaEventRecord(b->fork, s), "cudaEventRecord"));
+      for (int g : act) PIV_TRY(cuda_ok(cudaStreamWaitEvent(b->streams[g], b->fork, 0), "cudaStreamWaitEvent"));
+    } else {
+      for (int g : act) PIV_TRY(run_corr(mode, cs[g], b->plans[g]->st[k].corr_variant, b->streams[g]));
+    }
+    for (int g : act) PIV_TRY(run_post(b->plans[g], k, x[g], b->streams[g]));
+  }
+  for (int g : act) {
+    PIV_TRY(run_end(b->plans[g], x[g], u[g], v[g], val_locations ? val_locations[g] : nullptr,
+                    outliers ? outliers[g] : nullptr, 0, b->streams[g]));
+    PIV_TRY(cuda_ok(cudaEventRecord(b->done[g], b->streams[g]), "cudaEventRecord"));
+    PIV_TRY(cuda_ok(cudaStreamWaitEvent(s, b->done[g], 0), "cudaStreamWaitEvent"));
+  }
+  return PIV_OK;
+}
+
+int piv_batch_run(piv_batch* b, const int* n_pairs, const void* const* frames_a, const void* const* frames_b,
+                  double* const* u, double* const* v, uint8_t* const* val_locations, uint8_t* const* outliers,
+                  void* stream) {
+  if (!b || !n_pairs || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  PIV_TRY(batch_enqueue(b, n_pairs, frames_a, frames_b, u, v, val_locations, outliers, (cudaStream_t)stream));
+  return cuda_ok(cudaGetLastError(), "piv_batch_run");
+}
+
+int piv_batch_graph_capture(piv_batch* b, const int* n_pairs, const void* const* frames_a,
+                            const void* const* frames_b, double* const* u, double* const* v,
+                            uint8_t* const* val_locations, uint8_t* const* outliers, int* kernel_nodes,
+                            void* stream) {
+  if (!b || !n_pairs || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  if (!stream) return set_error(PIV_E_ARG, "graph capture needs a non-default stream");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    b->graph_exec = nullptr;
+  }
+  PIV_TRY(cuda_ok(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture"));
+  int rc = batch_enqueue(b, n_pairs, frames_a, frames_b, u, v, val_locations, outliers, s);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != PIV_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_cuda_error(e, "cudaStreamEndCapture");
+  if (kernel_nodes) {
+    size_t n = 0;
+    cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(graph, nodes.data(), &n);
+    int kn = 0;
+    for (size_t i = 0; i < n; ++i) {
+      cudaGraphNodeType t;
+      cudaGraphNodeGetType(nodes[i], &t);
+      if (t == cudaGraphNodeTypeKernel) ++kn;
+    }
+    *kernel_nodes = kn;
+  }
+  e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  return cuda_ok(e, "cudaGraphInstantiate");
+}
+
+int piv_batch_graph_launch(piv_batch* b, void* stream) {
+  if (!b || !b->graph_exec) return set_error(PIV_E_ARG, "no captured graph");
+  return cuda_ok(cudaGraphLaunch(b->graph_exec, (cudaStream_t)stream), "cudaGraphLaunch");
+}
+
+int piv_batch_set_schedule(piv_batch* b, int joint) {
+  if (!b) return set_error(PIV_E_ARG, "NULL batch");
+  b->joint = joint != 0;
+  if (b->graph_exec) {
+    cudaGraphExecDestroy(b->graph_exec);
+    b->graph_exec = nullptr;
+  }
+  return PIV_OK;
+}
+
+int piv_batch_status(piv_batch* b, int* status, void* stream) {
+  if (!b || !status) return set_error(PIV_E_ARG, "NULL argument");
+  int worst = PIV_OK;
+  for (piv_plan* p : b->plans) {
+    int st = PIV_OK;
+    PIV_TRY(piv_plan_status(p, &st, stream));
+    if (worst == PIV_OK) worst = st;
+  }
+  *status = worst;
+  return PIV_OK;
 }
 
 }  // extern "C"

@@ -14,6 +14,22 @@ int set_error(int code, const char* fmt, ...);
 int set_cuda_error(cudaError_t e, const char* what);
 
 // Arguments of one correlation pass over n_pairs frame pairs.
+// One frame geometry of a multi-geometry correlation launch: the windows of
+// n_pairs pairs of one frame size, global windows [win0, win0 + n_pairs m n)
+// of the launch, with their own frames and outputs.
+struct CorrSeg {
+  const void* frame_a;
+  const void* frame_b;
+  void* u;
+  void* v;
+  int* peak_i;
+  int* peak_j;
+  const uint8_t* win_mask;
+  long long win0;
+  int height, width, spacing, m, n, x_offset, y_offset, n_pairs;
+};
+constexpr int kMaxCorrSegs = 8;
+
 struct CorrArgs {
   const void* frame_a;
   const void* frame_b;
@@ -37,6 +53,13 @@ struct CorrArgs {
   size_t scratch_bytes;
   void* maps;           // optional [windows][N][N] output of the shifted correlation maps
   int* status;          // device word set to PIV_E_TIMEOUT when a bounded wait gives up (tensor engine)
+  // Multi-geometry launch (tensor engines): n_segs > 0 segments replace the
+  // single geometry above (frames, sizes, outputs, mask; the window and search
+  // sizes, pixel type and settings are shared), covering seg_windows windows
+  // in total. The table travels in the kernel parameters.
+  int n_segs;
+  long long seg_windows;
+  CorrSeg segs[kMaxCorrSegs];
 };
 
 // Launch variants (tile shape, radix split, CTAs per SM, staging) of the two

@@ -259,6 +259,41 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
 // next tile's rows are then copied into shared memory with cp.async while the
 // current tile runs through its four products; otherwise each tile loads its
 // rows from global memory when it starts.
+// The launch's segment table in shared memory (one segment built from the
+// single geometry of `a` when a.n_segs == 0); returns the segment count. All
+// threads call it; it ends with a barrier.
+PIV_D int load_segments(const CorrArgs& a, CorrSeg* seg_s) {
+  const int n = a.n_segs > 0 ? a.n_segs : 1;
+  if ((int)threadIdx.x < n) {
+    CorrSeg q;
+    if (a.n_segs > 0) {
+#pragma unroll
+      for (int k = 0; k < kMaxCorrSegs; ++k)  // static indices keep the table in parameter space
+        if (k == (int)threadIdx.x) q = a.segs[k];
+    } else {
+      q.frame_a = a.frame_a;
+      q.frame_b = a.frame_b;
+      q.u = a.u;
+      q.v = a.v;
+      q.peak_i = a.peak_i;
+      q.peak_j = a.peak_j;
+      q.win_mask = a.win_mask;
+      q.win0 = 0;
+      q.height = a.height;
+      q.width = a.width;
+      q.spacing = a.spacing;
+      q.m = a.m;
+      q.n = a.n;
+      q.x_offset = a.x_offset;
+      q.y_offset = a.y_offset;
+      q.n_pairs = a.n_pairs;
+    }
+    seg_s[threadIdx.x] = q;
+  }
+  __syncthreads();
+  return n;
+}
+
 template <int SS, bool ASYNC, bool SPLIT>
 __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::LB_BLOCKS)
     k_corr_tc(CorrArgs a, int* status) {
@@ -272,6 +307,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   __shared__ int sc_e[2][W];         // per frame and window: log2 of the operand scale
   __shared__ long long win_base[2][W];
   __shared__ int win_valid[2][W];
+  __shared__ long long win_loc[2][W];  // window index within its segment
+  __shared__ int win_seg[2][W];
+  __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float pk_val[W][NPART];
   __shared__ int pk_idx[W][NPART];
 
@@ -336,11 +374,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   const uint32_t sbase = tc::smem_u32(sm);
   uint32_t phase = 0;
 
-  const int sp = a.spacing, nf = a.n;
-  const int n_wins = a.m * a.n;
-  const long long total = (long long)a.n_pairs * n_wins;
+  const int n_seg = load_segments(a, seg_s);
+  const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + W - 1) / W);
-  const long long frame_elems = (long long)a.height * a.width;
 
   // Every thread waits for the last commit itself; a wait that gives up sets
   // abort_s, which all threads read after the next barrier and leave the tile
@@ -365,24 +401,33 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   auto window_setup = [&](int tl, int sl) {
     const long long g = (long long)tl * W + tid;
     int ok = tl < n_tiles && g < total;
-    long long base = 0;
+    long long base = 0, loc = 0;
+    int sg = 0;
     if (ok) {
-      const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-      if (a.win_mask) ok = a.win_mask[k] == 0;
-      base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
+      while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
+      const CorrSeg& q = seg_s[sg];
+      loc = g - q.win0;
+      const int nw = q.m * q.n;
+      const int pair = (int)(loc / nw), k = (int)(loc % nw);
+      if (q.win_mask) ok = q.win_mask[k] == 0;
+      base = pair * (long long)q.height * q.width + (long long)((k / q.n) * q.spacing + q.y_offset) * q.width +
+             (k % q.n) * q.spacing + q.x_offset;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
+    win_loc[sl][tid] = loc;
+    win_seg[sl][tid] = sg;
   };
   // Thread (half, t) starts the copies of row t of its frames of the tile in slot `sl`.
   auto stage_async = [&](int sl) {
     const int w = t / SS, y = t % SS;
     if (!win_valid[sl][w]) return;
-    const long long off = win_base[sl][w] + (long long)y * a.width;
+    const CorrSeg& q = seg_s[win_seg[sl][w]];
+    const long long off = win_base[sl][w] + (long long)y * q.width;
 #pragma unroll
     for (int fi = 0; fi < 2 / TPL; ++fi) {
       const int f = TPL == 2 ? half : fi;
-      const float* src = reinterpret_cast<const float*>(f == 0 ? a.frame_a : a.frame_b) + off;
+      const float* src = reinterpret_cast<const float*>(f == 0 ? q.frame_a : q.frame_b) + off;
       const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS * 4);
 #pragma unroll
       for (int c = 0; c < CH; ++c) cp_async16(row + 16 * stg_chunk<CH>(t, c), src + 4 * c);
@@ -422,7 +467,8 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
             r[4 * c + 3] = ok ? q4.w : 0.f;
           }
         } else {
-          load_row(f == 0 ? a.frame_a : a.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * a.width, ok, r);
+          const CorrSeg& q = seg_s[win_seg[sl][w]];
+          load_row(f == 0 ? q.frame_a : q.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * q.width, ok, r);
         }
         float sum = 0.f;
 #pragma unroll
@@ -678,17 +724,19 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
                      at(pi_, pj + 1), isp, jsp);
       }
-      float* uo = reinterpret_cast<float*>(a.u);
-      float* vo = reinterpret_cast<float*>(a.v);
+      const CorrSeg& sq = seg_s[win_seg[sl][ww]];
+      const long long gl = win_loc[sl][ww];
+      float* uo = reinterpret_cast<float*>(sq.u);
+      float* vo = reinterpret_cast<float*>(sq.v);
       if (win_valid[sl][ww]) {
-        uo[g] = sub_rn(jsp, (float)HN);
-        vo[g] = sub_rn(isp, (float)HN);
+        uo[gl] = sub_rn(jsp, (float)HN);
+        vo[gl] = sub_rn(isp, (float)HN);
       } else {
-        uo[g] = NAN;
-        vo[g] = NAN;
+        uo[gl] = NAN;
+        vo[gl] = NAN;
       }
-      if (a.peak_i) a.peak_i[g] = pi_;
-      if (a.peak_j) a.peak_j[g] = pj;
+      if (sq.peak_i) sq.peak_i[gl] = pi_;
+      if (sq.peak_j) sq.peak_j[gl] = pj;
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -744,6 +792,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   __shared__ int sc_e[2][W];
   __shared__ long long win_base[2][W];
   __shared__ int win_valid[2][W];
+  __shared__ long long win_loc[2][W];  // window index within its segment
+  __shared__ int win_seg[2][W];
+  __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float pk_val[W][8];
   __shared__ int pk_idx[W][8];
 
@@ -801,11 +852,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   const uint32_t sbase = tc::smem_u32(sm);
   uint32_t phase = 0;
 
-  const int sp = a.spacing, nf = a.n;
-  const int n_wins = a.m * a.n;
-  const long long total = (long long)a.n_pairs * n_wins;
+  const int n_seg = load_segments(a, seg_s);
+  const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + W - 1) / W);
-  const long long frame_elems = (long long)a.height * a.width;
 
   // Every thread waits for the last commit itself; a wait that gives up sets
   // abort_s, which all threads read after the next barrier and leave the tile
@@ -829,21 +878,30 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   auto window_setup = [&](int tl, int sl) {
     const long long g = (long long)tl * W + tid;
     int ok = tl < n_tiles && g < total;
-    long long base = 0;
+    long long base = 0, loc = 0;
+    int sg = 0;
     if (ok) {
-      const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
-      if (a.win_mask) ok = a.win_mask[k] == 0;
-      base = pair * frame_elems + (long long)((k / nf) * sp + a.y_offset) * a.width + (k % nf) * sp + a.x_offset;
+      while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
+      const CorrSeg& q = seg_s[sg];
+      loc = g - q.win0;
+      const int nw = q.m * q.n;
+      const int pair = (int)(loc / nw), k = (int)(loc % nw);
+      if (q.win_mask) ok = q.win_mask[k] == 0;
+      base = pair * (long long)q.height * q.width + (long long)((k / q.n) * q.spacing + q.y_offset) * q.width +
+             (k % q.n) * q.spacing + q.x_offset;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
+    win_loc[sl][tid] = loc;
+    win_seg[sl][tid] = sg;
   };
   // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it stages itself.
   auto stage_async = [&](int sl) {
     const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
     if (!win_valid[sl][w]) return;
-    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? a.frame_a : a.frame_b) + win_base[sl][w] +
-                         (long long)y * a.width;
+    const CorrSeg& sq = seg_s[win_seg[sl][w]];
+    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? sq.frame_a : sq.frame_b) + win_base[sl][w] +
+                         (long long)y * sq.width;
     const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS);
 #pragma unroll
     for (int c = 0; c < 2; ++c) cp_async16(row + 16 * stg64_chunk(t, 2 * h + c), src + 16 * (2 * h + c));
@@ -878,7 +936,8 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
           for (int k = 0; k < 16; ++k) r[16 * c + k] = ok ? (float)((wds[k >> 2] >> (8 * (k & 3))) & 0xffu) : 0.f;
         }
       } else {
-        load_row(f == 0 ? a.frame_a : a.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * a.width + 32 * h,
+        const CorrSeg& sq = seg_s[win_seg[sl][w]];
+        load_row(f == 0 ? sq.frame_a : sq.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * sq.width + 32 * h,
                  ok, r);
       }
       float sum = 0.f;
@@ -1139,17 +1198,19 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
                      at(pi_, pj + 1), isp, jsp);
       }
-      float* uo = reinterpret_cast<float*>(a.u);
-      float* vo = reinterpret_cast<float*>(a.v);
+      const CorrSeg& sq = seg_s[win_seg[sl][ww]];
+      const long long gl = win_loc[sl][ww];
+      float* uo = reinterpret_cast<float*>(sq.u);
+      float* vo = reinterpret_cast<float*>(sq.v);
       if (win_valid[sl][ww]) {
-        uo[g] = sub_rn(jsp, (float)HN);
-        vo[g] = sub_rn(isp, (float)HN);
+        uo[gl] = sub_rn(jsp, (float)HN);
+        vo[gl] = sub_rn(isp, (float)HN);
       } else {
-        uo[g] = NAN;
-        vo[g] = NAN;
+        uo[gl] = NAN;
+        vo[gl] = NAN;
       }
-      if (a.peak_i) a.peak_i[g] = pi_;
-      if (a.peak_j) a.peak_j[g] = pj;
+      if (sq.peak_i) sq.peak_i[gl] = pi_;
+      if (sq.peak_j) sq.peak_j[gl] = pj;
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -1170,7 +1231,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
 
 template <bool ASYNC>
 static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
-  const long long total = (long long)a.n_pairs * a.m * a.n;
+  const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + Tc64::W - 1) / Tc64::W);
   static thread_local int configured_dev = -1;
   int dev = 0;
@@ -1193,20 +1254,30 @@ static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
 
 // Rows of 8-bit frames start on 16-byte boundaries (asynchronous staging of
 // the 64-px engine).
-static bool tc64_aligned(const CorrArgs& a) {
-  return a.pixel_type == PIV_PIXEL_U8 && ((uintptr_t)a.frame_a % 16) == 0 && ((uintptr_t)a.frame_b % 16) == 0 &&
-         a.width % 16 == 0 && a.x_offset % 16 == 0 && a.spacing % 16 == 0;
+static bool rows_aligned(const void* fa, const void* fb, int width, int x_offset, int spacing, int px) {
+  return ((uintptr_t)fa % 16) == 0 && ((uintptr_t)fb % 16) == 0 && width % px == 0 && x_offset % px == 0 &&
+         spacing % px == 0;
 }
+
+// Every geometry of the launch satisfies rows_aligned with px pixels per 16 bytes.
+static bool all_rows_aligned(const CorrArgs& a, int px) {
+  if (a.n_segs <= 0) return rows_aligned(a.frame_a, a.frame_b, a.width, a.x_offset, a.spacing, px);
+  for (int k = 0; k < a.n_segs; ++k) {
+    const CorrSeg& q = a.segs[k];
+    if (!rows_aligned(q.frame_a, q.frame_b, q.width, q.x_offset, q.spacing, px)) return false;
+  }
+  return true;
+}
+
+static bool tc64_aligned(const CorrArgs& a) { return a.pixel_type == PIV_PIXEL_U8 && all_rows_aligned(a, 16); }
 
 // Rows of float frames start on 16-byte boundaries (asynchronous staging of
 // the 16/32-px engine).
-static bool tc_aligned(const CorrArgs& a) {
-  return a.pixel_type == PIV_PIXEL_F32 && ((uintptr_t)a.frame_a % 16) == 0 && ((uintptr_t)a.frame_b % 16) == 0 &&
-         a.width % 4 == 0 && a.x_offset % 4 == 0 && a.spacing % 4 == 0;
-}
+static bool tc_aligned(const CorrArgs& a) { return a.pixel_type == PIV_PIXEL_F32 && all_rows_aligned(a, 4); }
 
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
   if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT) return false;
+  if (a.n_segs < 0 || a.n_segs > kMaxCorrSegs) return false;
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
          (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode == PIV_DFT_TENSOR));
 }
@@ -1282,7 +1353,7 @@ static int tc_config_cached(TcLaunch*& cfg) {
 template <int SS, bool ASYNC, bool SPLIT>
 static int launch_tc_t(const CorrArgs& a, int per_sm, cudaStream_t stream) {
   using L = TcLayout<SS, SPLIT>;
-  const long long total = (long long)a.n_pairs * a.m * a.n;
+  const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + L::W - 1) / L::W);
   TcLaunch* cfg = nullptr;
   PIV_TRY_TC((tc_config_cached<SS, ASYNC, SPLIT>(cfg)));
@@ -1335,7 +1406,7 @@ int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int varia
 int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream) {
   if (!correlate_tensor_supported(a, dft_mode))
     return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
-  const long long total = (long long)a.n_pairs * a.m * a.n;
+  const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   if (total == 0) return PIV_OK;
   if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");
   if (a.ss == 64) {

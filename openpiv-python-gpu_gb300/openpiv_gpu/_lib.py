@@ -75,6 +75,17 @@ _SIGNATURES = {
     "piv_plan_variant_name": (c_int, [c_void_p, c_int, c_int, ctypes.c_char_p, c_size_t]),
     "piv_plan_set_variant": (c_int, [c_void_p, c_int, c_int]),
     "piv_autotune_cache_clear": (None, []),
+    "piv_batch_create": (c_int, [POINTER(PivConfig), c_int, POINTER(c_void_p)]),
+    "piv_batch_destroy": (None, [c_void_p]),
+    "piv_batch_plan": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),
+    "piv_batch_run": (c_int, [c_void_p, POINTER(c_int), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
+                              POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), c_void_p]),
+    "piv_batch_graph_capture": (c_int, [c_void_p, POINTER(c_int), POINTER(c_void_p), POINTER(c_void_p),
+                                        POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
+                                        POINTER(c_int), c_void_p]),
+    "piv_batch_graph_launch": (c_int, [c_void_p, c_void_p]),
+    "piv_batch_status": (c_int, [c_void_p, POINTER(c_int), c_void_p]),
+    "piv_batch_set_schedule": (c_int, [c_void_p, c_int]),
     "piv_plan_graph_capture": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, POINTER(c_int), c_void_p]),
     "piv_plan_graph_launch": (c_int, [c_void_p, c_void_p]),

@@ -1,12 +1,16 @@
 """Batched form: one submission of many pairs of uneven frame sizes.
 
-Pairs are grouped by frame size. Each group runs the whole multi-pass
-pipeline for all of its pairs in one plan run (one launch per stage and pass
-over every window of the group's pairs), the groups run on their own CUDA
-streams so that they overlap on the device, and the submission (fork, the
-groups' runs, join) is captured once as a single CUDA graph and replayed.
-Results come back per pair, in submission order.
+Pairs are grouped by frame size; the groups run under one ``piv_batch``
+(``include/piv_gb300.h``): each group has its own plan and CUDA stream for its
+per-field stages (predictor, deformation, validation, replacement,
+smoothing), and every pass on a tensor engine runs ONE correlation launch over
+the windows of every pair of every size (a segment table of the sizes travels
+in the kernel parameters). The submission is captured once as a CUDA graph and
+replayed. Results come back per pair, in submission order, and equal the
+pair's single-pair result.
 """
+
+import ctypes
 
 import numpy as np
 
@@ -33,15 +37,11 @@ class _Group:
         self.v = torch.empty_like(self.u)
         self.val = torch.empty((B, m, n), dtype=torch.uint8, device=dev)
         self.out = torch.empty_like(self.val)
-        self.plan = self.proc._plan(_lib.PIXEL["u8"], B)
-        self.stream = torch.cuda.Stream()
-        self.done = torch.cuda.Event()
 
-    def launch(self, stream):
-        B = len(self.indices)
-        _lib.check(_lib.lib().piv_plan_run(self.plan, B, self.fa.data_ptr(), self.fb.data_ptr(), 0,
-                                           self.u.data_ptr(), self.v.data_ptr(), self.val.data_ptr(),
-                                           self.out.data_ptr(), 0, stream.cuda_stream))
+    def config(self):
+        """The group's piv_config (keeps its iteration array alive on self)."""
+        cfg, self._keep = self.proc._config(_lib.PIXEL["u8"], len(self.indices))
+        return cfg
 
 
 class PIVMixedBatch:
@@ -52,18 +52,40 @@ class PIVMixedBatch:
     (``min_search_size`` included). ``load(pairs)`` copies a submission's
     frames to the device, ``run()`` replays the captured graph, ``results()``
     returns [(u, v)] per pair as NumPy arrays in submission order.
+
+    ``schedule``: "joint" (one correlation launch per pass over every size),
+    "streams" (each size on its own stream throughout) or "auto" (``capture``
+    times both graphs on the loaded frames and keeps the faster one; the
+    choice is in ``self.schedule``).
     """
 
-    def __init__(self, shapes, settings, dft="tensor"):
+    def __init__(self, shapes, settings, dft="tensor", schedule="auto"):
+        if schedule not in ("auto", "joint", "streams"):
+            raise ValueError(f"schedule must be 'auto', 'joint' or 'streams', not {schedule!r}")
+        self.schedule = schedule
+        self.schedule_ms = {}
         torch = _torch()
         self.shapes = [tuple(s) for s in shapes]
         order = {}
         for k, s in enumerate(self.shapes):
             order.setdefault(s, []).append(k)
         self.groups = [_Group(s, idx, settings, dft) for s, idx in order.items()]
+        G = len(self.groups)
+        cfgs = (_lib.PivConfig * G)(*[g.config() for g in self.groups])
+        self.batch = ctypes.c_void_p()
+        _lib.check(_lib.lib().piv_batch_create(cfgs, G, ctypes.byref(self.batch)))
+        ptrs = lambda name: (ctypes.c_void_p * G)(*[getattr(g, name).data_ptr() for g in self.groups])
+        self._args = ((ctypes.c_int * G)(*[len(g.indices) for g in self.groups]), ptrs("fa"), ptrs("fb"),
+                      ptrs("u"), ptrs("v"), ptrs("val"), ptrs("out"))
         self.stream = torch.cuda.Stream()
-        self.fork = torch.cuda.Event()
-        self.graph = None
+        self.graph = False
+        self.kernel_nodes = None
+
+    def __del__(self):
+        try:
+            _lib.lib().piv_batch_destroy(self.batch)
+        except Exception:
+            pass
 
     @property
     def windows(self):
@@ -82,35 +104,53 @@ class PIVMixedBatch:
                 g.fb.copy_(torch.from_numpy(fb), non_blocking=False)
         self.stream.synchronize()
 
-    def _submit(self):
-        self.fork.record(self.stream)
-        for g in self.groups:
-            g.stream.wait_event(self.fork)
-            g.launch(g.stream)
-            g.done.record(g.stream)
-        for g in self.groups:
-            self.stream.wait_event(g.done)
+    def _capture(self, joint):
+        lib = _lib.lib()
+        _lib.check(lib.piv_batch_set_schedule(self.batch, int(joint)))
+        _lib.check(lib.piv_batch_run(self.batch, *self._args, self.stream.cuda_stream))
+        self.stream.synchronize()
+        nk = ctypes.c_int(0)
+        _lib.check(lib.piv_batch_graph_capture(self.batch, *self._args, ctypes.byref(nk), self.stream.cuda_stream))
+        self.kernel_nodes = nk.value
+        self.graph = True
+
+    def _time(self, reps=3):
+        torch = _torch()
+        self.run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(self.stream)
+        for _ in range(reps):
+            self.run()
+        e1.record(self.stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
 
     def capture(self):
-        """Runs once directly (plans allocate and configure their kernels), then
-        captures the submission as one CUDA graph."""
-        torch = _torch()
-        with torch.cuda.stream(self.stream):
-            self._submit()
-        self.stream.synchronize()
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, stream=self.stream):
-            self._submit()
-        torch.cuda.synchronize()
+        """Runs once directly (plans configure their kernels), then captures the
+        submission as one CUDA graph (with schedule "auto", both schedules are
+        captured and timed and the faster one is kept)."""
+        if self.schedule != "auto":
+            self._capture(self.schedule == "joint")
+            return
+        for name in ("streams", "joint"):
+            self._capture(name == "joint")
+            self.schedule_ms[name] = self._time()
+        best = min(self.schedule_ms, key=self.schedule_ms.get)
+        if best != "joint":
+            self._capture(False)
+        self.schedule = best
 
     def run(self):
-        torch = _torch()
-        if self.graph is None:
-            with torch.cuda.stream(self.stream):
-                self._submit()
+        lib = _lib.lib()
+        if self.graph:
+            _lib.check(lib.piv_batch_graph_launch(self.batch, self.stream.cuda_stream))
         else:
-            with torch.cuda.stream(self.stream):
-                self.graph.replay()
+            _lib.check(lib.piv_batch_run(self.batch, *self._args, self.stream.cuda_stream))
+
+    def status(self):
+        st = ctypes.c_int(0)
+        _lib.check(_lib.lib().piv_batch_status(self.batch, ctypes.byref(st), self.stream.cuda_stream))
+        return st.value
 
     def results(self):
         self.stream.synchronize()

@@ -435,13 +435,8 @@ class PIVGPU:
         return its
 
     # -- execution ------------------------------------------------------------
-    def _plan(self, pixel_type, n_pairs, slot=0):
-        key = (pixel_type, slot)
-        entry = self._plans.get(key)
-        if entry is not None and entry[1] >= n_pairs:
-            return entry[0]
-        if entry is not None:
-            _lib.lib().piv_plan_destroy(entry[0])
+    def _config(self, pixel_type, n_pairs):
+        """(piv_config, objects it points to) for this instance's settings."""
         arr = (_lib.PivIteration * len(self._iterations))(*self._iterations)
         cfg = _lib.PivConfig()
         cfg.height, cfg.width = self.frame_shape
@@ -458,6 +453,16 @@ class PIVGPU:
             mask_buf = np.ascontiguousarray(self.mask, dtype=np.uint8)
             cfg.mask = mask_buf.ctypes.data
         cfg.dft_mode = _lib.DFT[self.dft]
+        return cfg, (arr, mask_buf)
+
+    def _plan(self, pixel_type, n_pairs, slot=0):
+        key = (pixel_type, slot)
+        entry = self._plans.get(key)
+        if entry is not None and entry[1] >= n_pairs:
+            return entry[0]
+        if entry is not None:
+            _lib.lib().piv_plan_destroy(entry[0])
+        cfg, _keep = self._config(pixel_type, n_pairs)
         plan = ctypes.c_void_p()
         _lib.check(_lib.lib().piv_plan_create(ctypes.byref(cfg), ctypes.byref(plan)))
         self._plans[key] = (plan, int(n_pairs))

@@ -95,10 +95,20 @@ def test_pipelined_batches_equal_single_runs():
     assert proc.status() == 0 and ref.status() == 0
 
 
-def test_mixed_size_submission_equals_single_runs():
-    """PIVMixedBatch: pairs of three frame sizes in one submission, captured as
-    one CUDA graph over per-size plans on their own streams; every pair's result
-    equals processing it alone."""
+MIXED_SHAPES = [(128, 160), (96, 96), (128, 160), (160, 224), (96, 96), (128, 160)]
+# Ten sizes: more than the eight segments of one launch, so passes on a tensor
+# engine take two joint launches.
+MANY_SHAPES = [(96 + 16 * (k % 5), 96 + 32 * (k // 5)) for k in range(10)] + [(96, 96)]
+
+
+@pytest.mark.parametrize("dft,shapes,schedule", [
+    ("tensor", MIXED_SHAPES, "joint"), ("tensor", MIXED_SHAPES, "streams"), ("tensor_split", MIXED_SHAPES, "joint"),
+    ("fft", MIXED_SHAPES, "joint"), ("tensor", MANY_SHAPES, "joint"), ("tensor", MIXED_SHAPES, "auto")])
+def test_mixed_size_submission_equals_single_runs(dft, shapes, schedule):
+    """PIVMixedBatch: pairs of several frame sizes in one submission (one
+    correlation launch per pass over every size on the tensor engines),
+    captured as one CUDA graph; every pair's result equals processing it
+    alone."""
     import torch
 
     from openpiv_gpu import _build, synthetic
@@ -107,17 +117,18 @@ def test_mixed_size_submission_equals_single_runs():
 
     _build.build()
     torch.cuda.set_device(0)
-    shapes = [(128, 160), (96, 96), (128, 160), (160, 224), (96, 96), (128, 160)]
     pairs = [synthetic.config_case(4, k, shape=sh)[:2] for k, sh in enumerate(shapes)]
     settings = dict(synthetic.CONFIGS[4]["piv"])
-    batch = PIVMixedBatch(shapes, settings, dft="tensor")
+    batch = PIVMixedBatch(shapes, settings, dft=dft, schedule=schedule)
     batch.load(pairs)
     batch.capture()
     batch.run()
     got = batch.results()
+    assert batch.status() == 0
     kw = dict(settings)
     mss = kw.pop("min_search_size")
     for (a, b), (u, v) in zip(pairs, got):
-        ue, ve = PIVGPU(a.shape, mss, dft="tensor", **kw).run_batch(a[None], b[None], host_out=True)
+        ue, ve = PIVGPU(a.shape, mss, dft=dft, **kw).run_batch(a[None], b[None], host_out=True)
         np.testing.assert_array_equal(u, ue[0])
         np.testing.assert_array_equal(v, ve[0])
+    print(f"{dft}, {len(set(shapes))} sizes, {batch.schedule} {batch.schedule_ms}: {batch.kernel_nodes} kernel nodes")
