@@ -509,7 +509,8 @@ def run_gpu(args):
                        "default_ms": [t["ms"][0] for t in proc.tuning()],
                        "tuned_ms": [None if t["ms"][t["variant"]] is None else t["ms"][t["variant"]]
                                     for t in proc.tuning()],
-                       "plain": [t["name"] for t in proc_plain.tuning()] if proc_plain is not None else None},
+                       "plain": [t["name"] for t in proc_plain.tuning()] if proc_plain is not None else None,
+                       "variants_ms": [dict(zip(t["variants"], t["ms"])) for t in proc.tuning()]},
             "e2e": e2e, "gpu_launches": kernels * args.steps, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu_baseline, "clocks": clocks, "accuracy": accuracy,
             "device_status": device_status,

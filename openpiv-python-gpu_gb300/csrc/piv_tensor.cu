@@ -255,10 +255,6 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
   return q;
 }
 
-// ASYNC: float32 frames whose window rows start on 16-byte boundaries. The
-// next tile's rows are then copied into shared memory with cp.async while the
-// current tile runs through its four products; otherwise each tile loads its
-// rows from global memory when it starts.
 // The launch's segment table in shared memory (one segment built from the
 // single geometry of `a` when a.n_segs == 0); returns the segment count. All
 // threads call it; it ends with a barrier.
@@ -294,6 +290,10 @@ PIV_D int load_segments(const CorrArgs& a, CorrSeg* seg_s) {
   return n;
 }
 
+// ASYNC: float32 frames whose window rows start on 16-byte boundaries. The
+// next tile's rows are then copied into shared memory with cp.async while the
+// current tile runs through its four products; otherwise each tile loads its
+// rows from global memory when it starts.
 template <int SS, bool ASYNC, bool SPLIT>
 __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::LB_BLOCKS)
     k_corr_tc(CorrArgs a, int* status) {
