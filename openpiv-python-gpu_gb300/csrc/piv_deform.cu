@@ -327,6 +327,112 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap
   }
 }
 
+// Cubic B-spline weights with the partition of the taps shared: u = 1 - t.
+PIV_D void bspline3_weights_fast(float t, float& w0, float& w1, float& w2, float& w3) {
+  const float t2 = t * t, t3 = t2 * t, u = 1.0f - t, u2 = u * u, u3 = u2 * u;
+  w0 = u3 * (1.0f / 6.0f);
+  w1 = fmaf(0.5f, t3, (2.0f / 3.0f) - t2);
+  w2 = fmaf(0.5f, u3, (2.0f / 3.0f) - u2);
+  w3 = t3 * (1.0f / 6.0f);
+}
+
+// sample_cubic with 32-bit indexing of one frame's coefficients (H W < 2^31).
+PIV_D float sample_cubic32(const float* __restrict__ coef, int W, int H, float xi, float yi) {
+  xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
+  yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
+  const float fx = floorf(xi), fy = floorf(yi);
+  const int x0 = (int)fx - 1, y0 = (int)fy - 1;
+  if ((unsigned)x0 > (unsigned)(W - 4) || (unsigned)y0 > (unsigned)(H - 4))
+    return sample_cubic_edge(coef, W, H, xi, yi);
+  float wx0, wx1, wx2, wx3, wy0, wy1, wy2, wy3;
+  bspline3_weights_fast(xi - fx, wx0, wx1, wx2, wx3);
+  bspline3_weights_fast(yi - fy, wy0, wy1, wy2, wy3);
+  const float* r0 = coef + (y0 * W + x0);
+  const float* r1 = r0 + W;
+  const float* r2 = r1 + W;
+  const float* r3 = r2 + W;
+  float s0 = wx0 * __ldg(r0), s1 = wx0 * __ldg(r1), s2 = wx0 * __ldg(r2), s3 = wx0 * __ldg(r3);
+  s0 = fmaf(wx1, __ldg(r0 + 1), s0); s1 = fmaf(wx1, __ldg(r1 + 1), s1);
+  s2 = fmaf(wx1, __ldg(r2 + 1), s2); s3 = fmaf(wx1, __ldg(r3 + 1), s3);
+  s0 = fmaf(wx2, __ldg(r0 + 2), s0); s1 = fmaf(wx2, __ldg(r1 + 2), s1);
+  s2 = fmaf(wx2, __ldg(r2 + 2), s2); s3 = fmaf(wx2, __ldg(r3 + 2), s3);
+  s0 = fmaf(wx3, __ldg(r0 + 3), s0); s1 = fmaf(wx3, __ldg(r1 + 3), s1);
+  s2 = fmaf(wx3, __ldg(r2 + 3), s2); s3 = fmaf(wx3, __ldg(r3 + 3), s3);
+  return fmaf(wy3, s3, fmaf(wy2, s2, fmaf(wy1, s1, wy0 * s0)));
+}
+
+// k_deform for the common case: float32 fields, cubic B-spline sampling of
+// both frames (0 < deforming_par < 1). The row weights of the block's four
+// rows are computed once per CTA; pixel offsets are 32-bit.
+__global__ void __launch_bounds__(kDeformThreads) k_deform_cubic(DeformArgs a, AxisMap ax, AxisMap ay, float dta,
+                                                                 float dtb) {
+  __shared__ float su[kDeformMaxGridRows][kDeformMaxCols], sv[kDeformMaxGridRows][kDeformMaxCols];
+  __shared__ int s_klo, s_khi;
+  __shared__ int s_y0[kDeformRows], s_y1[kDeformRows];
+  __shared__ float s_ty[kDeformRows];
+  const piv_geometry& g = a.geom;
+  const int H = g.height, W = g.width;
+  const int j0 = blockIdx.x * kDeformThreads;
+  const int j = j0 + threadIdx.x;
+  const int i0 = blockIdx.y * kDeformRows, pair = blockIdx.z;
+  const int i_last = min(i0 + kDeformRows, H) - 1;
+  const int r_lo = axis_weight(i0, ay).i;
+  const int r_hi = min(axis_weight(i_last, ay).i + 1, g.m - 1);
+  const AxisWeight wx = axis_weight(min(j, W - 1), ax);
+  if (threadIdx.x == 0) s_klo = axis_weight(j0, ax).i;
+  if (threadIdx.x == kDeformThreads - 1 || j == W - 1) s_khi = min(wx.i + 1, g.n - 1);
+  if (threadIdx.x < kDeformRows) {
+    const AxisWeight wy = axis_weight(min(i0 + (int)threadIdx.x, H - 1), ay);
+    s_y0[threadIdx.x] = wy.i - r_lo;
+    s_y1[threadIdx.x] = (g.m < 2 ? wy.i : wy.i + 1) - r_lo;
+    s_ty[threadIdx.x] = wy.t;
+  }
+  __syncthreads();
+  const int k_lo = s_klo, k_hi = s_khi;
+  const int nc = k_hi - k_lo + 1, nr = r_hi - r_lo + 1;
+  const long long fo = (long long)pair * g.m * g.n;
+  for (int e = threadIdx.x; e < nr * nc; e += kDeformThreads) {
+    const int r = e / nc, c = e % nc;
+    const long long q = fo + (long long)(r_lo + r) * g.n + k_lo + c;
+    su[r][c] = (float)__ldg(a.up + q);
+    sv[r][c] = (float)__ldg(a.vp + q);
+  }
+  __syncthreads();
+  if (j >= W) return;
+  const long long base = (long long)pair * H * W;
+  const float* ca = a.coef_a + base;
+  const float* cb = a.coef_b + base;
+  float* out_a = reinterpret_cast<float*>(a.out_a) + base;
+  float* out_b = reinterpret_cast<float*>(a.out_b) + base;
+  const uint8_t* mask = a.frame_mask;
+  const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
+  const float x = (float)j;
+#pragma unroll 1
+  for (int rr = 0; rr < kDeformRows; ++rr) {
+    const int i = i0 + rr;
+    if (i > i_last) break;
+    const int p = i * W + j;
+    if (mask && mask[p]) {
+      out_a[p] = 0.f;
+      out_b[p] = 0.f;
+      continue;
+    }
+    const int y0r = s_y0[rr], y1r = s_y1[rr];
+    const float ty = s_ty[rr];
+    const float u0 = fmaf(ty, su[y1r][c0] - su[y0r][c0], su[y0r][c0]);
+    const float u1 = fmaf(ty, su[y1r][c1] - su[y0r][c1], su[y0r][c1]);
+    const float v0 = fmaf(ty, sv[y1r][c0] - sv[y0r][c0], sv[y0r][c0]);
+    const float v1 = fmaf(ty, sv[y1r][c1] - sv[y0r][c1], sv[y0r][c1]);
+    const float up = fmaf(wx.t, u1 - u0, u0);
+    const float vp = fmaf(wx.t, v1 - v0, v0);
+    const float y = (float)i;
+    const float ra = sample_cubic32(ca, W, H, add_rn(x, mul_rn(up, dta)), add_rn(y, mul_rn(vp, dta)));
+    const float rb = sample_cubic32(cb, W, H, add_rn(x, mul_rn(up, dtb)), add_rn(y, mul_rn(vp, dtb)));
+    out_a[p] = ra;
+    out_b[p] = rb;
+  }
+}
+
 int deform(const DeformArgs& a, cudaStream_t stream) {
   const long long total = (long long)a.geom.height * a.geom.width * a.n_pairs;
   if (total == 0) return PIV_OK;
@@ -348,6 +454,8 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   const AxisMap ay = axis_map(a.geom.search_size, a.geom.y_offset, a.geom.spacing, a.geom.m);
   if (a.dtype == PIV_DTYPE_F64)
     k_deform<double><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, dta, dtb, do_a, do_b);
+  else if (a.order == 3 && do_a && do_b)
+    k_deform_cubic<<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb);
   else
     k_deform<float><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb, do_a, do_b);
   cudaError_t e = cudaGetLastError();
