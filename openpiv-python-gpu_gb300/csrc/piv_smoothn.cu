@@ -28,6 +28,8 @@ struct SmoothScratch {
   double* cn;    // [n][n]
   double* lam2;  // [mn]
   double* p;     // [pairs]
+  float* f2f;    // [pairs][mn] f2 in float32 (the GCV search's fast score)
+  float* lam2f;  // [mn] lam2 in float32
 };
 
 static size_t align_up(size_t v) { return (v + 255) / 256 * 256; }
@@ -40,7 +42,8 @@ size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
   const size_t mn = (size_t)m * n;
   const size_t shared = align_up((size_t)m * m * 8) + align_up((size_t)n * n * 8) + align_up(mn * 8) +
                         align_up((size_t)n_pairs * 8);
-  const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared;
+  const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared +
+                       align_up(mn * n_pairs * 4) + align_up(mn * 4);
   const size_t weighted = shared + weighted_pair_bytes(mn) * n_pairs;
   return plain > weighted ? plain : weighted;
 }
@@ -55,7 +58,9 @@ static SmoothScratch carve(void* base, int m, int n, int n_pairs) {
   s.cm = (double*)p; p += align_up((size_t)m * m * 8);
   s.cn = (double*)p; p += align_up((size_t)n * n * 8);
   s.lam2 = (double*)p; p += align_up(mn * 8);
-  s.p = (double*)p;
+  s.p = (double*)p; p += align_up((size_t)n_pairs * 8);
+  s.f2f = (float*)p; p += align_up(mn * n_pairs * 4);
+  s.lam2f = (float*)p;
   return s;
 }
 
@@ -69,12 +74,13 @@ __global__ void k_dct_matrix(int len, double* c) {
 }
 
 // lambda^2 with lambda = 2 (2 - (cos(pi i/m) + cos(pi j/n))).
-__global__ void k_lambda2(int m, int n, double* lam2) {
+__global__ void k_lambda2(int m, int n, double* lam2, float* lam2f = nullptr) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m * n) return;
   const int i = t / n, j = t % n;
   const double l = 2.0 * (2.0 - (cos(M_PI * i / m) + cos(M_PI * j / n)));
   lam2[t] = l * l;
+  if (lam2f) lam2f[t] = (float)(l * l);
 }
 
 // out[b][i][l] = sum_j in[b][i][j] * c[l][j]       (transform along rows, mode 0)
@@ -202,12 +208,14 @@ static void dct_pass(int m, int n, int batch, bool inverse, int cols, const doub
   else k_dct_lines<false><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, c, in, out);
 }
 
-__global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, double* __restrict__ f2) {
+__global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, double* __restrict__ f2,
+                     float* __restrict__ f2f) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= mn * n_pairs) return;
   const long long pair = t / mn, e = t % mn;
   const double a = fd[(2 * pair) * mn + e], b = fd[(2 * pair + 1) * mn + e];
   f2[t] = a * a + b * b;
+  f2f[t] = (float)(a * a + b * b);
 }
 
 static constexpr int kGcvThreads = 512;
@@ -226,6 +234,8 @@ PIV_D double rcp_fast(double d) {
 struct GcvEval {
   const double* f2;
   const double* lam2;
+  const float* f2f;
+  const float* lam2f;
   long long mn;
   double n_finite;
   int n_fields;
@@ -263,16 +273,23 @@ PIV_D double gcv_grad(const GcvEval& g, double p, double f0, double pmax, double
   return (f0 - gcv_score(g, p - h, red)) / h;
 }
 
-// GCV score in float32 arithmetic (float64 block reduction): enough to rank the
-// ten scan points, whose scores differ by far more than its error.
-PIV_D double gcv_score_f32(const GcvEval& g, double p, double* red) {
-  const float s = (float)pow(10.0, p);
+// GCV score with float32 terms and float64 sums: 1 - gamma = s l / (1 + s l)
+// is formed directly (no cancellation), so every term is a product of
+// positive factors within a few float32 ulps; the rounding errors of the
+// terms are independent, and their sum over the field stays near 1e-9 of the
+// score. s = 10^p is formed once per CTA in float64. Used to rank the scan
+// points and for the bounded local search; the gradient test, which divides
+// score differences by 1e-8, uses the float64 score.
+PIV_D double gcv_score_fast(const GcvEval& g, double p, double* red) {
+  if (threadIdx.x == 0) red[64] = pow(10.0, p);
+  __syncthreads();
+  const float s = (float)red[64];
   float rss = 0.f, tr = 0.f;
   for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
-    const float gm = __frcp_rn(fmaf(s, (float)g.lam2[e], 1.0f));
-    const float d = gm - 1.0f;
-    rss = fmaf((float)g.f2[e] * d, d, rss);
-    tr += gm;
+    const float sl = s * g.lam2f[e];
+    const float d = sl * __frcp_rn(1.0f + sl);  // 1 - gamma
+    rss = fmaf(g.f2f[e] * d, d, rss);
+    tr += d;
   }
   double drss = rss, dtr = tr;
   for (int o = 16; o > 0; o >>= 1) {
@@ -285,23 +302,24 @@ PIV_D double gcv_score_f32(const GcvEval& g, double p, double* red) {
   __syncthreads();
   double trss = 0.0, ttr = 0.0;
   for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
-  const double q = 1.0 - ttr / (double)g.mn;
+  const double q = ttr / (double)g.mn;
   return trss / g.n_finite / (q * q) / g.n_fields;
 }
 
 __global__ void __launch_bounds__(kGcvThreads)
-k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2, double pmin,
-      double pmax, double* __restrict__ p_out) {
-  __shared__ double red[64];
+k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2,
+      const float* __restrict__ f2f, const float* __restrict__ lam2f, double pmin, double pmax,
+      double* __restrict__ p_out) {
+  __shared__ double red[65];
   const int pair = blockIdx.x;
   const long long mn = (long long)m * n;
-  GcvEval g{f2 + pair * mn, lam2, mn, (double)mn, 2};
-  // 10-point scan (gpu_smoothn.py:182-188), ranked in float32; the best point
-  // is scored again in float64 for the gradient test and the local search.
+  GcvEval g{f2 + pair * mn, lam2, f2f + pair * mn, lam2f, mn, (double)mn, 2};
+  // 10-point scan (gpu_smoothn.py:182-188), ranked with the fast score; the
+  // best point is scored in float64 for the gradient test.
   double best_p = pmin, best_f = INFINITY;
   for (int k = 0; k < 10; ++k) {
     const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
-    const double fk = gcv_score_f32(g, pk, red);
+    const double fk = gcv_score_fast(g, pk, red);
     if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
   }
   double p = best_p;
@@ -313,10 +331,11 @@ k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __
     const double step = (pmax - pmin) / 9.0;
     double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
     const double cg = 0.3819660112501051;
-    double x = p, w = p, v = p, fx = f0, fw = f0, fv = f0, d = 0.0, e = 0.0;
+    const double fs = gcv_score_fast(g, p, red);
+    double x = p, w = p, v = p, fx = fs, fw = fs, fv = fs, d = 0.0, e = 0.0;
     for (int it = 0; it < 200; ++it) {
       const double xm = 0.5 * (a + b);
-      const double tol1 = 1e-11 * fabs(x) + 1e-13, tol2 = 2.0 * tol1;
+      const double tol1 = 1e-8 * fabs(x) + 1e-10, tol2 = 2.0 * tol1;
       if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
       bool golden = true;
       if (fabs(e) > tol1) {
@@ -338,7 +357,7 @@ k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __
         d = cg * e;
       }
       const double u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
-      const double fu = gcv_score(g, u, red);
+      const double fu = gcv_score_fast(g, u, red);
       if (fu <= fx) {
         if (u >= x) a = x; else b = x;
         v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
@@ -704,7 +723,7 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
   const int bs = 256;
   k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, sc.cm);
   k_dct_matrix<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n, sc.cn);
-  k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, sc.lam2);
+  k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, sc.lam2, sc.lam2f);
   // Gather u and v as [pair][field][mn] into tmp.
   for (int f = 0; f < 2; ++f) {
     cudaMemcpy2DAsync(sc.tmp + f * mn, 2 * mn * 8, f == 0 ? u_in : v_in, mn * 8, mn * 8, n_pairs,
@@ -726,8 +745,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
     const double a_max = pow(h_max, 2.0 / rank), a_min = pow(h_min, 2.0 / rank);
     const double pmin = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_max)) / 4.0 / a_max, 2.0) - 1.0) / 16.0);
     const double pmax = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_min)) / 4.0 / a_min, 2.0) - 1.0) / 16.0);
-    k_f2<<<(unsigned)((mn * n_pairs + bs - 1) / bs), bs, 0, stream>>>(mn, n_pairs, sc.tmp, sc.f2);
-    k_gcv<<<n_pairs, kGcvThreads, 0, stream>>>(m, n, n_pairs, sc.f2, sc.lam2, pmin, pmax, sc.p);
+    k_f2<<<(unsigned)((mn * n_pairs + bs - 1) / bs), bs, 0, stream>>>(mn, n_pairs, sc.tmp, sc.f2, sc.f2f);
+    k_gcv<<<n_pairs, kGcvThreads, 0, stream>>>(m, n, n_pairs, sc.f2, sc.lam2, sc.f2f, sc.lam2f, pmin, pmax, sc.p);
     pvec = sc.p;
     rc = check("k_gcv");
     if (rc) return rc;
