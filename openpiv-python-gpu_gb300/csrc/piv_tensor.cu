@@ -206,6 +206,10 @@ PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uin
 // 2^e for |e| <= 126.
 PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
 
+// floor(log2(x)) for finite x > 0 from the exponent field: ilogbf for normal x;
+// subnormal x gives -127 (the callers clamp the scale exponent anyway).
+PIV_D int exp2_floor(float x) { return ((__float_as_int(x) >> 23) & 0xff) - 127; }
+
 // CNT consecutive pixels of one window row as float; the pixel type is
 // resolved once, outside the unrolled loads, so that all of them are in flight
 // together.
@@ -407,11 +411,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
       const CorrSeg& q = seg_s[sg];
       loc = g - q.win0;
-      const int nw = q.m * q.n;
-      const int pair = (int)(loc / nw), k = (int)(loc % nw);
+      // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
+      const int li = (int)loc, nw = q.m * q.n;
+      const int pair = li / nw, k = li - pair * nw;
+      const int wr = k / q.n, wc = k - wr * q.n;
       if (q.win_mask) ok = q.win_mask[k] == 0;
-      base = pair * (long long)q.height * q.width + (long long)((k / q.n) * q.spacing + q.y_offset) * q.width +
-             (k % q.n) * q.spacing + q.x_offset;
+      base = pair * (long long)q.height * q.width + (long long)(wr * q.spacing + q.y_offset) * q.width +
+             wc * q.spacing + q.x_offset;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 #pragma unroll
         for (int o = 1; o < SS; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
         int e = 0;
-        if (l > 0.f) e = min(120, max(-120, L::SCALE_BITS - ilogbf(l)));
+        if (l > 0.f) e = min(120, max(-120, L::SCALE_BITS - exp2_floor(l)));
         const float s = pow2i(e);
 #pragma unroll
         for (int x = 0; x < SS; ++x) r[x] *= s;
@@ -718,8 +724,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = -sc_e[0][ww] - sc_e[1][ww];
         // Shifted (i, j) -> stored row slot i - pi + 1, natural column j ^ N/2.
+        // x 2^ue as two exact power-of-two products (|ue| <= 240; each factor is a normal float).
+        const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
         auto at = [&](int i, int j) -> float {
-          return (i == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (i - pi_ + 1)) * N + (j ^ HN)], ue);
+          return (i == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (i - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
         };
         subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
                      at(pi_, pj + 1), isp, jsp);
@@ -884,11 +892,13 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
       const CorrSeg& q = seg_s[sg];
       loc = g - q.win0;
-      const int nw = q.m * q.n;
-      const int pair = (int)(loc / nw), k = (int)(loc % nw);
+      // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
+      const int li = (int)loc, nw = q.m * q.n;
+      const int pair = li / nw, k = li - pair * nw;
+      const int wr = k / q.n, wc = k - wr * q.n;
       if (q.win_mask) ok = q.win_mask[k] == 0;
-      base = pair * (long long)q.height * q.width + (long long)((k / q.n) * q.spacing + q.y_offset) * q.width +
-             (k % q.n) * q.spacing + q.x_offset;
+      base = pair * (long long)q.height * q.width + (long long)(wr * q.spacing + q.y_offset) * q.width +
+             wc * q.spacing + q.x_offset;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
@@ -961,7 +971,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       __syncthreads();
       const float l1 = red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3];
       int e = 0;
-      if (l1 > 0.f) e = min(120, max(-120, 6 - ilogbf(l1)));
+      if (l1 > 0.f) e = min(120, max(-120, 6 - exp2_floor(l1)));
       const float s = pow2i(e);
 #pragma unroll
       for (int x = 0; x < 32; ++x) r[x] *= s;
@@ -1192,8 +1202,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = -sc_e[0][ww] - sc_e[1][ww];
+        const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
         auto at = [&](int ii, int j) -> float {
-          return (ii == 0 || j == 0) ? 0.f : ldexpf(nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)], ue);
+          return (ii == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
         };
         subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
                      at(pi_, pj + 1), isp, jsp);
@@ -1278,6 +1289,9 @@ static bool tc_aligned(const CorrArgs& a) { return a.pixel_type == PIV_PIXEL_F32
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
   if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT) return false;
   if (a.n_segs < 0 || a.n_segs > kMaxCorrSegs) return false;
+  if (a.n_segs == 0 && (long long)a.n_pairs * a.m * a.n >= (1LL << 31)) return false;
+  for (int k = 0; k < a.n_segs; ++k)
+    if ((long long)a.segs[k].n_pairs * a.segs[k].m * a.segs[k].n >= (1LL << 31)) return false;
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
          (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode == PIV_DFT_TENSOR));
 }
