@@ -430,6 +430,34 @@ PIV_D double2 block_sum2(double a, double b, double* red) {
   return make_double2(ta, tb);
 }
 
+// The first nwa warps of the block: a named barrier (id 1) among them, and
+// sums of two doubles over them (every thread of the group gets both). With
+// one warp the shuffle tree alone suffices. Float64 throughput on this GPU is
+// a small fraction of float32, so work that only the warps holding data need
+// is kept off the others.
+PIV_D void group_bar(int nwa) {
+  if (nwa == 1) __syncwarp();
+  else asm volatile("bar.sync 1, %0;" ::"r"(nwa * 32) : "memory");
+}
+
+PIV_D double2 group_sum2(double a, double b, double* red, int nwa) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(~0u, a, o);
+    b += __shfl_xor_sync(~0u, b, o);
+  }
+  if (nwa == 1) return make_double2(a, b);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { red[w] = a; red[32 + w] = b; }
+  group_bar(nwa);
+  double ta = l < nwa ? red[l] : 0.0, tb = l < nwa ? red[32 + l] : 0.0;
+  for (int o = 16; o > 0; o >>= 1) {
+    ta += __shfl_xor_sync(~0u, ta, o);
+    tb += __shfl_xor_sync(~0u, tb, o);
+  }
+  group_bar(nwa);  // red is rewritten by the next call
+  return make_double2(ta, tb);
+}
+
 PIV_D int block_count(int v, int* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -441,39 +469,40 @@ PIV_D int block_count(int v, int* red) {
   return t;
 }
 
-// Stable compaction of the flagged positions into list (ascending), returns count.
+// Stable compaction of the flagged positions into list (ascending), returns
+// count; rank[p] = position in list, or -1. Each thread takes a contiguous
+// range of the field, so one block-wide scan of the per-thread counts places
+// every range (three barriers in all, whatever the field size).
 PIV_D int block_compact(const uint8_t* flags, int mn, int* list, int* rank, int* red) {
-  __shared__ int base_s;
-  if (threadIdx.x == 0) base_s = 0;
-  __syncthreads();
-  for (int start = 0; start < mn; start += blockDim.x) {
-    const int p = start + threadIdx.x;
-    const int f = (p < mn && flags[p]) ? 1 : 0;
-    // exclusive scan over the block
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int x = f;
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(~0u, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) red[w] = x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      for (int k = 0; k < nw; ++k) { int t = red[k]; red[k] = acc; acc += t; }
-      red[nw] = acc;
-    }
-    __syncthreads();
-    const int pos = base_s + red[w] + x - f;
-    if (p < mn) {
-      if (f) { list[pos] = p; rank[p] = pos; }
-      else rank[p] = -1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) base_s += red[nw];
-    __syncthreads();
+  const int nt = blockDim.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+  const int per = (mn + nt - 1) / nt, p0 = tid * per, p1 = min(mn, p0 + per);
+  int c = 0;
+  for (int p = p0; p < p1; ++p) c += flags[p] ? 1 : 0;
+  int x = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(~0u, x, o);
+    if (lane >= o) x += y;
   }
-  return base_s;
+  if (lane == 31) red[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < nw ? red[lane] : 0, ts = t;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(~0u, ts, o);
+      if (lane >= o) ts += y;
+    }
+    if (lane < nw) red[lane] = ts - t;  // exclusive prefix of the warps
+    if (lane == 31) red[nw] = ts;       // total (nw <= 32)
+  }
+  __syncthreads();
+  int pos = red[w] + x - c;
+  for (int p = p0; p < p1; ++p) {
+    if (flags[p]) { list[pos] = p; rank[p] = pos; ++pos; }
+    else rank[p] = -1;
+  }
+  const int total = red[nw];
+  __syncthreads();  // red is reused by the caller
+  return total;
 }
 
 // Coefficient magnitude 1/n_r of the spring link (gpu_validation.py:365-371),
@@ -533,89 +562,96 @@ __global__ void __launch_bounds__(kRepThreads) k_replace(RepArgs a, int* status)
     if (nv == 0) break;
     // 1. Replacement values from the current fields.
     if (a.method == PIV_REPLACE_SPRING && nv <= kCgSmall) {
-      // Conjugate gradients on (D - Adj) x = D rhs for both fields, the
-      // vectors of outlier r = tid + k nt in registers, p in shared memory.
-      FieldView fu{u, m, n, val, 0.0}, fv{v, m, n, val, 0.0};
-      double xu[kCgPer], xv[kCgPer], ru[kCgPer], rv[kCgPer], dd[kCgPer];
-      int nb[kCgPer][4];
-      double rr_u = 0, rr_v = 0;
-#pragma unroll
-      for (int k = 0; k < kCgPer; ++k) {
-        const int r = tid + k * nt;
-        xu[k] = xv[k] = ru[k] = rv[k] = dd[k] = 0;
-        nb[k][0] = nb[k][1] = nb[k][2] = nb[k][3] = -1;
-        if (r < nv) {
-          const int p = sc.list[r], i = p / n, j = p % n;
-          dd[k] = 1.0 / spring_coef(i, j, m, n, s, a.dtype);
-          ru[k] = dd[k] * (double)spring_rhs<T>(fu, i, j, s);
-          rv[k] = dd[k] * (double)spring_rhs<T>(fv, i, j, s);
-          const int oi[4] = {-s, 0, 0, s}, oj[4] = {0, -s, s, 0};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int ii = i + oi[e], jj = j + oj[e];
-            nb[k][e] = (ii < 0 || ii >= m || jj < 0 || jj >= n) ? -1 : sc.rank[ii * n + jj];
-          }
-          cg_pu[r] = ru[k];
-          cg_pv[r] = rv[k];
-          rr_u += ru[k] * ru[k];
-          rr_v += rv[k] * rv[k];
-        }
-      }
-      const double2 rr = block_sum2(rr_u, rr_v, red_d);  // also publishes cg_pu / cg_pv
-      rr_u = rr.x;
-      rr_v = rr.y;
-      const double tol_u = rr_u * 1e-28, tol_v = rr_v * 1e-28;
-      bool done_u = rr_u <= tol_u || rr_u == 0, done_v = rr_v <= tol_v || rr_v == 0;
-      int iter = 0;
-      for (; iter < kCgMaxIters && !(done_u && done_v); ++iter) {
-        double qu[kCgPer], qv[kCgPer], pq_u = 0, pq_v = 0;
+      // Conjugate gradients on (D - Adj) x = D rhs for both fields, run by the
+      // nwa warps that hold outliers (outlier r = tid + k nt in registers, the
+      // search direction p in shared memory); the other warps wait at the
+      // block barrier below.
+      const int nwa = min(nt >> 5, (nv + 31) >> 5);
+      if ((tid >> 5) < nwa) {
+        FieldView fu{u, m, n, val, 0.0}, fv{v, m, n, val, 0.0};
+        double xu[kCgPer], xv[kCgPer], ru[kCgPer], rv[kCgPer], dd[kCgPer];
+        int nb[kCgPer][4];
+        double rr_u = 0, rr_v = 0;
 #pragma unroll
         for (int k = 0; k < kCgPer; ++k) {
           const int r = tid + k * nt;
-          qu[k] = qv[k] = 0;
+          xu[k] = xv[k] = ru[k] = rv[k] = dd[k] = 0;
+          nb[k][0] = nb[k][1] = nb[k][2] = nb[k][3] = -1;
           if (r < nv) {
-            double au = dd[k] * cg_pu[r], av = dd[k] * cg_pv[r];
+            const int p = sc.list[r], i = p / n, j = p % n;
+            dd[k] = 1.0 / spring_coef(i, j, m, n, s, a.dtype);
+            ru[k] = dd[k] * (double)spring_rhs<T>(fu, i, j, s);
+            rv[k] = dd[k] * (double)spring_rhs<T>(fv, i, j, s);
+            const int oi[4] = {-s, 0, 0, s}, oj[4] = {0, -s, s, 0};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const int q = nb[k][e];
-              if (q >= 0) { au -= cg_pu[q]; av -= cg_pv[q]; }
+              const int ii = i + oi[e], jj = j + oj[e];
+              nb[k][e] = (ii < 0 || ii >= m || jj < 0 || jj >= n) ? -1 : sc.rank[ii * n + jj];
             }
-            qu[k] = au; qv[k] = av;
-            pq_u += cg_pu[r] * au; pq_v += cg_pv[r] * av;
+            cg_pu[r] = ru[k];
+            cg_pv[r] = rv[k];
+            rr_u += ru[k] * ru[k];
+            rr_v += rv[k] * rv[k];
           }
         }
-        const double2 pq = block_sum2(pq_u, pq_v, red_d);
-        const double al_u = done_u ? 0.0 : rr_u / pq.x, al_v = done_v ? 0.0 : rr_v / pq.y;
-        double nr_u = 0, nr_v = 0;
+        group_bar(nwa);  // publishes cg_pu / cg_pv
+        const double2 rr = group_sum2(rr_u, rr_v, red_d, nwa);
+        rr_u = rr.x;
+        rr_v = rr.y;
+        const double tol_u = rr_u * 1e-28, tol_v = rr_v * 1e-28;
+        bool done_u = rr_u <= tol_u || rr_u == 0, done_v = rr_v <= tol_v || rr_v == 0;
+        int iter = 0;
+        for (; iter < kCgMaxIters && !(done_u && done_v); ++iter) {
+          double qu[kCgPer], qv[kCgPer], pq_u = 0, pq_v = 0;
+#pragma unroll
+          for (int k = 0; k < kCgPer; ++k) {
+            const int r = tid + k * nt;
+            qu[k] = qv[k] = 0;
+            if (r < nv) {
+              double au = dd[k] * cg_pu[r], av = dd[k] * cg_pv[r];
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const int q = nb[k][e];
+                if (q >= 0) { au -= cg_pu[q]; av -= cg_pv[q]; }
+              }
+              qu[k] = au; qv[k] = av;
+              pq_u += cg_pu[r] * au; pq_v += cg_pv[r] * av;
+            }
+          }
+          const double2 pq = group_sum2(pq_u, pq_v, red_d, nwa);
+          const double al_u = done_u ? 0.0 : rr_u / pq.x, al_v = done_v ? 0.0 : rr_v / pq.y;
+          double nr_u = 0, nr_v = 0;
+#pragma unroll
+          for (int k = 0; k < kCgPer; ++k) {
+            const int r = tid + k * nt;
+            if (r < nv) {
+              xu[k] += al_u * cg_pu[r]; xv[k] += al_v * cg_pv[r];
+              ru[k] -= al_u * qu[k]; rv[k] -= al_v * qv[k];
+              nr_u += ru[k] * ru[k]; nr_v += rv[k] * rv[k];
+            }
+          }
+          const double2 nr = group_sum2(nr_u, nr_v, red_d, nwa);
+          const double be_u = done_u ? 0.0 : nr.x / rr_u, be_v = done_v ? 0.0 : nr.y / rr_v;
+          group_bar(nwa);  // every read of p in this iteration is done
+#pragma unroll
+          for (int k = 0; k < kCgPer; ++k) {
+            const int r = tid + k * nt;
+            if (r < nv) {
+              if (!done_u) cg_pu[r] = ru[k] + be_u * cg_pu[r];
+              if (!done_v) cg_pv[r] = rv[k] + be_v * cg_pv[r];
+            }
+          }
+          rr_u = nr.x; rr_v = nr.y;
+          done_u = done_u || rr_u <= tol_u;
+          done_v = done_v || rr_v <= tol_v;
+          group_bar(nwa);  // the new p is visible to the next product
+        }
+        if (iter >= kCgMaxIters && tid == 0 && status) atomicExch(status, PIV_E_TIMEOUT);
 #pragma unroll
         for (int k = 0; k < kCgPer; ++k) {
           const int r = tid + k * nt;
-          if (r < nv) {
-            xu[k] += al_u * cg_pu[r]; xv[k] += al_v * cg_pv[r];
-            ru[k] -= al_u * qu[k]; rv[k] -= al_v * qv[k];
-            nr_u += ru[k] * ru[k]; nr_v += rv[k] * rv[k];
-          }
+          if (r < nv) { sc.new_u[r] = xu[k]; sc.new_v[r] = xv[k]; }
         }
-        const double2 nr = block_sum2(nr_u, nr_v, red_d);
-        const double be_u = done_u ? 0.0 : nr.x / rr_u, be_v = done_v ? 0.0 : nr.y / rr_v;
-#pragma unroll
-        for (int k = 0; k < kCgPer; ++k) {
-          const int r = tid + k * nt;
-          if (r < nv) {
-            if (!done_u) cg_pu[r] = ru[k] + be_u * cg_pu[r];
-            if (!done_v) cg_pv[r] = rv[k] + be_v * cg_pv[r];
-          }
-        }
-        rr_u = nr.x; rr_v = nr.y;
-        done_u = done_u || rr_u <= tol_u;
-        done_v = done_v || rr_v <= tol_v;
-        __syncthreads();
-      }
-      if (iter >= kCgMaxIters && tid == 0 && status) atomicExch(status, PIV_E_TIMEOUT);
-#pragma unroll
-      for (int k = 0; k < kCgPer; ++k) {
-        const int r = tid + k * nt;
-        if (r < nv) { sc.new_u[r] = xu[k]; sc.new_v[r] = xv[k]; }
       }
     } else if (a.method == PIV_REPLACE_SPRING) {
       FieldView fu{u, m, n, val, 0.0}, fv{v, m, n, val, 0.0};
