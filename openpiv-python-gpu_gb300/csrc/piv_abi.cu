@@ -392,7 +392,8 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
     rc = plan_alloc(p, &p->def_a, (size_t)P * hw * tsz);
     if (rc == PIV_OK) rc = plan_alloc(p, &p->def_b, (size_t)P * hw * tsz);
   }
-  if (rc == PIV_OK && p->any_cubic) rc = plan_alloc_t(p, &p->coef, 2 * (size_t)P * hw);
+  const size_t chw = (size_t)(cfg->height + 2 * kCoefPad) * (cfg->width + 2 * kCoefPad);  // padded coefficient frame
+  if (rc == PIV_OK && p->any_cubic) rc = plan_alloc_t(p, &p->coef, 2 * (size_t)P * chw);
   if (rc == PIV_OK && cfg->mask) {
     rc = plan_alloc_t(p, &p->frame_mask, hw);
     if (rc == PIV_OK) cudaMemcpy(p->frame_mask, cfg->mask, hw, cudaMemcpyHostToDevice);
@@ -536,7 +537,7 @@ static int run_begin(piv_plan* p, int n_pairs, const void* frames_a, const void*
 static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
   const piv_config& cfg = p->cfg;
   const int H = cfg.height, W = cfg.width;
-  const size_t hw = (size_t)H * W;
+  const size_t chw = (size_t)(H + 2 * kCoefPad) * (W + 2 * kCoefPad);  // padded coefficient frame
   const int n_pairs = x.n_pairs;
   IterState& st = p->st[k];
   const piv_iteration& it = st.it;
@@ -554,8 +555,9 @@ static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
     }
     mark(p, x, k * PIV_STAGES + 0, s);
     if (it.deforming_order == 3 && !x.coef_ready) {
-      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fa, cfg.pixel_type, p->coef, s));
-      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fb, cfg.pixel_type, p->coef + (size_t)cfg.max_pairs * hw, s));
+      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fa, cfg.pixel_type, p->coef, s, kCoefPad));
+      PIV_TRY(spline_prefilter(H, W, n_pairs, x.fb, cfg.pixel_type, p->coef + (size_t)cfg.max_pairs * chw, s,
+                               kCoefPad));
       x.coef_ready = true;
     }
     DeformArgs d;
@@ -569,7 +571,8 @@ static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
     d.deforming_par = it.deforming_par;
     d.order = it.deforming_order == 3 ? 3 : 1;
     d.coef_a = p->coef;
-    d.coef_b = p->coef ? p->coef + (size_t)cfg.max_pairs * hw : nullptr;
+    d.coef_b = p->coef ? p->coef + (size_t)cfg.max_pairs * chw : nullptr;
+    d.coef_pad = kCoefPad;
     d.frame_mask = p->frame_mask;
     d.dtype = cfg.dtype;
     d.out_a = p->def_a;
@@ -892,6 +895,7 @@ int piv_deform(const piv_geometry* g, int n_pairs, const void* frames_a, const v
   d.order = deforming_order == 3 ? 3 : 1;
   d.coef_a = coef_a;
   d.coef_b = coef_b;
+  d.coef_pad = 0;
   d.frame_mask = frame_mask;
   d.dtype = dtype;
   d.out_a = out_a;

@@ -209,6 +209,31 @@ PIV_D float sample_cubic(const float* __restrict__ coef, int W, int H, float xi,
   return acc;
 }
 
+// Cubic B-spline sample of a padded coefficient frame (origin of the frame at
+// coef, row stride S = W + 4, mirrored 2-pixel border): a sample clamped into
+// the frame has all 16 taps inside the padded buffer.
+PIV_D float sample_cubic_padded(const float* __restrict__ coef, int S, int W, int H, float xi, float yi) {
+  xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
+  yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
+  const float fx = floorf(xi), fy = floorf(yi);
+  const int x0 = (int)fx - 1, y0 = (int)fy - 1;
+  float w[4], v[4];
+  bspline3_weights(xi - fx, w);
+  bspline3_weights(yi - fy, v);
+  const float* p = coef + (y0 * S + x0);
+  float acc = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float* row = p + r * S;
+    float s = w[0] * __ldg(row);
+    s = fmaf(w[1], __ldg(row + 1), s);
+    s = fmaf(w[2], __ldg(row + 2), s);
+    s = fmaf(w[3], __ldg(row + 3), s);
+    acc = fmaf(v[r], s, acc);
+  }
+  return acc;
+}
+
 // Predictor weight of one axis at integer pixel coordinate q on the uniform
 // grid g_k = k*sp + ss/2 + off: interval index clamped to [0, len-2], weight
 // from the unclamped distance. Works in doubled integer coordinates so that
@@ -284,6 +309,11 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap
   const long long base = (long long)pair * H * W;
   T* out_a = reinterpret_cast<T*>(a.out_a) + base;
   T* out_b = reinterpret_cast<T*>(a.out_b) + base;
+  // Coefficient frames of the pair (origin of the frame, row stride cs).
+  const int cpad = a.coef_pad, cs = W + 2 * cpad;
+  const long long cbase = (long long)pair * (H + 2 * cpad) * cs + (long long)cpad * cs + cpad;
+  const float* cfa = a.coef_a ? a.coef_a + cbase : nullptr;
+  const float* cfb = a.coef_b ? a.coef_b + cbase : nullptr;
   const int c0 = wx.i - k_lo, c1 = (g.n < 2 ? wx.i : wx.i + 1) - k_lo;
   const T x = (T)j;
 #pragma unroll 1
@@ -310,15 +340,17 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform(DeformArgs a, AxisMap
     T ra, rb;
     if (do_a) {
       const T xi = add_rn(x, mul_rn(up, dta)), yi = add_rn(y, mul_rn(vp, dta));
-      ra = a.order == 3 ? (T)sample_cubic(a.coef_a + base, W, H, (float)xi, (float)yi)
-                        : sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi);
+      ra = a.order != 3 ? sample_bilinear<T>(a.frames_a, a.pixel_type, base, W, H, xi, yi)
+           : a.coef_pad ? (T)sample_cubic_padded(cfa, cs, W, H, (float)xi, (float)yi)
+                        : (T)sample_cubic(cfa, W, H, (float)xi, (float)yi);
     } else {
       ra = load_pixel<T>(a.frames_a, a.pixel_type, base + p);
     }
     if (do_b) {
       const T xi = add_rn(x, mul_rn(up, dtb)), yi = add_rn(y, mul_rn(vp, dtb));
-      rb = a.order == 3 ? (T)sample_cubic(a.coef_b + base, W, H, (float)xi, (float)yi)
-                        : sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi);
+      rb = a.order != 3 ? sample_bilinear<T>(a.frames_b, a.pixel_type, base, W, H, xi, yi)
+           : a.coef_pad ? (T)sample_cubic_padded(cfb, cs, W, H, (float)xi, (float)yi)
+                        : (T)sample_cubic(cfb, W, H, (float)xi, (float)yi);
     } else {
       rb = load_pixel<T>(a.frames_b, a.pixel_type, base + p);
     }
@@ -361,9 +393,33 @@ PIV_D float sample_cubic32(const float* __restrict__ coef, int W, int H, float x
   return fmaf(wy3, s3, fmaf(wy2, s2, fmaf(wy1, s1, wy0 * s0)));
 }
 
+// sample_cubic32 on a padded coefficient frame (row stride S): no edge case.
+PIV_D float sample_cubic32p(const float* __restrict__ coef, int S, int W, int H, float xi, float yi) {
+  xi = fminf(fmaxf(xi, 0.0f), (float)(W - 1));
+  yi = fminf(fmaxf(yi, 0.0f), (float)(H - 1));
+  const float fx = floorf(xi), fy = floorf(yi);
+  const int x0 = (int)fx - 1, y0 = (int)fy - 1;
+  float wx0, wx1, wx2, wx3, wy0, wy1, wy2, wy3;
+  bspline3_weights_fast(xi - fx, wx0, wx1, wx2, wx3);
+  bspline3_weights_fast(yi - fy, wy0, wy1, wy2, wy3);
+  const float* r0 = coef + (y0 * S + x0);
+  const float* r1 = r0 + S;
+  const float* r2 = r1 + S;
+  const float* r3 = r2 + S;
+  float s0 = wx0 * __ldg(r0), s1 = wx0 * __ldg(r1), s2 = wx0 * __ldg(r2), s3 = wx0 * __ldg(r3);
+  s0 = fmaf(wx1, __ldg(r0 + 1), s0); s1 = fmaf(wx1, __ldg(r1 + 1), s1);
+  s2 = fmaf(wx1, __ldg(r2 + 1), s2); s3 = fmaf(wx1, __ldg(r3 + 1), s3);
+  s0 = fmaf(wx2, __ldg(r0 + 2), s0); s1 = fmaf(wx2, __ldg(r1 + 2), s1);
+  s2 = fmaf(wx2, __ldg(r2 + 2), s2); s3 = fmaf(wx2, __ldg(r3 + 2), s3);
+  s0 = fmaf(wx3, __ldg(r0 + 3), s0); s1 = fmaf(wx3, __ldg(r1 + 3), s1);
+  s2 = fmaf(wx3, __ldg(r2 + 3), s2); s3 = fmaf(wx3, __ldg(r3 + 3), s3);
+  return fmaf(wy3, s3, fmaf(wy2, s2, fmaf(wy1, s1, wy0 * s0)));
+}
+
 // k_deform for the common case: float32 fields, cubic B-spline sampling of
 // both frames (0 < deforming_par < 1). The row weights of the block's four
 // rows are computed once per CTA; pixel offsets are 32-bit.
+template <bool PADDED>
 __global__ void __launch_bounds__(kDeformThreads) k_deform_cubic(DeformArgs a, AxisMap ax, AxisMap ay, float dta,
                                                                  float dtb) {
   __shared__ float su[kDeformMaxGridRows][kDeformMaxCols], sv[kDeformMaxGridRows][kDeformMaxCols];
@@ -400,8 +456,11 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform_cubic(DeformArgs a, A
   __syncthreads();
   if (j >= W) return;
   const long long base = (long long)pair * H * W;
-  const float* ca = a.coef_a + base;
-  const float* cb = a.coef_b + base;
+  const int cs = PADDED ? W + 2 * kCoefPad : W;
+  const long long cbase = PADDED ? (long long)pair * (H + 2 * kCoefPad) * cs + (long long)kCoefPad * cs + kCoefPad
+                                 : base;
+  const float* ca = a.coef_a + cbase;
+  const float* cb = a.coef_b + cbase;
   float* out_a = reinterpret_cast<float*>(a.out_a) + base;
   float* out_b = reinterpret_cast<float*>(a.out_b) + base;
   const uint8_t* mask = a.frame_mask;
@@ -426,8 +485,10 @@ __global__ void __launch_bounds__(kDeformThreads) k_deform_cubic(DeformArgs a, A
     const float up = fmaf(wx.t, u1 - u0, u0);
     const float vp = fmaf(wx.t, v1 - v0, v0);
     const float y = (float)i;
-    const float ra = sample_cubic32(ca, W, H, add_rn(x, mul_rn(up, dta)), add_rn(y, mul_rn(vp, dta)));
-    const float rb = sample_cubic32(cb, W, H, add_rn(x, mul_rn(up, dtb)), add_rn(y, mul_rn(vp, dtb)));
+    const float xa = add_rn(x, mul_rn(up, dta)), ya = add_rn(y, mul_rn(vp, dta));
+    const float xb = add_rn(x, mul_rn(up, dtb)), yb = add_rn(y, mul_rn(vp, dtb));
+    const float ra = PADDED ? sample_cubic32p(ca, cs, W, H, xa, ya) : sample_cubic32(ca, W, H, xa, ya);
+    const float rb = PADDED ? sample_cubic32p(cb, cs, W, H, xb, yb) : sample_cubic32(cb, W, H, xb, yb);
     out_a[p] = ra;
     out_b[p] = rb;
   }
@@ -438,6 +499,7 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   if (total == 0) return PIV_OK;
   if (a.order == 3 && (!a.coef_a || !a.coef_b))
     return set_error(PIV_E_ARG, "cubic deformation needs spline coefficient frames");
+  if (a.coef_pad != 0 && a.coef_pad != kCoefPad) return set_error(PIV_E_ARG, "coef_pad must be 0 or %d", kCoefPad);
   if (a.geom.spacing < 1) return set_error(PIV_E_ARG, "deformation: spacing must be >= 1");
   const double dp = a.deforming_par;
   double dta = 0, dtb = 0;
@@ -454,8 +516,10 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
   const AxisMap ay = axis_map(a.geom.search_size, a.geom.y_offset, a.geom.spacing, a.geom.m);
   if (a.dtype == PIV_DTYPE_F64)
     k_deform<double><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, dta, dtb, do_a, do_b);
+  else if (a.order == 3 && do_a && do_b && a.coef_pad)
+    k_deform_cubic<true><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb);
   else if (a.order == 3 && do_a && do_b)
-    k_deform_cubic<<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb);
+    k_deform_cubic<false><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb);
   else
     k_deform<float><<<grid, kDeformThreads, 0, stream>>>(a, ax, ay, (float)dta, (float)dtb, do_a, do_b);
   cudaError_t e = cudaGetLastError();
@@ -490,7 +554,8 @@ PIV_D int mirror_any(int q, int n) {
 }
 
 template <typename P>
-__global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __restrict__ in, float* __restrict__ out) {
+__global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __restrict__ in, float* __restrict__ out,
+                                                   int pad) {
   __shared__ float reg[kPfR * kPfS];
   const int x0 = blockIdx.x * kPfT, y0 = blockIdx.y * kPfT;
   const long long fbase = (long long)blockIdx.z * H * W;
@@ -593,8 +658,8 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
       for (int k = 0; k < 8; ++k) reg[(k0 + k) * kPfS + col] = v[k];
     }
     float d = 0.f;
-    const int gx = x0 + threadIdx.x;
-    float* dst = out + fbase + gx;
+    const int gx = x0 + threadIdx.x, os = W + 2 * pad;
+    float* dst = out + (long long)blockIdx.z * (H + 2 * pad) * os + (long long)pad * os + pad + gx;
     for (int k0 = kPfR - 8; k0 + 8 > kPfK; k0 -= 8) {
       float v[8];
 #pragma unroll
@@ -607,25 +672,59 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         const int gy = y0 + k0 + k - kPfK;
-        if (k0 + k >= kPfK && k0 + k < kPfK + kPfT && gx < W && gy < H) dst[(long long)gy * W] = 36.0f * v[k];
+        if (k0 + k >= kPfK && k0 + k < kPfK + kPfT && gx < W && gy < H) dst[(long long)gy * os] = 36.0f * v[k];
       }
     }
   }
 }
 
+// The 2-pixel border of padded coefficient frames: border element (y, x) of
+// the frame holds coefficient (mirror(y), mirror(x)), as the unpadded
+// sampler's mirror rule reads it. Grid: x over the border elements, y over
+// frames.
+__global__ void k_coef_border(int H, int W, float* __restrict__ coef) {
+  const int S = W + 2 * kCoefPad, HP = H + 2 * kCoefPad;
+  const int n_border = S * HP - H * W;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_border) return;
+  float* f = coef + (long long)blockIdx.y * HP * S;
+  // Border elements: the 2 * kCoefPad full rows first, then the side columns.
+  int y, x;
+  const int top = 2 * kCoefPad * S;
+  if (t < top) {
+    const int r = t / S;
+    y = r < kCoefPad ? r - kCoefPad : H + (r - kCoefPad);
+    x = t % S - kCoefPad;
+  } else {
+    const int q = t - top, r = q / (2 * kCoefPad), c = q % (2 * kCoefPad);
+    y = r;
+    x = c < kCoefPad ? c - kCoefPad : W + (c - kCoefPad);
+  }
+  const int my = mirror_any(y, H), mx = mirror_any(x, W);  // mirror_index's value wherever that is in range
+  f[(long long)(y + kCoefPad) * S + x + kCoefPad] = f[(long long)(my + kCoefPad) * S + mx + kCoefPad];
+}
+
 int spline_prefilter(int H, int W, int n_frames, const void* frames, int pixel_type, float* coef,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int pad) {
   if ((long long)H * W * n_frames == 0) return PIV_OK;
   if (n_frames > 65535) return set_error(PIV_E_UNSUPPORTED, "spline prefilter: more than 65535 frames");
+  if (pad != 0 && pad != kCoefPad) return set_error(PIV_E_ARG, "spline prefilter: pad must be 0 or %d", kCoefPad);
   const dim3 grid((unsigned)((W + kPfT - 1) / kPfT), (unsigned)((H + kPfT - 1) / kPfT), (unsigned)n_frames);
   switch (pixel_type) {
-    case PIV_PIXEL_U8: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint8_t*)frames, coef); break;
-    case PIV_PIXEL_U16: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint16_t*)frames, coef); break;
-    case PIV_PIXEL_F32: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const float*)frames, coef); break;
-    default: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const double*)frames, coef); break;
+    case PIV_PIXEL_U8: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint8_t*)frames, coef, pad); break;
+    case PIV_PIXEL_U16: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint16_t*)frames, coef, pad); break;
+    case PIV_PIXEL_F32: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const float*)frames, coef, pad); break;
+    default: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const double*)frames, coef, pad); break;
   }
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_prefilter launch");
+  if (e != cudaSuccess) return set_cuda_error(e, "k_prefilter launch");
+  if (pad) {
+    const int n_border = (W + 2 * kCoefPad) * (H + 2 * kCoefPad) - H * W;
+    k_coef_border<<<dim3((unsigned)((n_border + 255) / 256), (unsigned)n_frames), 256, 0, stream>>>(H, W, coef);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error(e, "k_coef_border launch");
+  }
+  return PIV_OK;
 }
 
 }  // namespace piv

@@ -87,6 +87,7 @@ struct DeformArgs {
   int order;
   const float* coef_a;
   const float* coef_b;
+  int coef_pad;  // 0: [pairs][H][W]; kCoefPad: [pairs][H + 4][W + 4] with a mirrored 2-pixel border
   const uint8_t* frame_mask;
   int dtype;
   void* out_a;
@@ -95,8 +96,12 @@ struct DeformArgs {
 int deform(const DeformArgs& a, cudaStream_t stream);
 int regrid(const piv_geometry& src, const piv_geometry& dst, int n_pairs, const double* u_src, const double* v_src,
            double* u_dst, double* v_dst, cudaStream_t stream);
+// pad = 0: coef is [n_frames][height][width]; pad = kCoefPad: [n_frames][height
+// + 4][width + 4], the frame at offset (2, 2) and the border holding the
+// mirrored coefficients, so that cubic taps never need the mirror rule.
+constexpr int kCoefPad = 2;
 int spline_prefilter(int height, int width, int n_frames, const void* frames, int pixel_type, float* coef,
-                     cudaStream_t stream);
+                     cudaStream_t stream, int pad = 0);
 
 // Validation and replacement.
 struct ValArgs {
