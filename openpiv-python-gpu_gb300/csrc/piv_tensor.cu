@@ -646,80 +646,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     // (scaled by 2^(e_a + e_b)); shifted row index i = r ^ N/2, shifted
     // column j = s ^ N/2. Lags without window overlap (i = 0 or j = 0) are 0.
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
-#pragma unroll
-    for (int ri = 0; ri < 2 / TPL; ++ri) {
-      const int rt = TPL == 2 ? half : ri;
-      const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
-      float v[N];
-#pragma unroll
-      for (int c0 = 0; c0 < N; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
-      tc::reg_fence(v);
-      float rowc[N];
-#pragma unroll
-      for (int j = 0; j < N; ++j) rowc[j] = j == 0 ? 0.f : v[j ^ HN];
-      float best;
-      int bj;
-      first_max<N>(rowc, best, bj);
-      int idx = i * N + bj;
-      if (i == 0) { best = 0.f; idx = 0; }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-        const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-        if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
-      }
-      if (lane == 0) {
-        pk_val[w][r / 32] = best;
-        pk_idx[w][r / 32] = idx;
-      }
-      if (a.maps && g0 + w < total) {
-        const int ue = -sc_e[0][w] - sc_e[1][w];
-        float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
-#pragma unroll
-        for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
-      }
-    }
-    __syncthreads();
-    if (tid < W) {
-      float v = pk_val[tid][0];
-      int idx = pk_idx[tid][0];
-#pragma unroll
-      for (int p = 1; p < NPART; ++p)
-        if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
-          v = pk_val[tid][p];
-          idx = pk_idx[tid][p];
-        }
-      pk_idx[tid][0] = idx;
-    }
-    __syncthreads();
-    // The rows next to the peak go to shared memory for the five-point fit.
-#pragma unroll
-    for (int ri = 0; ri < 2 / TPL; ++ri) {
-      const int rt = TPL == 2 ? half : ri;
-      const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
-      const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
-      const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
-      if (__any_sync(0xffffffffu, mine)) {
-        float v[N];
-#pragma unroll
-        for (int c0 = 0; c0 < N; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-        tc::tmem_ld_wait();
-        tc::reg_fence(v);
-        if (mine) {
-          float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
-#pragma unroll
-          for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
-        }
-      }
-    }
-    __syncthreads();
-    if (tid < W && g0 + tid < total) {
-      const int ww = tid;
-      const long long g = g0 + ww;
-      const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
+    // Subpixel fit and outputs of window ww with flat peak index pidx (its
+    // neighbour rows in nbrow).
+    auto finish = [&](int ww, int pidx) {
+      const int pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = -sc_e[0][ww] - sc_e[1][ww];
@@ -745,6 +675,122 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
+    };
+    if constexpr (N == 32 && TPL == 1) {
+      // One window per warp and row tile (N = 32 rows): the warp finds its
+      // window's peak by shuffles and the lanes of the rows next to it store
+      // them at once (no second TMEM pass); then one barrier, and W lanes fit.
+#pragma unroll
+      for (int rt = 0; rt < 2; ++rt) {
+        const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
+        float v[N];
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+        tc::reg_fence(v);
+        float rowc[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) rowc[j] = j == 0 ? 0.f : v[j ^ HN];
+        float best;
+        int bj;
+        first_max<N>(rowc, best, bj);
+        int idx = i * N + bj;
+        if (i == 0) { best = 0.f; idx = 0; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+          const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+          if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
+        }
+        if (a.maps && g0 + w < total) {
+          const int ue = -sc_e[0][w] - sc_e[1][w];
+          float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
+#pragma unroll
+          for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
+        }
+        const int pi_ = idx / N, pj = idx % N;
+        if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1) {
+          float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
+#pragma unroll
+          for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+        }
+        if (lane == 0) pk_idx[w][0] = idx;
+      }
+      __syncthreads();
+      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
+    } else {
+#pragma unroll
+      for (int ri = 0; ri < 2 / TPL; ++ri) {
+        const int rt = TPL == 2 ? half : ri;
+        const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
+        float v[N];
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16)
+          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+        tc::reg_fence(v);
+        float rowc[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) rowc[j] = j == 0 ? 0.f : v[j ^ HN];
+        float best;
+        int bj;
+        first_max<N>(rowc, best, bj);
+        int idx = i * N + bj;
+        if (i == 0) { best = 0.f; idx = 0; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+          const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+          if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
+        }
+        if (lane == 0) {
+          pk_val[w][r / 32] = best;
+          pk_idx[w][r / 32] = idx;
+        }
+        if (a.maps && g0 + w < total) {
+          const int ue = -sc_e[0][w] - sc_e[1][w];
+          float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
+#pragma unroll
+          for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
+        }
+      }
+      __syncthreads();
+      if (tid < W) {
+        float v = pk_val[tid][0];
+        int idx = pk_idx[tid][0];
+#pragma unroll
+        for (int p = 1; p < NPART; ++p)
+          if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
+            v = pk_val[tid][p];
+            idx = pk_idx[tid][p];
+          }
+        pk_idx[tid][0] = idx;
+      }
+      __syncthreads();
+      // The rows next to the peak go to shared memory for the five-point fit.
+#pragma unroll
+      for (int ri = 0; ri < 2 / TPL; ++ri) {
+        const int rt = TPL == 2 ? half : ri;
+        const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
+        const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
+        const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
+        if (__any_sync(0xffffffffu, mine)) {
+          float v[N];
+#pragma unroll
+          for (int c0 = 0; c0 < N; c0 += 16)
+            tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tc::tmem_ld_wait();
+          tc::reg_fence(v);
+          if (mine) {
+            float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
+#pragma unroll
+            for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
     }
     tc::fence_before_sync();
     __syncthreads();
