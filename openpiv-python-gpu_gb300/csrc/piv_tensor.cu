@@ -756,24 +756,25 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
       }
       __syncthreads();
-      if (tid < W) {
-        float v = pk_val[tid][0];
-        int idx = pk_idx[tid][0];
+      // First maximum of window w over its NPART warp partials (each thread
+      // that needs it combines them itself: no further barrier).
+      auto window_peak = [&](int w) -> int {
+        float v = pk_val[w][0];
+        int idx = pk_idx[w][0];
 #pragma unroll
         for (int p = 1; p < NPART; ++p)
-          if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
-            v = pk_val[tid][p];
-            idx = pk_idx[tid][p];
+          if (pk_val[w][p] > v || (pk_val[w][p] == v && pk_idx[w][p] < idx)) {
+            v = pk_val[w][p];
+            idx = pk_idx[w][p];
           }
-        pk_idx[tid][0] = idx;
-      }
-      __syncthreads();
+        return idx;
+      };
       // The rows next to the peak go to shared memory for the five-point fit.
 #pragma unroll
       for (int ri = 0; ri < 2 / TPL; ++ri) {
         const int rt = TPL == 2 ? half : ri;
         const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
-        const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
+        const int pidx = window_peak(w), pi_ = pidx / N, pj = pidx % N;
         const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
         if (__any_sync(0xffffffffu, mine)) {
           float v[N];
@@ -790,7 +791,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
       }
       __syncthreads();
-      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
+      if (tid < W && g0 + tid < total) finish(tid, window_peak(tid));
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -1243,7 +1244,6 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     __syncthreads();
     if (tid < W && g0 + tid < total) {
       const int ww = tid;
-      const long long g = g0 + ww;
       const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
