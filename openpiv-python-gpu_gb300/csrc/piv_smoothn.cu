@@ -35,8 +35,11 @@ struct SmoothScratch {
 static size_t align_up(size_t v) { return (v + 255) / 256 * 256; }
 
 // Per-pair block of the weighted path: f, z, t, fd, tmp (2 mn doubles each),
-// w (mn doubles) and the column-nearest table (mn ints).
-static size_t weighted_pair_bytes(size_t mn) { return align_up(11 * mn * 8 + mn * 4); }
+// w (mn doubles), the column-nearest table (mn ints) and the hi/lo float
+// split of a DCT input (2 mn floats).
+static size_t weighted_pair_bytes(size_t mn) { return align_up(11 * mn * 8 + mn * 4 + 2 * mn * 4); }
+// The DCT matrices of the weighted path as hi/lo float pairs (2 (m^2 + n^2) floats).
+static size_t weighted_matrix_bytes(int m, int n) { return align_up(2 * ((size_t)m * m + (size_t)n * n) * 4); }
 
 size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
   const size_t mn = (size_t)m * n;
@@ -44,7 +47,7 @@ size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
                         align_up((size_t)n_pairs * 8);
   const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared +
                        align_up(mn * n_pairs * 4) + align_up(mn * 4);
-  const size_t weighted = shared + weighted_pair_bytes(mn) * n_pairs;
+  const size_t weighted = shared + weighted_matrix_bytes(m, n) + weighted_pair_bytes(mn) * n_pairs;
   return plain > weighted ? plain : weighted;
 }
 
@@ -428,30 +431,83 @@ PIV_D double cta_sum(double v, double* red) {
   return t;
 }
 
-// 2-D orthonormal DCT-II (inv = false) or DCT-III of one m x n field inside the CTA.
-PIV_D void cta_dct2(const double* in, double* tmp, double* out, int m, int n, const double* __restrict__ cm,
-                    const double* __restrict__ cn, bool inv) {
+// x -> (hi, lo) float pairs: hi = (float)x, lo = (float)(x - hi).
+__global__ void k_split_f64(int count, const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const float h = (float)x[t];
+  hi[t] = h;
+  lo[t] = (float)(x[t] - (double)h);
+}
+
+// Dot product of two hi/lo float vectors in float32 with error-free
+// transformations: every product's rounding error is kept (fma), the cross
+// terms a_hi b_lo + a_lo b_hi join a small-term sum, and the main sum is
+// compensated (TwoSum). The result, (hi, lo), is within ~1e-13 of the float64
+// dot product here (orthonormal cosine matrices, smooth fields), at a fraction
+// of the cost of float64 FMAs on this GPU.
+struct DfAcc {
+  float s = 0.f, c = 0.f;
+  PIV_D void add(float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    c += fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
+    const float t = s + p, bp = t - s;
+    c += (s - (t - bp)) + (p - bp);
+    s = t;
+  }
+  PIV_D void result(float& hi, float& lo) const {
+    hi = s + c;
+    lo = c - (hi - s);
+  }
+};
+
+struct DfMats {
+  const float *cmh, *cml, *cnh, *cnl;  // [m][m], [n][n] hi and lo parts
+};
+
+// 2-D orthonormal DCT-II (inv = false) or DCT-III of one m x n field inside the
+// CTA, in the double-float arithmetic of DfAcc. xs: 2 mn floats (the input's
+// hi/lo split); tmp: 2 mn floats (the row pass); in and out may not overlap
+// tmp or xs.
+PIV_D void cta_dct2(const double* in, float* xs, float* tmp, double* out, int m, int n, const DfMats& M, bool inv) {
   const int mn = m * n;
   for (int e = threadIdx.x; e < mn; e += blockDim.x) {
+    const double x = in[e];
+    const float h = (float)x;
+    xs[e] = h;
+    xs[mn + e] = (float)(x - (double)h);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < mn; e += blockDim.x) {
     const int i = e / n, l = e % n;
-    double acc = 0.0;
-    for (int j = 0; j < n; ++j) acc = fma(in[i * n + j], inv ? cn[j * n + l] : cn[l * n + j], acc);
-    tmp[e] = acc;
+    DfAcc acc;
+    for (int j = 0; j < n; ++j) {
+      const int ci = inv ? j * n + l : l * n + j;
+      acc.add(xs[i * n + j], xs[mn + i * n + j], M.cnh[ci], M.cnl[ci]);
+    }
+    acc.result(tmp[e], tmp[mn + e]);
   }
   __syncthreads();
   for (int e = threadIdx.x; e < mn; e += blockDim.x) {
     const int k = e / n, j = e % n;
-    double acc = 0.0;
-    for (int i = 0; i < m; ++i) acc = fma(inv ? cm[i * m + k] : cm[k * m + i], tmp[i * n + j], acc);
-    out[e] = acc;
+    DfAcc acc;
+    for (int i = 0; i < m; ++i) {
+      const int ci = inv ? i * m + k : k * m + i;
+      acc.add(M.cmh[ci], M.cml[ci], tmp[i * n + j], tmp[mn + i * n + j]);
+    }
+    float h, l;
+    acc.result(h, l);
+    out[e] = (double)h + (double)l;
   }
   __syncthreads();
 }
 
 struct SwCtx {
   int m, n, mn;
-  const double *cm, *cn, *lam2;
+  const double* lam2;
+  DfMats mats;
   double *f, *z, *t, *fd, *tmp, *w;
+  float* xs;  // 2 mn floats: hi/lo split of a DCT input
   double n_finite, w_mean;
   double* red;
 };
@@ -462,18 +518,19 @@ PIV_D double sw_gcv(const SwCtx& c, double p) {
   double rss = 0.0, tr = 0.0;
   if (c.w_mean > 0.9) {
     for (int e = threadIdx.x; e < c.mn; e += blockDim.x) {
-      const double gm = 1.0 / (1.0 + s * c.lam2[e]);
+      const double gm = rcp_fast(1.0 + s * c.lam2[e]);
       const double d = gm - 1.0;
       rss += (c.fd[e] * c.fd[e] + c.fd[c.mn + e] * c.fd[c.mn + e]) * d * d;
       tr += gm;
     }
   } else {
-    for (int e = threadIdx.x; e < c.mn; e += blockDim.x) tr += 1.0 / (1.0 + s * c.lam2[e]);
+    for (int e = threadIdx.x; e < c.mn; e += blockDim.x) tr += rcp_fast(1.0 + s * c.lam2[e]);
     for (int fi = 0; fi < 2; ++fi) {
       // f_hat = IDCT2(gamma fd); t holds gamma fd, z is kept.
-      for (int e = threadIdx.x; e < c.mn; e += blockDim.x) c.t[fi * c.mn + e] = c.fd[fi * c.mn + e] / (1.0 + s * c.lam2[e]);
+      for (int e = threadIdx.x; e < c.mn; e += blockDim.x)
+        c.t[fi * c.mn + e] = c.fd[fi * c.mn + e] * rcp_fast(1.0 + s * c.lam2[e]);
       __syncthreads();
-      cta_dct2(c.t + fi * c.mn, c.tmp, c.tmp + c.mn, c.m, c.n, c.cm, c.cn, true);
+      cta_dct2(c.t + fi * c.mn, c.xs, reinterpret_cast<float*>(c.tmp), c.tmp + c.mn, c.m, c.n, c.mats, true);
       for (int e = threadIdx.x; e < c.mn; e += blockDim.x) {
         const double fv = c.f[fi * c.mn + e];
         if (isfinite(fv) || c.w[e] > 0) {
@@ -552,18 +609,19 @@ PIV_D double sw_search(const SwCtx& c, double p, bool have_p, double pmin, doubl
 __global__ void __launch_bounds__(kSwThreads)
 k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double* u_out, double* v_out,
                    const uint8_t* __restrict__ mask,
-                   double fixed_p, int is_auto, double pmin, double pmax, const double* __restrict__ cm,
-                   const double* __restrict__ cn, const double* __restrict__ lam2, unsigned char* scratch,
-                   size_t pair_bytes, double* p_out) {
+                   double fixed_p, int is_auto, double pmin, double pmax, DfMats mats,
+                   const double* __restrict__ lam2, unsigned char* scratch, size_t pair_bytes, double* p_out) {
   __shared__ double red[32];
   __shared__ int s_flag;
   const int pair = blockIdx.x, mn = m * n, tid = threadIdx.x, nt = blockDim.x;
   double* base = reinterpret_cast<double*>(scratch + pair_bytes * pair);
   SwCtx c;
-  c.m = m; c.n = n; c.mn = mn; c.cm = cm; c.cn = cn; c.lam2 = lam2;
+  c.m = m; c.n = n; c.mn = mn; c.mats = mats; c.lam2 = lam2;
   c.f = base; c.z = base + 2 * mn; c.t = base + 4 * mn; c.fd = base + 6 * mn; c.tmp = base + 8 * mn;
   c.w = base + 10 * mn; c.red = red;
   int* near = reinterpret_cast<int*>(base + 11 * mn);
+  c.xs = reinterpret_cast<float*>(near + mn);
+  float* tmpf = reinterpret_cast<float*>(c.tmp);
   const long long off = (long long)pair * mn;
   // Fields, finite mask and weights.
   double nf = 0.0, ws = 0.0;
@@ -627,11 +685,11 @@ k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double*
   const int n0 = (m + 9) / 10 + 1, n1 = (n + 9) / 10 + 1;
   for (int fi = 0; fi < 2; ++fi) {
     if (weighted) {
-      cta_dct2(c.f + fi * mn, c.tmp, c.t + fi * mn, m, n, cm, cn, false);
+      cta_dct2(c.f + fi * mn, c.xs, tmpf, c.t + fi * mn, m, n, mats, false);
       for (int e = tid; e < mn; e += nt)
         if (e / n >= n0 && e % n >= n1) c.t[fi * mn + e] = 0.0;
       __syncthreads();
-      cta_dct2(c.t + fi * mn, c.tmp, c.z + fi * mn, m, n, cm, cn, true);
+      cta_dct2(c.t + fi * mn, c.xs, tmpf, c.z + fi * mn, m, n, mats, true);
     } else {
       for (int e = tid; e < mn; e += nt) c.z[fi * mn + e] = 0.0;
     }
@@ -646,7 +704,7 @@ k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double*
       c.t[e] = wv * (c.f[e] - c.z[e]) + c.z[e];
     }
     __syncthreads();
-    for (int fi = 0; fi < 2; ++fi) cta_dct2(c.t + fi * mn, c.tmp, c.fd + fi * mn, m, n, cm, cn, false);
+    for (int fi = 0; fi < 2; ++fi) cta_dct2(c.t + fi * mn, c.xs, tmpf, c.fd + fi * mn, m, n, mats, false);
     if (is_auto && ((k + 1) & k) == 0) {
       p = sw_search(c, p, have_p, pmin, pmax);
       have_p = true;
@@ -654,9 +712,9 @@ k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double*
     const double s = pow(10.0, p);
     double num = 0.0, den = 0.0;
     for (int fi = 0; fi < 2; ++fi) {
-      for (int e = tid; e < mn; e += nt) c.t[fi * mn + e] = c.fd[fi * mn + e] / (1.0 + s * lam2[e]);
+      for (int e = tid; e < mn; e += nt) c.t[fi * mn + e] = c.fd[fi * mn + e] * rcp_fast(1.0 + s * lam2[e]);
       __syncthreads();
-      cta_dct2(c.t + fi * mn, c.tmp, c.tmp + mn, m, n, cm, cn, true);
+      cta_dct2(c.t + fi * mn, c.xs, tmpf, c.tmp + mn, m, n, mats, true);
       for (int e = tid; e < mn; e += nt) {
         const double z0 = c.z[fi * mn + e];
         const double z1 = rf * c.tmp[mn + e] + (1.0 - rf) * z0;
@@ -690,9 +748,15 @@ static int smoothn_weighted(int m, int n, int n_pairs, const double* u_in, const
   double* cn = (double*)p; p += align_up((size_t)n * n * 8);
   double* lam2 = (double*)p; p += align_up(mn * 8);
   p += align_up((size_t)n_pairs * 8);
+  float* mf = (float*)p; p += weighted_matrix_bytes(m, n);
+  const DfMats mats{mf, mf + m * m, mf + 2 * m * m, mf + 2 * m * m + n * n};
   const int bs = 256;
   k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, cm);
   k_dct_matrix<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n, cn);
+  k_split_f64<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m * m, cm, const_cast<float*>(mats.cmh),
+                                                         const_cast<float*>(mats.cml));
+  k_split_f64<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n * n, cn, const_cast<float*>(mats.cnh),
+                                                         const_cast<float*>(mats.cnl));
   k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, lam2);
   const bool is_auto = !(s > 0);
   double pmin = 0, pmax = 0;
@@ -704,7 +768,7 @@ static int smoothn_weighted(int m, int n, int n_pairs, const double* u_in, const
     pmax = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_min)) / 4.0 / a_min, 2.0) - 1.0) / 16.0);
   }
   k_smoothn_weighted<<<n_pairs, kSwThreads, 0, stream>>>(m, n, u_in, v_in, u_out, v_out, field_mask,
-                                                          is_auto ? 0.0 : log10(s), is_auto ? 1 : 0, pmin, pmax, cm, cn,
+                                                          is_auto ? 0.0 : log10(s), is_auto ? 1 : 0, pmin, pmax, mats,
                                                           lam2, (unsigned char*)p, weighted_pair_bytes(mn), p_out);
   return check("k_smoothn_weighted");
 }
