@@ -132,3 +132,25 @@ def test_mixed_size_submission_equals_single_runs(dft, shapes, schedule):
         np.testing.assert_array_equal(u, ue[0])
         np.testing.assert_array_equal(v, ve[0])
     print(f"{dft}, {len(set(shapes))} sizes, {batch.schedule} {batch.schedule_ms}: {batch.kernel_nodes} kernel nodes")
+
+
+def test_batch_rejects_configurations_with_different_passes():
+    """piv_batch_create: the size groups must share the passes (search, window
+    and transform sizes), dtype and correlation engine."""
+    import ctypes as ct
+
+    from openpiv_gpu import _build, _lib, synthetic
+    from openpiv_gpu.gpu_process import PIVGPU
+
+    _build.build()
+    kw = dict(synthetic.CONFIGS[4]["piv"])
+    mss = kw.pop("min_search_size")
+    a = PIVGPU((128, 160), mss, **kw, dft="tensor")
+    b = PIVGPU((96, 96), 2 * mss, **kw, dft="tensor")  # other search sizes
+    c = PIVGPU((96, 96), mss, **kw, dft="fft")         # other engine
+    for other in (b, c):
+        (ca, ka), (cb, kb) = a._config(_lib.PIXEL["u8"], 2), other._config(_lib.PIXEL["u8"], 2)
+        cfgs = (_lib.PivConfig * 2)(ca, cb)
+        batch = ct.c_void_p()
+        assert _lib.lib().piv_batch_create(cfgs, 2, ct.byref(batch)) == _lib.PIV_E_ARG
+        assert "differs" in _lib.last_error()
