@@ -30,6 +30,8 @@ struct SmoothScratch {
   double* p;     // [pairs]
   float* f2f;    // [pairs][mn] f2 in float32 (the GCV search's fast score)
   float* lam2f;  // [mn] lam2 in float32
+  float* cmf;    // [2][m][m] cm as hi/lo floats (the DCT lines' double-float products)
+  float* cnf;    // [2][n][n]
 };
 
 static size_t align_up(size_t v) { return (v + 255) / 256 * 256; }
@@ -46,7 +48,8 @@ size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
   const size_t shared = align_up((size_t)m * m * 8) + align_up((size_t)n * n * 8) + align_up(mn * 8) +
                         align_up((size_t)n_pairs * 8);
   const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared +
-                       align_up(mn * n_pairs * 4) + align_up(mn * 4);
+                       align_up(mn * n_pairs * 4) + align_up(mn * 4) + align_up((size_t)m * m * 8) +
+                       align_up((size_t)n * n * 8);
   const size_t weighted = shared + weighted_matrix_bytes(m, n) + weighted_pair_bytes(mn) * n_pairs;
   return plain > weighted ? plain : weighted;
 }
@@ -63,7 +66,9 @@ static SmoothScratch carve(void* base, int m, int n, int n_pairs) {
   s.lam2 = (double*)p; p += align_up(mn * 8);
   s.p = (double*)p; p += align_up((size_t)n_pairs * 8);
   s.f2f = (float*)p; p += align_up(mn * n_pairs * 4);
-  s.lam2f = (float*)p;
+  s.lam2f = (float*)p; p += align_up(mn * 4);
+  s.cmf = (float*)p; p += align_up((size_t)m * m * 8);
+  s.cnf = (float*)p;
   return s;
 }
 
@@ -120,21 +125,56 @@ __global__ void k_dct_apply(int m, int n, int batch, int mode, const double* __r
 // in shared memory as [position][line]; `cols` selects lines along the
 // columns of the [m][n] fields (stride n) instead of along the rows.
 // Lines up to 90 long keep the staging under the default 48 KB of shared memory.
+// x -> (hi, lo) float pairs: hi = (float)x, lo = (float)(x - hi).
+__global__ void k_split_f64(int count, const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const float h = (float)x[t];
+  hi[t] = h;
+  lo[t] = (float)(x[t] - (double)h);
+}
+
+// Dot product of two hi/lo float vectors in float32 with error-free
+// transformations: every product's rounding error is kept (fma), the cross
+// terms a_hi b_lo + a_lo b_hi join a small-term sum, and the main sum is
+// compensated (TwoSum). The result, (hi, lo), is within ~1e-13 of the float64
+// dot product here (orthonormal cosine matrices, smooth fields), at a fraction
+// of the cost of float64 FMAs on this GPU.
+struct DfAcc {
+  float s = 0.f, c = 0.f;
+  PIV_D void add(float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    c += fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
+    const float t = s + p, bp = t - s;
+    c += (s - (t - bp)) + (p - bp);
+    s = t;
+  }
+  PIV_D void result(float& hi, float& lo) const {
+    hi = s + c;
+    lo = c - (hi - s);
+  }
+};
+
 static constexpr int kDctLines = 32, kDctThreads = 256, kDctMaxLen = 90;
 
+// DCT-II (or, INV, DCT-III) of kDctLines lines per CTA with the symmetric
+// split of the cosine matrix (half the products). The products are
+// double-float (DfAcc: hi/lo float pairs with error-free transformations,
+// within ~1e-13 of float64); cf holds the matrix as [2][L][L] hi/lo floats.
 template <bool INV>
-__global__ void __launch_bounds__(kDctThreads) k_dct_lines(int m, int n, int batch, int cols, const double* __restrict__ c,
+__global__ void __launch_bounds__(kDctThreads) k_dct_lines(int m, int n, int batch, int cols, const float* __restrict__ cf,
                                                            const double* __restrict__ in, double* __restrict__ out) {
   extern __shared__ double dsm[];
   const int L = cols ? m : n;
   const long long mn = (long long)m * n;
   const long long n_lines = (long long)batch * (cols ? n : m);
   const long long l0 = (long long)blockIdx.x * kDctLines;
-  constexpr int S = kDctLines + 1;           // odd stride (in doubles): conflict-free rows of 32 lines
-  double* xs = dsm;                          // [L][S]
-  double* es = dsm + L * S;                  // [h][S] sums, then outputs
-  double* os = es + ((L + 1) / 2) * S;       // [h][S] differences
+  constexpr int S = kDctLines + 1;           // odd stride: conflict-free rows of 32 lines
+  double* xs = dsm;                          // [L][S] doubles
   const int h = L / 2, hc = (L + 1) / 2;
+  float* fs = reinterpret_cast<float*>(dsm + L * S);  // 4 hc S floats after xs
+  const float* ch = cf;
+  const float* cl = cf + (size_t)L * L;
   auto addr = [&](long long line, int e) -> long long {
     if (cols) {
       const long long f = line / n, col = line % n;
@@ -152,35 +192,56 @@ __global__ void __launch_bounds__(kDctThreads) k_dct_lines(int m, int n, int bat
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kDctThreads / 32;
+  auto split = [](double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+  };
   if (!INV) {
+    // Sums and differences of mirrored inputs, as hi/lo floats.
+    float* esh = fs;
+    float* esl = fs + hc * S;
+    float* osh = fs + 2 * hc * S;
+    float* osl = fs + 3 * hc * S;
     for (int i = warp; i < h; i += nw) {
       const double a = xs[i * S + lane], b = xs[(L - 1 - i) * S + lane];
-      es[i * S + lane] = a + b;
-      os[i * S + lane] = a - b;
+      split(a + b, esh[i * S + lane], esl[i * S + lane]);
+      split(a - b, osh[i * S + lane], osl[i * S + lane]);
     }
+    float mid_h = 0.f, mid_l = 0.f;
+    if (L & 1) split(xs[h * S + lane], mid_h, mid_l);
     __syncthreads();
-    // y[k] into xs (the inputs are no longer needed once es/os are built).
-    const double mid = (L & 1) ? xs[h * S + lane] : 0.0;
-    __syncthreads();
+    // y[k] into xs (the inputs are no longer needed).
     for (int k = warp; k < L; k += nw) {
-      const double* src = (k & 1) ? os : es;
-      const double* ck = c + (long long)k * L;
-      double acc = (L & 1) ? ck[h] * mid : 0.0;
-      for (int i = 0; i < h; ++i) acc = fma(ck[i], src[i * S + lane], acc);
-      xs[k * S + lane] = acc;
+      const float* sh = (k & 1) ? osh : esh;
+      const float* sl = (k & 1) ? osl : esl;
+      const float* ckh = ch + (long long)k * L;
+      const float* ckl = cl + (long long)k * L;
+      DfAcc acc;
+      if (L & 1) acc.add(ckh[h], ckl[h], mid_h, mid_l);
+      for (int i = 0; i < h; ++i) acc.add(ckh[i], ckl[i], sh[i * S + lane], sl[i * S + lane]);
+      float rh, rl;
+      acc.result(rh, rl);
+      xs[k * S + lane] = (double)rh + (double)rl;
     }
   } else {
-    for (int i = warp; i < hc; i += nw) {
-      double ev = 0.0, od = 0.0;
-      for (int k = 0; k < L; k += 2) ev = fma(c[(long long)k * L + i], xs[k * S + lane], ev);
-      for (int k = 1; k < L; k += 2) od = fma(c[(long long)k * L + i], xs[k * S + lane], od);
-      es[i * S + lane] = ev + od;         // x[i]
-      os[i * S + lane] = ev - od;         // x[L-1-i]
+    // The inputs as hi/lo floats.
+    float* xh = fs;
+    float* xl = fs + L * S;
+    for (int idx = threadIdx.x; idx < L * kDctLines; idx += kDctThreads) {
+      const int q = (idx / kDctLines) * S + idx % kDctLines;
+      split(xs[q], xh[q], xl[q]);
     }
     __syncthreads();
     for (int i = warp; i < hc; i += nw) {
-      xs[i * S + lane] = es[i * S + lane];
-      if (L - 1 - i != i) xs[(L - 1 - i) * S + lane] = os[i * S + lane];
+      DfAcc ev, od;
+      for (int k = 0; k < L; k += 2) ev.add(ch[(long long)k * L + i], cl[(long long)k * L + i], xh[k * S + lane], xl[k * S + lane]);
+      for (int k = 1; k < L; k += 2) od.add(ch[(long long)k * L + i], cl[(long long)k * L + i], xh[k * S + lane], xl[k * S + lane]);
+      float eh, el, oh, ol;
+      ev.result(eh, el);
+      od.result(oh, ol);
+      const double e = (double)eh + (double)el, o = (double)oh + (double)ol;
+      xs[i * S + lane] = e + o;                          // x[i]
+      if (L - 1 - i != i) xs[(L - 1 - i) * S + lane] = e - o;  // x[L-1-i]
     }
   }
   __syncthreads();
@@ -195,8 +256,8 @@ __global__ void __launch_bounds__(kDctThreads) k_dct_lines(int m, int n, int bat
 
 // One DCT pass over `batch` fields: forward (DCT-II) or inverse (DCT-III)
 // along rows (cols = 0, matrix c of size n) or columns (cols = 1, size m).
-static void dct_pass(int m, int n, int batch, bool inverse, int cols, const double* c, const double* in, double* out,
-                     cudaStream_t stream) {
+static void dct_pass(int m, int n, int batch, bool inverse, int cols, const double* c, const float* cf,
+                     const double* in, double* out, cudaStream_t stream) {
   const int L = cols ? m : n;
   const long long n_lines = (long long)batch * (cols ? n : m);
   if (L > kDctMaxLen) {
@@ -207,8 +268,8 @@ static void dct_pass(int m, int n, int batch, bool inverse, int cols, const doub
   }
   const size_t smem = (size_t)(L + 2 * ((L + 1) / 2)) * (kDctLines + 1) * sizeof(double);
   const unsigned grid = (unsigned)((n_lines + kDctLines - 1) / kDctLines);
-  if (inverse) k_dct_lines<true><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, c, in, out);
-  else k_dct_lines<false><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, c, in, out);
+  if (inverse) k_dct_lines<true><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, cf, in, out);
+  else k_dct_lines<false><<<grid, kDctThreads, smem, stream>>>(m, n, batch, cols, cf, in, out);
 }
 
 __global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, double* __restrict__ f2,
@@ -430,36 +491,6 @@ PIV_D double cta_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(~0u, t, o);
   return t;
 }
-
-// x -> (hi, lo) float pairs: hi = (float)x, lo = (float)(x - hi).
-__global__ void k_split_f64(int count, const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const float h = (float)x[t];
-  hi[t] = h;
-  lo[t] = (float)(x[t] - (double)h);
-}
-
-// Dot product of two hi/lo float vectors in float32 with error-free
-// transformations: every product's rounding error is kept (fma), the cross
-// terms a_hi b_lo + a_lo b_hi join a small-term sum, and the main sum is
-// compensated (TwoSum). The result, (hi, lo), is within ~1e-13 of the float64
-// dot product here (orthonormal cosine matrices, smooth fields), at a fraction
-// of the cost of float64 FMAs on this GPU.
-struct DfAcc {
-  float s = 0.f, c = 0.f;
-  PIV_D void add(float ah, float al, float bh, float bl) {
-    const float p = ah * bh;
-    c += fmaf(ah, bh, -p) + fmaf(ah, bl, al * bh);
-    const float t = s + p, bp = t - s;
-    c += (s - (t - bp)) + (p - bp);
-    s = t;
-  }
-  PIV_D void result(float& hi, float& lo) const {
-    hi = s + c;
-    lo = c - (hi - s);
-  }
-};
 
 struct DfMats {
   const float *cmh, *cml, *cnh, *cnl;  // [m][m], [n][n] hi and lo parts
@@ -787,6 +818,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
   const int bs = 256;
   k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, sc.cm);
   k_dct_matrix<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n, sc.cn);
+  k_split_f64<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m * m, sc.cm, sc.cmf, sc.cmf + m * m);
+  k_split_f64<<<(n * n + bs - 1) / bs, bs, 0, stream>>>(n * n, sc.cn, sc.cnf, sc.cnf + n * n);
   k_lambda2<<<(unsigned)((mn + bs - 1) / bs), bs, 0, stream>>>(m, n, sc.lam2, sc.lam2f);
   // Gather u and v as [pair][field][mn] into tmp.
   for (int f = 0; f < 2; ++f) {
@@ -794,8 +827,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
                       cudaMemcpyDeviceToDevice, stream);
   }
   // Forward DCT-II: rows then columns.
-  dct_pass(m, n, 2 * n_pairs, false, 0, sc.cn, sc.tmp, sc.fd, stream);
-  dct_pass(m, n, 2 * n_pairs, false, 1, sc.cm, sc.fd, sc.tmp, stream);
+  dct_pass(m, n, 2 * n_pairs, false, 0, sc.cn, sc.cnf, sc.tmp, sc.fd, stream);
+  dct_pass(m, n, 2 * n_pairs, false, 1, sc.cm, sc.cmf, sc.fd, sc.tmp, stream);
   int rc = check("smoothn forward dct");
   if (rc) return rc;
   // tmp now holds the DCT coefficients.
@@ -821,8 +854,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
   k_apply_gamma<<<dim3((unsigned)((2 * mn + bs - 1) / bs), (unsigned)n_pairs), bs, 0, stream>>>(mn, n_pairs, sc.lam2,
                                                                                                pvec, fixed_p, sc.tmp);
   // Inverse DCT (DCT-III): rows then columns.
-  dct_pass(m, n, 2 * n_pairs, true, 0, sc.cn, sc.tmp, sc.fd, stream);
-  dct_pass(m, n, 2 * n_pairs, true, 1, sc.cm, sc.fd, sc.tmp, stream);
+  dct_pass(m, n, 2 * n_pairs, true, 0, sc.cn, sc.cnf, sc.tmp, sc.fd, stream);
+  dct_pass(m, n, 2 * n_pairs, true, 1, sc.cm, sc.cmf, sc.fd, sc.tmp, stream);
   for (int f = 0; f < 2; ++f) {
     cudaMemcpy2DAsync(f == 0 ? u_out : v_out, mn * 8, sc.tmp + f * mn, 2 * mn * 8, mn * 8, n_pairs,
                       cudaMemcpyDeviceToDevice, stream);

@@ -146,7 +146,7 @@ def test_batch_rejects_configurations_with_different_passes():
     kw = dict(synthetic.CONFIGS[4]["piv"])
     mss = kw.pop("min_search_size")
     a = PIVGPU((128, 160), mss, **kw, dft="tensor")
-    b = PIVGPU((96, 96), 2 * mss, **kw, dft="tensor")  # other search sizes
+    b = PIVGPU((160, 224), 2 * mss, **kw, dft="tensor")  # other search sizes
     c = PIVGPU((96, 96), mss, **kw, dft="fft")         # other engine
     for other in (b, c):
         (ca, ka), (cb, kb) = a._config(_lib.PIXEL["u8"], 2), other._config(_lib.PIXEL["u8"], 2)
