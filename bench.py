@@ -288,6 +288,28 @@ def ncu_traffic():
 # ---------------------------------------------------------------------------
 # Arms.
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# Ranks (replicas only: each rank processes its own pairs; the process group
+# only aligns the timed regions and takes the slowest rank's time).
+# ---------------------------------------------------------------------------
+def shard_pairs(rank, batch, distinct=DISTINCT):
+    """Indices of the distinct synthetic pairs rank `rank` processes: batch
+    pairs starting at rank * batch, cycling through the distinct pairs."""
+    return [(rank * batch + k) % distinct for k in range(batch)]
+
+
+def max_over_ranks(value, dist=None):
+    """The largest `value` over the ranks of the default process group (the
+    value itself without one)."""
+    if dist is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -338,7 +360,7 @@ def run_gpu(args):
     lib = _lib.load()
     B = args.pairs
     pairs = generate_pairs(DISTINCT)
-    idx = [(rank * B + k) % DISTINCT for k in range(B)]
+    idx = shard_pairs(rank, B)
     host_a = np.stack([pairs[i][0] for i in idx])
     host_b = np.stack([pairs[i][1] for i in idx])
     fa = torch.as_tensor(host_a).cuda()
@@ -387,10 +409,7 @@ def run_gpu(args):
     sampler.start()
     ms, kernels, (u_dev, v_dev) = graph_time(proc)
     clocks = sampler.stop()
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     ms_step = ms / args.steps
     value = B * world / (ms_step * 1e-3)
     windows_per_pair = sum(f.n_wins for f in proc.piv_fields)
@@ -399,10 +418,7 @@ def run_gpu(args):
     if args.dft != "fft" and not args.no_plain:
         proc_plain = make("fft")
         ms_p, _, _ = graph_time(proc_plain)
-        if dist:
-            t = torch.tensor([ms_p], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms_p = float(t.item())
+        ms_p = max_over_ranks(ms_p, dist)
         plain = {"pairs_per_s": B * world / (ms_p / args.steps * 1e-3), "ms_per_step": ms_p / args.steps}
         plain["chosen_over_plain"] = value / plain["pairs_per_s"]
     split = None
@@ -410,10 +426,7 @@ def run_gpu(args):
     if args.dft == "tensor" and not args.no_split:
         proc_split = make("tensor_split")
         ms_s, _, _ = graph_time(proc_split)
-        if dist:
-            t = torch.tensor([ms_s], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms_s = float(t.item())
+        ms_s = max_over_ranks(ms_s, dist)
         split = {"pairs_per_s": B * world / (ms_s / args.steps * 1e-3), "ms_per_step": ms_s / args.steps}
         if plain:
             split["over_plain"] = split["pairs_per_s"] / plain["pairs_per_s"]
@@ -487,10 +500,7 @@ def run_gpu(args):
     for res_u, res_v in proc.run_batches((na, nb) for _ in range(args.steps)):
         pass
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist)
     device_status = proc.status()  # PIV_OK unless a bounded device-side wait gave up
     m, n = proc.piv_fields[-1].field_shape
     e2e = {"value": B * world * args.steps / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": int(2 * B * FRAME[0] * FRAME[1]),
