@@ -166,6 +166,12 @@ int piv_plan_variant_name(const piv_plan* plan, int iter, int variant, char* buf
 int piv_plan_set_variant(piv_plan* plan, int iter, int variant);
 /* Forgets the process-wide autotuner results. */
 void piv_autotune_cache_clear(void);
+/* Failure-detection self test: one bounded mbarrier wait that no arrival
+ * completes (the primitive behind every tensor-core completion wait), run for
+ * max_polls polls; *status receives the status word the kernel wrote,
+ * PIV_E_TIMEOUT. The context stays usable afterwards. Synchronises `stream`.
+ * No counterpart in the reference. */
+int piv_selftest_bounded_wait(unsigned int max_polls, int* status, void* stream);
 
 /* Multi-size batch: a submission of pairs of several frame sizes processed
  * together (the reference processes one pair per PIVGPU call,

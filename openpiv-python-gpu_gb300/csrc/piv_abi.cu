@@ -1086,6 +1086,19 @@ int piv_plan_set_variant(piv_plan* p, int iter, int variant) {
   return PIV_OK;
 }
 
+int piv_selftest_bounded_wait(unsigned int max_polls, int* status, void* stream_ptr) {
+  if (!status) return set_error(PIV_E_ARG, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream_ptr;
+  int* dev = nullptr;
+  PIV_TRY(cuda_ok(cudaMallocAsync((void**)&dev, sizeof(int), s), "cudaMallocAsync"));
+  cudaMemsetAsync(dev, 0, sizeof(int), s);
+  int rc = bounded_wait_probe(max_polls, dev, s);
+  if (rc == PIV_OK) rc = cuda_ok(cudaMemcpyAsync(status, dev, sizeof(int), cudaMemcpyDeviceToHost, s), "status copy");
+  cudaFreeAsync(dev, s);
+  if (rc == PIV_OK) rc = cuda_ok(cudaStreamSynchronize(s), "stream synchronize");
+  return rc;
+}
+
 void piv_autotune_cache_clear(void) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   g_tune_cache.clear();

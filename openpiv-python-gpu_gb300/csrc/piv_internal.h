@@ -73,6 +73,8 @@ int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t 
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode);
 int correlate_tensor_variant_count(const CorrArgs& a, int dft_mode);
 int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int variant, int* per_sm, int* async);
+// One bounded mbarrier wait that nothing completes; writes PIV_E_TIMEOUT to *status_dev.
+int bounded_wait_probe(uint32_t max_polls, int* status_dev, cudaStream_t stream);
 
 // Deformation.
 struct DeformArgs {

@@ -1332,6 +1332,23 @@ static bool tc64_aligned(const CorrArgs& a) { return a.pixel_type == PIV_PIXEL_U
 // the 16/32-px engine).
 static bool tc_aligned(const CorrArgs& a) { return a.pixel_type == PIV_PIXEL_F32 && all_rows_aligned(a, 4); }
 
+// One bounded wait on an mbarrier that no arrival completes: the primitive
+// behind every tcgen05 completion wait of the correlation kernels, run until
+// it gives up. Writes the status word the kernels would set.
+__global__ void k_wait_probe(uint32_t max_polls, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  const bool ok = tc::mbar_wait_bounded(&bar, 0, max_polls);
+  if (threadIdx.x == 0) *status = ok ? PIV_OK : PIV_E_TIMEOUT;
+}
+
+int bounded_wait_probe(uint32_t max_polls, int* status_dev, cudaStream_t stream) {
+  k_wait_probe<<<1, 32, 0, stream>>>(max_polls, status_dev);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_wait_probe launch");
+}
+
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
   if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT) return false;
   if (a.n_segs < 0 || a.n_segs > kMaxCorrSegs) return false;

@@ -75,6 +75,7 @@ _SIGNATURES = {
     "piv_plan_variant_name": (c_int, [c_void_p, c_int, c_int, ctypes.c_char_p, c_size_t]),
     "piv_plan_set_variant": (c_int, [c_void_p, c_int, c_int]),
     "piv_autotune_cache_clear": (None, []),
+    "piv_selftest_bounded_wait": (c_int, [ctypes.c_uint, POINTER(c_int), c_void_p]),
     "piv_batch_create": (c_int, [POINTER(PivConfig), c_int, POINTER(c_void_p)]),
     "piv_batch_destroy": (None, [c_void_p]),
     "piv_batch_plan": (c_int, [c_void_p, c_int, POINTER(c_void_p)]),

@@ -522,3 +522,14 @@ def test_tensor_pipeline_accuracy():
     assert rms_t < 0.01
     assert rms_s < 1e-4
     assert rms_f < 1e-4
+
+
+def test_bounded_wait_gives_up_and_leaves_the_context_usable(env):
+    """A tensor-core completion wait that nothing completes gives up after its
+    poll limit and reports PIV_E_TIMEOUT through the status word (no trap, no
+    hang); a correlation on the same context afterwards is still exact."""
+    torch, _lib, lib = env
+    st = ctypes.c_int(0)
+    _lib.check(lib.piv_selftest_bounded_wait(2000, ctypes.byref(st), _stream(torch)))
+    assert st.value == _lib.PIV_E_TIMEOUT
+    test_tensor_maps_match_oracle(env, 16, "tensor", 5e-3)
