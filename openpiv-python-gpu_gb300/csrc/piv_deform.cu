@@ -541,7 +541,10 @@ static constexpr int kPfK = 12;
 static constexpr int kPfT = 64;                    // output tile edge
 static constexpr int kPfR = kPfT + 2 * kPfK;       // region edge (a multiple of 8)
 static_assert(kPfR % 8 == 0, "the recursions run in chunks of eight");
-static constexpr int kPfS = kPfR + 1;              // odd row stride: conflict-free row and column walks
+// Row stride: a multiple of four floats (16-byte rows for vector access) whose
+// rows fall on distinct banks for eight consecutive rows (92 = 28 mod 32), and
+// consecutive columns on consecutive banks.
+static constexpr int kPfS = kPfR + 4;
 static constexpr float kPole = -0.26794919243112270f;  // sqrt(3) - 2
 
 // Mirror ('d c b | a b c d | c b a') index for any integer q.
@@ -578,9 +581,9 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
     for (int u = 0; u < (kTotal + 127) / 128; ++u) {
       const int e = threadIdx.x + 128 * u;
       if (e < kTotal) {
-        float* d = reg + (e / kWords) * kPfS + 4 * (e % kWords);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) d[k] = (float)((wv[u] >> (8 * k)) & 0xffu);
+        const uint32_t w = wv[u];
+        *reinterpret_cast<float4*>(reg + (e / kWords) * kPfS + 4 * (e % kWords)) =
+            make_float4((float)(w & 0xffu), (float)((w >> 8) & 0xffu), (float)((w >> 16) & 0xffu), (float)(w >> 24));
       }
     }
   } else {
@@ -608,71 +611,59 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
   }
   __syncthreads();
   const float z = kPole;
-  // The recursions run in chunks of eight: the chunk's shared-memory reads
-  // are issued together, then the dependent chain runs in registers.
+  // Each line runs in registers: loaded once, both recursions, stored once.
   // Along x: one thread per region row; only the tile's columns are kept.
   if (threadIdx.x < kPfR) {
-    float* row = reg + threadIdx.x * kPfS;
+    float v[kPfR];
+    const float4* rp = reinterpret_cast<const float4*>(reg + threadIdx.x * kPfS);
+#pragma unroll
+    for (int q = 0; q < kPfR / 4; ++q) {
+      const float4 t = rp[q];
+      v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+    }
     float c = 0.f;
-    for (int k0 = 0; k0 < kPfR; k0 += 8) {
-      float v[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = row[k0 + k];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        c = fmaf(z, c, v[k]);
-        v[k] = c;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) row[k0 + k] = v[k];
+    for (int k = 0; k < kPfR; ++k) {
+      c = fmaf(z, c, v[k]);
+      v[k] = c;
     }
     float d = 0.f;
-    for (int k0 = kPfR - 8; k0 + 8 > kPfK; k0 -= 8) {
-      float v[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = row[k0 + k];
-#pragma unroll
-      for (int k = 7; k >= 0; --k) {
-        d = z * (d - v[k]);
-        v[k] = d;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) row[k0 + k] = v[k];
+    for (int k = kPfR - 1; k >= kPfK; --k) {
+      d = z * (d - v[k]);
+      v[k] = d;
     }
+    float4* wp = reinterpret_cast<float4*>(reg + threadIdx.x * kPfS + kPfK);
+#pragma unroll
+    for (int q = 0; q < kPfT / 4; ++q)
+      wp[q] = make_float4(v[kPfK + 4 * q], v[kPfK + 4 * q + 1], v[kPfK + 4 * q + 2], v[kPfK + 4 * q + 3]);
   }
   __syncthreads();
   // Along y: one thread per tile column; writes the tile with the gain 6 * 6.
   if (threadIdx.x < kPfT) {
     const int col = kPfK + threadIdx.x;
+    float v[kPfR];
+#pragma unroll
+    for (int k = 0; k < kPfR; ++k) v[k] = reg[k * kPfS + col];
     float c = 0.f;
-    for (int k0 = 0; k0 < kPfR; k0 += 8) {
-      float v[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = reg[(k0 + k) * kPfS + col];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        c = fmaf(z, c, v[k]);
-        v[k] = c;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) reg[(k0 + k) * kPfS + col] = v[k];
+    for (int k = 0; k < kPfR; ++k) {
+      c = fmaf(z, c, v[k]);
+      v[k] = c;
     }
     float d = 0.f;
+#pragma unroll
+    for (int k = kPfR - 1; k >= kPfK; --k) {
+      d = z * (d - v[k]);
+      v[k] = d;
+    }
     const int gx = x0 + threadIdx.x, os = W + 2 * pad;
-    float* dst = out + (long long)blockIdx.z * (H + 2 * pad) * os + (long long)pad * os + pad + gx;
-    for (int k0 = kPfR - 8; k0 + 8 > kPfK; k0 -= 8) {
-      float v[8];
+    if (gx < W) {
+      float* dst = out + (long long)blockIdx.z * (H + 2 * pad) * os + (long long)pad * os + pad + gx;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = reg[(k0 + k) * kPfS + col];
-#pragma unroll
-      for (int k = 7; k >= 0; --k) {
-        d = z * (d - v[k]);
-        v[k] = d;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int gy = y0 + k0 + k - kPfK;
-        if (k0 + k >= kPfK && k0 + k < kPfK + kPfT && gx < W && gy < H) dst[(long long)gy * os] = 36.0f * v[k];
+      for (int k = kPfK; k < kPfK + kPfT; ++k) {
+        const int gy = y0 + k - kPfK;
+        if (gy < H) dst[(long long)gy * os] = 36.0f * v[k];
       }
     }
   }
