@@ -484,6 +484,12 @@ def run_gpu(args):
     if on_tensor:
         roofline["executed_tflops"] = (n_win * tc_executed_flops(f.search_size, N, args.dft == "tensor_split")
                                        / (corr[dom] * 1e-3) / 1e12)
+        roofline["executed_frac"] = roofline["executed_tflops"] / peak
+    if roofline["traffic"]:
+        # The same launch against the HBM roofline: DRAM bytes / launch time.
+        hbm = peaks.get("hbm_gbs")
+        roofline["dram_gbs"] = roofline["traffic"] / (corr[dom] * 1e-3) / 1e9
+        roofline["dram_frac"] = roofline["dram_gbs"] / hbm if hbm else None
 
     # End to end through the public API: pinned host frames in, fields out
     # (PIVGPU.run_batches: two plans on two streams, so that a batch's upload
