@@ -266,13 +266,13 @@ PIV_D AxisWeight axis_weight(int q, int ss, int off, int sp, int len) {
 }
 
 static constexpr int kDeformThreads = 256;
-static constexpr int kDeformRows = 4;                       // image rows per CTA
+static constexpr int kDeformRows = 8;                       // image rows per CTA
 // Field columns / rows one CTA can touch (spacing >= 1).
 static constexpr int kDeformMaxCols = kDeformThreads + 2;
 static constexpr int kDeformMaxGridRows = kDeformRows + 1;
 
-// One thread per pixel column of a 4-row x 256-pixel block; each thread
-// handles the block's four rows. The predictor (float32; the reference
+// One thread per pixel column of an 8-row x 256-pixel block; each thread
+// handles the block's eight rows. The predictor (float32; the reference
 // evaluates it in float64 and casts to the frame type, a difference of one or
 // two float32 ulps) is staged as the field rows and columns the block touches
 // and interpolated along y, then x. Frame A is sampled at x + up*dta and frame
@@ -417,8 +417,8 @@ PIV_D float sample_cubic32p(const float* __restrict__ coef, int S, int W, int H,
 }
 
 // k_deform for the common case: float32 fields, cubic B-spline sampling of
-// both frames (0 < deforming_par < 1). The row weights of the block's four
-// rows are computed once per CTA; pixel offsets are 32-bit.
+// both frames (0 < deforming_par < 1). The row weights of the block's rows
+// are computed once per CTA; pixel offsets are 32-bit.
 template <bool PADDED>
 __global__ void __launch_bounds__(kDeformThreads) k_deform_cubic(DeformArgs a, AxisMap ax, AxisMap ay, float dta,
                                                                  float dtb) {

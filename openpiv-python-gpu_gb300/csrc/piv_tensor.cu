@@ -68,8 +68,10 @@ struct TcLayout {
   static constexpr int CH = SS / 4;                     // 16-byte chunks per staged row
   // Threads per TMEM lane: with two, every phase splits its frames, columns
   // or row tiles between the pair, which doubles the warps an SM holds when
-  // the TMEM allows only two CTAs.
-  static constexpr int TPL = SS == 32 ? 2 : 1;
+  // the TMEM allows only two CTAs (ss 32) or the shared memory three (the
+  // split form of ss 16). The plain ss-16 form keeps one: at four CTAs per SM
+  // two threads per lane would have 64 registers each and spill.
+  static constexpr int TPL = SS == 32 || SPLIT ? 2 : 1;
   static constexpr int NT = 128 * TPL;
   // CTAs per SM the register budget is compiled for (shared memory limits the
   // split form to 3 CTAs for ss 16 and 1 for ss 32).
