@@ -524,25 +524,35 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     // (w, c) of tile e (k = 2c) and tile o (k = 2c + 1).
     {
       const int w = t / SS, y = t % SS;
-#pragma unroll
-      for (int fi = 0; fi < 2 / TPL; ++fi) {
-        const int f = TPL == 2 ? half : fi;
-        float v[N];
-#pragma unroll
-        for (int c0 = 0; c0 < N; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + f * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-        tc::tmem_ld_wait();
-        tc::reg_fence(v);
+      // The thread's columns as chunks of 16 (frame-major); chunk k + 1 is
+      // loaded while chunk k is converted.
+      constexpr int K = (2 / TPL) * N / 16;
+      auto col_src = [&](int k) -> uint32_t {
+        const int cs = 16 * k, f = TPL == 2 ? half : cs / N;
+        return tmem + lane_sel + f * N + cs % N;
+      };
+      auto put = [&](int k, const float (&vals)[16]) {
+        const int cs = 16 * k, f = TPL == 2 ? half : cs / N, c0 = (cs % N) / 2;
 #pragma unroll
         for (int rt = 0; rt < 2; ++rt) {
-          unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
+          float v8[8];
 #pragma unroll
-          for (int c0 = 0; c0 < HN; c0 += 8) {
-            float v8[8];
+          for (int j = 0; j < 8; ++j) v8[j] = vals[2 * j + rt];
+          st8s<SPLIT>(sm + L::OP + (f * 2 + rt) * L::A2_BYTES, L::NOP, off_mn(w * HN + c0, y, 128), v8);
+        }
+      };
+      float b0[16], b1[16];
+      tc::tmem_ld16(col_src(0), b0);
+      tc::tmem_ld_wait();
+      tc::reg_fence(b0);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
-            st8s<SPLIT>(dst, L::NOP, off_mn(w * HN + c0, y, 128), v8);
-          }
+      for (int k = 0; k < K; ++k) {
+        if (k + 1 < K) tc::tmem_ld16(col_src(k + 1), (k & 1) ? b0 : b1);
+        put(k, (k & 1) ? b1 : b0);
+        if (k + 1 < K) {
+          tc::tmem_ld_wait();
+          if (k & 1) tc::reg_fence(b0);
+          else tc::reg_fence(b1);
         }
       }
     }
