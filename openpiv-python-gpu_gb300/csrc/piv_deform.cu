@@ -565,49 +565,44 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
   const int x0 = blockIdx.x * kPfT, y0 = blockIdx.y * kPfT;
   const long long fbase = (long long)blockIdx.z * H * W;
   const P* src = in + fbase;
-  constexpr int kElems = kPfR * kPfR;
   const bool interior = x0 >= kPfK && y0 >= kPfK && x0 + kPfT + kPfK <= W && y0 + kPfT + kPfK <= H;
   if (sizeof(P) == 1 && interior && (W & 3) == 0 && ((uintptr_t)in & 3) == 0) {
     // 8-bit frames away from the edges: the region's rows start on 4-byte
-    // boundaries (x0 - 12 is a multiple of 4), so each thread reads whole words.
-    constexpr int kWords = kPfR / 4, kTotal = kPfR * kWords;
-    const uint32_t* wsrc = reinterpret_cast<const uint32_t*>(src + (long long)(y0 - kPfK) * W + (x0 - kPfK));
-    const int wstride = W / 4;
-    uint32_t wv[(kTotal + 127) / 128];
+    // boundaries (x0 - 12 is a multiple of 4). Thread t < 110 converts word
+    // column t % 22 of region rows t / 22, t / 22 + 5, ...: its addresses
+    // advance by a fixed stride, all of its loads in flight together.
+    constexpr int kWords = kPfR / 4, kGroups = 128 / kWords, kIters = (kPfR + kGroups - 1) / kGroups;
+    const int t = threadIdx.x;
+    if (t < kWords * kGroups) {
+      const int wc = t % kWords, r0 = t / kWords;
+      const long long wstep = (long long)kGroups * (W / 4);
+      const uint32_t* wsrc =
+          reinterpret_cast<const uint32_t*>(src + (long long)(y0 - kPfK + r0) * W + (x0 - kPfK)) + wc;
+      float* dst = reg + r0 * kPfS + 4 * wc;
+      uint32_t wv[kIters];
 #pragma unroll
-    for (int u = 0; u < (kTotal + 127) / 128; ++u) {
-      const int e = threadIdx.x + 128 * u;
-      wv[u] = e < kTotal ? __ldg(wsrc + (long long)(e / kWords) * wstride + e % kWords) : 0u;
-    }
+      for (int k = 0; k < kIters; ++k) wv[k] = r0 + kGroups * k < kPfR ? __ldg(wsrc + k * wstep) : 0u;
 #pragma unroll
-    for (int u = 0; u < (kTotal + 127) / 128; ++u) {
-      const int e = threadIdx.x + 128 * u;
-      if (e < kTotal) {
-        const uint32_t w = wv[u];
-        *reinterpret_cast<float4*>(reg + (e / kWords) * kPfS + 4 * (e % kWords)) =
-            make_float4((float)(w & 0xffu), (float)((w >> 8) & 0xffu), (float)((w >> 16) & 0xffu), (float)(w >> 24));
-      }
+      for (int k = 0; k < kIters; ++k)
+        if (r0 + kGroups * k < kPfR) {
+          const uint32_t w = wv[k];
+          *reinterpret_cast<float4*>(dst + k * kGroups * kPfS) = make_float4(
+              (float)(w & 0xffu), (float)((w >> 8) & 0xffu), (float)((w >> 16) & 0xffu), (float)(w >> 24));
+        }
     }
   } else {
-    // Any pixel type, mirrored edges: eight scalar loads per thread in flight.
-    for (int e0 = threadIdx.x; e0 < kElems; e0 += 128 * 8) {
-      float v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + 128 * u;
-        v[u] = 0.f;
-        if (e < kElems) {
-          const int ry = e / kPfR, rx = e % kPfR;
-          int gy = y0 - kPfK + ry, gx = x0 - kPfK + rx;
-          if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
-          if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
-          v[u] = (float)__ldg(src + (long long)gy * W + gx);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + 128 * u;
-        if (e < kElems) reg[(e / kPfR) * kPfS + e % kPfR] = v[u];
+    // Any pixel type, mirrored edges: thread t < 88 holds region column t (its
+    // mirrored frame column found once) and walks the region's rows.
+    const int t = threadIdx.x;
+    if (t < kPfR) {
+      int gx = x0 - kPfK + t;
+      if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
+      const P* col = src + gx;
+#pragma unroll 8
+      for (int r = 0; r < kPfR; ++r) {
+        int gy = y0 - kPfK + r;
+        if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
+        reg[r * kPfS + t] = (float)__ldg(col + (long long)gy * W);
       }
     }
   }
