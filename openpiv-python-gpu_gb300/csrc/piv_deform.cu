@@ -535,9 +535,13 @@ int deform(const DeformArgs& a, cudaStream_t stream) {
 // frame. Each CTA filters a 64 x 64 output tile from a 12-pixel mirrored halo
 // in shared memory with the causal / anti-causal recursions
 //   c+[k] = s[k] + z c+[k-1],   c-[k] = z (c-[k+1] - c+[k]),   c = 6 c-
-// started from zero at the halo's outer edge: the start-up error reaching the
-// tile is below |z|^12 / (1 - |z|) < 2e-7 of the signal, under float32
-// rounding of the recursion itself.
+// started from zero 12 samples before the first value that is kept: the
+// start-up error is below |z|^12 / (1 - |z|) < 2e-7 of the signal, under
+// float32 rounding of the recursion itself. Each line (a region row, then a
+// tile column) is split between two threads: the first keeps outputs
+// [12, 44) from recursions over samples [0, 56), the second outputs [44, 76)
+// from samples [32, 88), so that both recursions start 12 samples outside
+// the half they keep.
 // ---------------------------------------------------------------------------
 static constexpr int kPfK = 12;
 static constexpr int kPfT = 64;                    // output tile edge
@@ -547,6 +551,9 @@ static_assert(kPfR % 8 == 0, "the recursions run in chunks of eight");
 // rows fall on distinct banks for eight consecutive rows (92 = 28 mod 32), and
 // consecutive columns on consecutive banks.
 static constexpr int kPfS = kPfR + 4;
+static constexpr int kPfL = kPfT / 2 + 2 * kPfK;   // samples of a half line's recursions (56)
+static constexpr int kPfNT = 2 * kPfR + 16;        // threads: two per region row, in whole warps
+static_assert(kPfNT % 32 == 0 && kPfL % 4 == 0, "prefilter launch shape");
 static constexpr float kPole = -0.26794919243112270f;  // sqrt(3) - 2
 
 // Mirror ('d c b | a b c d | c b a') index for any integer q.
@@ -558,21 +565,39 @@ PIV_D int mirror_any(int q, int n) {
   return q < n ? q : p - q;
 }
 
+// Causal then anti-causal recursion over a half line v[0, kPfL) (both started
+// from zero); v[kPfK, kPfL) then holds c-.
+PIV_D void half_line(float (&v)[kPfL]) {
+  const float z = kPole;
+  float c = 0.f;
+#pragma unroll
+  for (int k = 0; k < kPfL; ++k) {
+    c = fmaf(z, c, v[k]);
+    v[k] = c;
+  }
+  float d = 0.f;
+#pragma unroll
+  for (int k = kPfL - 1; k >= kPfK; --k) {
+    d = z * (d - v[k]);
+    v[k] = d;
+  }
+}
+
 template <typename P>
-__global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __restrict__ in, float* __restrict__ out,
-                                                   int pad) {
-  __shared__ float reg[kPfR * kPfS];
+__global__ void __launch_bounds__(kPfNT) k_prefilter(int H, int W, const P* __restrict__ in, float* __restrict__ out,
+                                                     int pad) {
+  __shared__ __align__(16) float reg[kPfR * kPfS];
   const int x0 = blockIdx.x * kPfT, y0 = blockIdx.y * kPfT;
   const long long fbase = (long long)blockIdx.z * H * W;
   const P* src = in + fbase;
+  const int t = threadIdx.x;
   const bool interior = x0 >= kPfK && y0 >= kPfK && x0 + kPfT + kPfK <= W && y0 + kPfT + kPfK <= H;
   if (sizeof(P) == 1 && interior && (W & 3) == 0 && ((uintptr_t)in & 3) == 0) {
     // 8-bit frames away from the edges: the region's rows start on 4-byte
-    // boundaries (x0 - 12 is a multiple of 4). Thread t < 110 converts word
-    // column t % 22 of region rows t / 22, t / 22 + 5, ...: its addresses
+    // boundaries (x0 - 12 is a multiple of 4). Thread t < 176 converts word
+    // column t % 22 of region rows t / 22, t / 22 + 8, ...: its addresses
     // advance by a fixed stride, all of its loads in flight together.
-    constexpr int kWords = kPfR / 4, kGroups = 128 / kWords, kIters = (kPfR + kGroups - 1) / kGroups;
-    const int t = threadIdx.x;
+    constexpr int kWords = kPfR / 4, kGroups = kPfNT / kWords, kIters = (kPfR + kGroups - 1) / kGroups;
     if (t < kWords * kGroups) {
       const int wc = t % kWords, r0 = t / kWords;
       const long long wstep = (long long)kGroups * (W / 4);
@@ -590,76 +615,55 @@ __global__ void __launch_bounds__(128) k_prefilter(int H, int W, const P* __rest
               (float)(w & 0xffu), (float)((w >> 8) & 0xffu), (float)((w >> 16) & 0xffu), (float)(w >> 24));
         }
     }
-  } else {
-    // Any pixel type, mirrored edges: thread t < 88 holds region column t (its
-    // mirrored frame column found once) and walks the region's rows.
-    const int t = threadIdx.x;
-    if (t < kPfR) {
-      int gx = x0 - kPfK + t;
-      if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
-      const P* col = src + gx;
-#pragma unroll 8
-      for (int r = 0; r < kPfR; ++r) {
-        int gy = y0 - kPfK + r;
-        if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
-        reg[r * kPfS + t] = (float)__ldg(col + (long long)gy * W);
-      }
+  } else if (t < 2 * kPfR) {
+    // Any pixel type, mirrored edges: thread t holds region column t % 88 (its
+    // mirrored frame column found once) and walks half of the region's rows.
+    const int rc = t % kPfR, r0 = (t / kPfR) * (kPfR / 2);
+    int gx = x0 - kPfK + rc;
+    if (gx < 0 || gx >= W) gx = mirror_any(gx, W);
+    const P* col = src + gx;
+#pragma unroll 4
+    for (int r = r0; r < r0 + kPfR / 2; ++r) {
+      int gy = y0 - kPfK + r;
+      if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
+      reg[r * kPfS + rc] = (float)__ldg(col + (long long)gy * W);
     }
   }
   __syncthreads();
-  const float z = kPole;
-  // Each line runs in registers: loaded once, both recursions, stored once.
-  // Along x: one thread per region row; only the tile's columns are kept.
-  if (threadIdx.x < kPfR) {
-    float v[kPfR];
-    const float4* rp = reinterpret_cast<const float4*>(reg + threadIdx.x * kPfS);
+  // Along x: thread t < 176 takes half t / 88 of region row t % 88; every
+  // thread reads its samples before any writes its outputs back in place.
+  float v[kPfL];
+  const int xr = t % kPfR, xs = (t / kPfR) * (kPfR - kPfL);
+  if (t < 2 * kPfR) {
+    const float4* rp = reinterpret_cast<const float4*>(reg + xr * kPfS + xs);
 #pragma unroll
-    for (int q = 0; q < kPfR / 4; ++q) {
-      const float4 t = rp[q];
-      v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+    for (int q = 0; q < kPfL / 4; ++q) {
+      const float4 u = rp[q];
+      v[4 * q] = u.x; v[4 * q + 1] = u.y; v[4 * q + 2] = u.z; v[4 * q + 3] = u.w;
     }
-    float c = 0.f;
+    half_line(v);
+  }
+  __syncthreads();
+  if (t < 2 * kPfR) {
+    float4* wp = reinterpret_cast<float4*>(reg + xr * kPfS + xs + kPfK);
 #pragma unroll
-    for (int k = 0; k < kPfR; ++k) {
-      c = fmaf(z, c, v[k]);
-      v[k] = c;
-    }
-    float d = 0.f;
-#pragma unroll
-    for (int k = kPfR - 1; k >= kPfK; --k) {
-      d = z * (d - v[k]);
-      v[k] = d;
-    }
-    float4* wp = reinterpret_cast<float4*>(reg + threadIdx.x * kPfS + kPfK);
-#pragma unroll
-    for (int q = 0; q < kPfT / 4; ++q)
+    for (int q = 0; q < kPfT / 8; ++q)
       wp[q] = make_float4(v[kPfK + 4 * q], v[kPfK + 4 * q + 1], v[kPfK + 4 * q + 2], v[kPfK + 4 * q + 3]);
   }
   __syncthreads();
-  // Along y: one thread per tile column; writes the tile with the gain 6 * 6.
-  if (threadIdx.x < kPfT) {
-    const int col = kPfK + threadIdx.x;
-    float v[kPfR];
+  // Along y: thread t < 128 takes half t / 64 of tile column t % 64; writes
+  // its 32 rows of the tile with the gain 6 * 6.
+  if (t < 2 * kPfT) {
+    const int tc = t % kPfT, ys = (t / kPfT) * (kPfR - kPfL), col = kPfK + tc;
 #pragma unroll
-    for (int k = 0; k < kPfR; ++k) v[k] = reg[k * kPfS + col];
-    float c = 0.f;
-#pragma unroll
-    for (int k = 0; k < kPfR; ++k) {
-      c = fmaf(z, c, v[k]);
-      v[k] = c;
-    }
-    float d = 0.f;
-#pragma unroll
-    for (int k = kPfR - 1; k >= kPfK; --k) {
-      d = z * (d - v[k]);
-      v[k] = d;
-    }
-    const int gx = x0 + threadIdx.x, os = W + 2 * pad;
+    for (int k = 0; k < kPfL; ++k) v[k] = reg[(ys + k) * kPfS + col];
+    half_line(v);
+    const int gx = x0 + tc, os = W + 2 * pad;
     if (gx < W) {
       float* dst = out + (long long)blockIdx.z * (H + 2 * pad) * os + (long long)pad * os + pad + gx;
 #pragma unroll
-      for (int k = kPfK; k < kPfK + kPfT; ++k) {
-        const int gy = y0 + k - kPfK;
+      for (int k = kPfK; k < kPfK + kPfT / 2; ++k) {
+        const int gy = y0 + ys + k - kPfK;
         if (gy < H) dst[(long long)gy * os] = 36.0f * v[k];
       }
     }
@@ -699,10 +703,10 @@ int spline_prefilter(int H, int W, int n_frames, const void* frames, int pixel_t
   if (pad != 0 && pad != kCoefPad) return set_error(PIV_E_ARG, "spline prefilter: pad must be 0 or %d", kCoefPad);
   const dim3 grid((unsigned)((W + kPfT - 1) / kPfT), (unsigned)((H + kPfT - 1) / kPfT), (unsigned)n_frames);
   switch (pixel_type) {
-    case PIV_PIXEL_U8: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint8_t*)frames, coef, pad); break;
-    case PIV_PIXEL_U16: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const uint16_t*)frames, coef, pad); break;
-    case PIV_PIXEL_F32: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const float*)frames, coef, pad); break;
-    default: k_prefilter<<<grid, 128, 0, stream>>>(H, W, (const double*)frames, coef, pad); break;
+    case PIV_PIXEL_U8: k_prefilter<<<grid, kPfNT, 0, stream>>>(H, W, (const uint8_t*)frames, coef, pad); break;
+    case PIV_PIXEL_U16: k_prefilter<<<grid, kPfNT, 0, stream>>>(H, W, (const uint16_t*)frames, coef, pad); break;
+    case PIV_PIXEL_F32: k_prefilter<<<grid, kPfNT, 0, stream>>>(H, W, (const float*)frames, coef, pad); break;
+    default: k_prefilter<<<grid, kPfNT, 0, stream>>>(H, W, (const double*)frames, coef, pad); break;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_cuda_error(e, "k_prefilter launch");
