@@ -370,65 +370,165 @@ PIV_D double gcv_score_fast(const GcvEval& g, double p, double* red) {
   return trss / g.n_finite / (q * q) / g.n_fields;
 }
 
+// One CTA per pair. Every thread takes part in the sums of each score; the
+// search itself (scan bookkeeping, gradient test, Brent's iteration: scalar
+// float64 work) runs in warp 0 alone, which announces each next point as
+// s = 10^p in shared memory. Float64 runs at a small fraction of the float32
+// rate on this GPU, so the search is not repeated by all 16 warps. The
+// operations and their order are those of gcv_score / gcv_score_fast.
 __global__ void __launch_bounds__(kGcvThreads)
 k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2,
       const float* __restrict__ f2f, const float* __restrict__ lam2f, double pmin, double pmax,
       double* __restrict__ p_out) {
-  __shared__ double red[65];
+  __shared__ double red[64];
+  __shared__ double sh_s;  // 10^p of the next score
+  __shared__ int sh_go;    // warp 0's decision for the next step
   const int pair = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const bool w0 = warp == 0;
   const long long mn = (long long)m * n;
-  GcvEval g{f2 + pair * mn, lam2, f2f + pair * mn, lam2f, mn, (double)mn, 2};
+  const double* f2p = f2 + pair * mn;
+  const float* f2fp = f2f + pair * mn;
+  const double n_finite = (double)mn;
+  // Combines the per-warp sums in red[] (valid in warp 0).
+  auto combine = [&](double& trss, double& ttr) {
+    trss = 0.0;
+    ttr = 0.0;
+    for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
+  };
+  // Scores at the announced point (all threads, after a barrier that follows
+  // the announcement); the value is valid in warp 0.
+  auto score_fast = [&]() -> double {
+    const float s = (float)sh_s;
+    float rss = 0.f, tr = 0.f;
+    for (long long e = threadIdx.x; e < mn; e += blockDim.x) {
+      const float sl = s * lam2f[e];
+      const float d = sl * __frcp_rn(1.0f + sl);  // 1 - gamma
+      rss = fmaf(f2fp[e] * d, d, rss);
+      tr += d;
+    }
+    double drss = rss, dtr = tr;
+    for (int o = 16; o > 0; o >>= 1) {
+      drss += __shfl_xor_sync(~0u, drss, o);
+      dtr += __shfl_xor_sync(~0u, dtr, o);
+    }
+    if (lane == 0) { red[warp] = drss; red[32 + warp] = dtr; }
+    __syncthreads();
+    double f = 0.0;
+    if (w0) {
+      double trss, ttr;
+      combine(trss, ttr);
+      const double q = ttr / (double)mn;
+      f = trss / n_finite / (q * q) / 2;
+    }
+    return f;
+  };
+  auto score = [&]() -> double {
+    const double s = sh_s;
+    double rss = 0.0, tr = 0.0;
+    for (long long e = threadIdx.x; e < mn; e += blockDim.x) {
+      const double gm = rcp_fast(1.0 + s * lam2[e]);
+      const double d = gm - 1.0;
+      rss += f2p[e] * d * d;
+      tr += gm;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      rss += __shfl_xor_sync(~0u, rss, o);
+      tr += __shfl_xor_sync(~0u, tr, o);
+    }
+    if (lane == 0) { red[warp] = rss; red[32 + warp] = tr; }
+    __syncthreads();
+    double f = 0.0;
+    if (w0) {
+      double trss, ttr;
+      combine(trss, ttr);
+      const double q = 1.0 - ttr / (double)mn;
+      f = trss / n_finite / (q * q) / 2;
+    }
+    return f;
+  };
+  // Announces p (thread 0) and makes it visible; the barrier also orders the
+  // previous score's reads of red[] before the next score's writes.
+  auto announce = [&](double p) {
+    if (threadIdx.x == 0) sh_s = pow(10.0, p);
+    __syncthreads();
+  };
   // 10-point scan (gpu_smoothn.py:182-188), ranked with the fast score; the
   // best point is scored in float64 for the gradient test.
   double best_p = pmin, best_f = INFINITY;
   for (int k = 0; k < 10; ++k) {
     const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
-    const double fk = gcv_score_fast(g, pk, red);
+    announce(pk);
+    const double fk = score_fast();
     if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
   }
   double p = best_p;
-  const double f0 = gcv_score(g, p, red);
-  const double g0 = gcv_grad(g, p, f0, pmax, red);
-  const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
-  if (!(fabs(pg) <= 1e-5)) {
+  announce(p);
+  const double f0 = score();
+  // Finite-difference gradient as the reference's L-BFGS-B call computes it
+  // (absolute step 1e-8, backward at the upper bound).
+  const double h = 1e-8;
+  const bool fwd = p + h <= pmax;
+  announce(fwd ? p + h : p - h);
+  const double fh = score();
+  if (threadIdx.x == 0) {
+    const double g0 = fwd ? (fh - f0) / h : (f0 - fh) / h;
+    const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
+    sh_go = !(fabs(pg) <= 1e-5);
+  }
+  announce(p);  // also publishes sh_go
+  if (sh_go) {
     // Brent's bounded minimisation on the bracket around the scan point.
     const double step = (pmax - pmin) / 9.0;
     double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
     const double cg = 0.3819660112501051;
-    const double fs = gcv_score_fast(g, p, red);
+    const double fs = score_fast();
     double x = p, w = p, v = p, fx = fs, fw = fs, fv = fs, d = 0.0, e = 0.0;
     for (int it = 0; it < 200; ++it) {
-      const double xm = 0.5 * (a + b);
-      const double tol1 = 1e-8 * fabs(x) + 1e-10, tol2 = 2.0 * tol1;
-      if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
-      bool golden = true;
-      if (fabs(e) > tol1) {
-        double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
-        q = 2.0 * (q - r);
-        if (q > 0) pp = -pp;
-        q = fabs(q);
-        const double etemp = e;
-        e = d;
-        if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
-          d = pp / q;
-          const double u = x + d;
-          if (u - a < tol2 || b - u < tol2) d = xm >= x ? tol1 : -tol1;
-          golden = false;
+      double u = 0.0;
+      if (w0) {
+        const double xm = 0.5 * (a + b);
+        const double tol1 = 1e-8 * fabs(x) + 1e-10, tol2 = 2.0 * tol1;
+        const bool done = fabs(x - xm) <= tol2 - 0.5 * (b - a);
+        if (!done) {
+          bool golden = true;
+          if (fabs(e) > tol1) {
+            double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
+            q = 2.0 * (q - r);
+            if (q > 0) pp = -pp;
+            q = fabs(q);
+            const double etemp = e;
+            e = d;
+            if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
+              d = pp / q;
+              const double uu = x + d;
+              if (uu - a < tol2 || b - uu < tol2) d = xm >= x ? tol1 : -tol1;
+              golden = false;
+            }
+          }
+          if (golden) {
+            e = (x >= xm) ? a - x : b - x;
+            d = cg * e;
+          }
+          u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
+        }
+        if (lane == 0) {
+          sh_go = !done;
+          if (!done) sh_s = pow(10.0, u);
         }
       }
-      if (golden) {
-        e = (x >= xm) ? a - x : b - x;
-        d = cg * e;
-      }
-      const double u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
-      const double fu = gcv_score_fast(g, u, red);
-      if (fu <= fx) {
-        if (u >= x) a = x; else b = x;
-        v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
-      } else {
-        if (u < x) a = u; else b = u;
-        if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
-        else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+      __syncthreads();
+      if (!sh_go) break;
+      const double fu = score_fast();
+      if (w0) {
+        if (fu <= fx) {
+          if (u >= x) a = x; else b = x;
+          v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
+        } else {
+          if (u < x) a = u; else b = u;
+          if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
+          else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+        }
       }
     }
     p = x;
