@@ -95,6 +95,11 @@ PIV_D int stg_chunk(int t, int c) {
 PIV_D void cp_async16(uint32_t smem_addr, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr), "l"(gmem) : "memory");
 }
+// 16 bytes from gmem, or (valid false) 16 zero bytes without a global read.
+PIV_D void cp_async16_zfill(uint32_t smem_addr, const void* gmem, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr), "l"(gmem), "r"(valid ? 16 : 0)
+               : "memory");
+}
 PIV_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 PIV_D void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
@@ -426,19 +431,21 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     win_loc[sl][tid] = loc;
     win_seg[sl][tid] = sg;
   };
-  // Thread (half, t) starts the copies of row t of its frames of the tile in slot `sl`.
+  // Thread (half, t) starts the copies of row t of its frames of the tile in
+  // slot `sl`; rows of invalid windows are zero-filled (no global read), so
+  // the staging phase reads every row unconditionally.
   auto stage_async = [&](int sl) {
     const int w = t / SS, y = t % SS;
-    if (!win_valid[sl][w]) return;
+    const bool ok = win_valid[sl][w] != 0;
     const CorrSeg& q = seg_s[win_seg[sl][w]];
-    const long long off = win_base[sl][w] + (long long)y * q.width;
+    const long long off = ok ? win_base[sl][w] + (long long)y * q.width : 0;
 #pragma unroll
     for (int fi = 0; fi < 2 / TPL; ++fi) {
       const int f = TPL == 2 ? half : fi;
       const float* src = reinterpret_cast<const float*>(f == 0 ? q.frame_a : q.frame_b) + off;
       const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS * 4);
 #pragma unroll
-      for (int c = 0; c < CH; ++c) cp_async16(row + 16 * stg_chunk<CH>(t, c), src + 4 * c);
+      for (int c = 0; c < CH; ++c) cp_async16_zfill(row + 16 * stg_chunk<CH>(t, c), src + (ok ? 4 * c : 0), ok);
     }
   };
 
@@ -469,10 +476,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             const float4 q4 = *reinterpret_cast<const float4*>(row + 16 * stg_chunk<CH>(t, c));
-            r[4 * c] = ok ? q4.x : 0.f;
-            r[4 * c + 1] = ok ? q4.y : 0.f;
-            r[4 * c + 2] = ok ? q4.z : 0.f;
-            r[4 * c + 3] = ok ? q4.w : 0.f;
+            r[4 * c] = q4.x;
+            r[4 * c + 1] = q4.y;
+            r[4 * c + 2] = q4.z;
+            r[4 * c + 3] = q4.w;
           }
         } else {
           const CorrSeg& q = seg_s[win_seg[sl][w]];
@@ -964,16 +971,17 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     win_loc[sl][tid] = loc;
     win_seg[sl][tid] = sg;
   };
-  // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it stages itself.
+  // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it
+  // stages itself; rows of invalid windows are zero-filled (no global read).
   auto stage_async = [&](int sl) {
     const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
-    if (!win_valid[sl][w]) return;
+    const bool ok = win_valid[sl][w] != 0;
     const CorrSeg& sq = seg_s[win_seg[sl][w]];
-    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? sq.frame_a : sq.frame_b) + win_base[sl][w] +
-                         (long long)y * sq.width;
+    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? sq.frame_a : sq.frame_b) +
+                         (ok ? win_base[sl][w] + (long long)y * sq.width + 16 * 2 * h : 0);
     const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS);
 #pragma unroll
-    for (int c = 0; c < 2; ++c) cp_async16(row + 16 * stg64_chunk(t, 2 * h + c), src + 16 * (2 * h + c));
+    for (int c = 0; c < 2; ++c) cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
   };
 
   if (tid < W) window_setup(blockIdx.x, 0);
@@ -1002,7 +1010,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
           const uint4 q4 = *reinterpret_cast<const uint4*>(row + 16 * stg64_chunk(t, 2 * h + c));
           const uint32_t wds[4] = {q4.x, q4.y, q4.z, q4.w};
 #pragma unroll
-          for (int k = 0; k < 16; ++k) r[16 * c + k] = ok ? (float)((wds[k >> 2] >> (8 * (k & 3))) & 0xffu) : 0.f;
+          for (int k = 0; k < 16; ++k) r[16 * c + k] = (float)((wds[k >> 2] >> (8 * (k & 3))) & 0xffu);
         }
       } else {
         const CorrSeg& sq = seg_s[win_seg[sl][w]];
