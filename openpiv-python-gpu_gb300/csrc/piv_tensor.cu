@@ -127,6 +127,19 @@ PIV_D void first_max(const float (&x)[N], float& best, int& bj) {
   bj = bk[0];
 }
 
+// Warp-wide first maximum of (best, idx) over the 32 lanes: the largest
+// value, ties to the lowest index, in two warp reductions. Values are finite;
+// -0 is folded into +0 first, so that equal values have equal integer keys
+// (the order-preserving key of a float: its bits, the magnitude bits
+// inverted for negative values).
+PIV_D void warp_first_max(float& best, int& idx) {
+  const int bits = __float_as_int(best + 0.0f);
+  const int key = bits ^ ((bits >> 31) & 0x7fffffff);
+  const int kmax = __reduce_max_sync(0xffffffffu, key);
+  idx = (int)__reduce_min_sync(0xffffffffu, key == kmax ? (unsigned)idx : 0xffffffffu);
+  best = __int_as_float(kmax ^ ((kmax >> 31) & 0x7fffffff));
+}
+
 // Subpixel peak (gpu_process.py:1256-1294) from the five map values.
 PIV_D void subpixel_fit(int subpixel, int pi_, int pj, float c, float cd, float cu, float cl, float cr, float& isp,
                         float& jsp) {
@@ -716,12 +729,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         first_max<N>(rowc, best, bj);
         int idx = i * N + bj;
         if (i == 0) { best = 0.f; idx = 0; }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-          const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-          if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
-        }
+        warp_first_max(best, idx);
         if (a.maps && g0 + w < total) {
           const int ue = -sc_e[0][w] - sc_e[1][w];
           float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
@@ -757,12 +765,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         first_max<N>(rowc, best, bj);
         int idx = i * N + bj;
         if (i == 0) { best = 0.f; idx = 0; }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-          const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-          if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
-        }
+        warp_first_max(best, idx);
         if (lane == 0) {
           pk_val[w][r / 32] = best;
           pk_idx[w][r / 32] = idx;
@@ -1214,12 +1217,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       first_max<64>(v, best, bk);
       int idx = i * N + 64 * ch + bk;
       if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-        const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
-        if (v2 > best || (v2 == best && i2 < idx)) { best = v2; idx = i2; }
-      }
+      warp_first_max(best, idx);
       if (lane == 0) {
         pk_val[w][ch * 4 + (t >> 5)] = best;
         pk_idx[w][ch * 4 + (t >> 5)] = idx;
