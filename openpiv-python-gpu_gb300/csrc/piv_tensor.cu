@@ -472,7 +472,6 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
     const long long g0 = (long long)tile * W;
-    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
     if (ASYNC) cp_async_wait_all();
     __syncthreads();
 
@@ -524,10 +523,6 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
     }
     if (!sync_for_mma()) break;
-    if (ASYNC) {
-      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
-      cp_async_commit();
-    }
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
     if (tid == 0) {
@@ -538,6 +533,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
                          L::NB1, 256, 128, SS * 16, SS / 16, id, false);
       tc::mma_commit(&bar);
     }
+    // The next tile's window corners, while the products run (slot sl ^ 1 was
+    // last read by the previous tile's fits, before its final barrier).
+    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
     wait_mma();
 
     // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
@@ -577,6 +575,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
     }
     if (!sync_for_mma()) break;
+    if (ASYNC) {
+      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
+      cp_async_commit();
+    }
 
     // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
     if (tid == 0) {
@@ -997,7 +999,6 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
     const long long g0 = (long long)tile * W;
-    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
     if (ASYNC) cp_async_wait_all();
     __syncthreads();
 
@@ -1050,10 +1051,6 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     }
     if (!sync_for_mma()) break;
-    if (ASYNC) {
-      stage_async(sl ^ 1);
-      cp_async_commit();
-    }
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
     if (tid == 0) {
@@ -1068,6 +1065,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         }
       tc::mma_commit(&bar);
     }
+    // The next tile's window corners, while the products run (slot sl ^ 1 was
+    // last read by the previous tile's fits, before its final barrier).
+    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
     wait_mma();
 
     // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
@@ -1092,6 +1092,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
     }
     if (!sync_for_mma()) break;
+    if (ASYNC) {
+      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
+      cp_async_commit();
+    }
 
     // ---- Stage 2: X = T^T F^T -> TMEM cols [(rt 2 + f) N, +N).
     if (tid == 0) {
