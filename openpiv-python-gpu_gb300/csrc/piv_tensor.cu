@@ -140,6 +140,16 @@ PIV_D void warp_first_max(float& best, int& idx) {
   best = __int_as_float(kmax ^ ((kmax >> 31) & 0x7fffffff));
 }
 
+// 64-bit key of a candidate peak whose unsigned maximum is the first maximum:
+// the value's order-preserving bits (-0 folded into +0) above the inverted
+// flat index (a lower index gives a larger key among equal values).
+PIV_D unsigned long long peak_key(float best, int idx) {
+  const int bits = __float_as_int(best + 0.0f);
+  const unsigned k = (unsigned)(bits ^ ((bits >> 31) & 0x7fffffff)) ^ 0x80000000u;
+  return ((unsigned long long)k << 32) | (unsigned)~idx;
+}
+PIV_D int peak_index(unsigned long long key) { return (int)~(unsigned)key; }
+
 // Subpixel peak (gpu_process.py:1256-1294) from the five map values.
 PIV_D void subpixel_fit(int subpixel, int pi_, int pj, float c, float cd, float cu, float cl, float cr, float& isp,
                         float& jsp) {
@@ -874,8 +884,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   __shared__ long long win_loc[2][W];  // window index within its segment
   __shared__ int win_seg[2][W];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
-  __shared__ float pk_val[W][8];
-  __shared__ int pk_idx[W][8];
+  __shared__ unsigned long long pk_key[W];  // per window: the running first maximum (peak_key)
 
   const int tid = threadIdx.x;
   const int q = tid >> 7, t = tid & 127;
@@ -989,6 +998,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     for (int c = 0; c < 2; ++c) cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
   };
 
+  if (tid < W) pk_key[tid] = 0ull;
   if (tid < W) window_setup(blockIdx.x, 0);
   __syncthreads();
   if (ASYNC) {
@@ -1222,10 +1232,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       int idx = i * N + 64 * ch + bk;
       if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
       warp_first_max(best, idx);
-      if (lane == 0) {
-        pk_val[w][ch * 4 + (t >> 5)] = best;
-        pk_idx[w][ch * 4 + (t >> 5)] = idx;
-      }
+      if (lane == 0) atomicMax(&pk_key[w], peak_key(best, idx));
       if (a.maps && g0 + w < total) {
         const int ue = -sc_e[0][w] - sc_e[1][w];
         float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
@@ -1234,20 +1241,8 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
     }
     __syncthreads();
-    if (tid < W) {
-      float v = pk_val[tid][0];
-      int idx = pk_idx[tid][0];
-#pragma unroll
-      for (int p = 1; p < 8; ++p)
-        if (pk_val[tid][p] > v || (pk_val[tid][p] == v && pk_idx[tid][p] < idx)) {
-          v = pk_val[tid][p];
-          idx = pk_idx[tid][p];
-        }
-      pk_idx[tid][0] = idx;
-    }
-    __syncthreads();
     {
-      const int pidx = pk_idx[w][0], pi_ = pidx / N, pj = pidx % N;
+      const int pidx = peak_index(pk_key[w]), pi_ = pidx / N, pj = pidx % N;
       const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
       if (__any_sync(0xffffffffu, mine)) {
         float v[64];
@@ -1266,7 +1261,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     __syncthreads();
     if (tid < W && g0 + tid < total) {
       const int ww = tid;
-      const int pidx = pk_idx[ww][0], pi_ = pidx / N, pj = pidx % N;
+      const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
         const int ue = -sc_e[0][ww] - sc_e[1][ww];
@@ -1291,6 +1286,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
     }
+    if (tid < W) pk_key[tid] = 0ull;  // after its last read (above, same thread); ready for the next tile
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
