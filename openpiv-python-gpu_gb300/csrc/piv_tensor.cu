@@ -221,14 +221,14 @@ PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uin
                      uint32_t b, uint32_t b_lo, uint32_t b_step, uint32_t b_lbo, uint32_t b_sbo, int ks_n,
                      uint32_t id, bool acc_first) {
   for (int ks = 0; ks < ks_n; ++ks)
-    tc::mma_f16(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo), id,
+    tc::mma_f16<SPLIT>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo), id,
                 acc_first || ks > 0);
   if (SPLIT) {
     for (int ks = 0; ks < ks_n; ++ks)
-      tc::mma_f16(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + b_lo + ks * b_step, b_lbo, b_sbo),
+      tc::mma_f16<SPLIT>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + b_lo + ks * b_step, b_lbo, b_sbo),
                   id, 1);
     for (int ks = 0; ks < ks_n; ++ks)
-      tc::mma_f16(d, tc::sdesc(a + a_lo + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo),
+      tc::mma_f16<SPLIT>(d, tc::sdesc(a + a_lo + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo),
                   id, 1);
   }
 }
@@ -535,13 +535,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
-    if (tid == 0) {
+    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
       const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
       for (int f = 0; f < 2; ++f)
         mma_chain<SPLIT>(tmem + f * N, sbase + L::OP + f * L::A1_BYTES, L::NOP, 256, 128, SS * 16, sbase + L::B1,
                          L::NB1, 256, 128, SS * 16, SS / 16, id, false);
-      tc::mma_commit(&bar);
+      tc::mma_commit<SPLIT>(&bar);
     }
     // The next tile's window corners, while the products run (slot sl ^ 1 was
     // last read by the previous tile's fits, before its final barrier).
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     }
 
     // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
-    if (tid == 0) {
+    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt)
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         for (int f = 0; f < 2; ++f)
           mma_chain<SPLIT>(tmem + rt * 2 * N + f * N, sbase + L::OP + (f * 2 + rt) * L::A2_BYTES, L::NOP, 32 * 128,
                            128 * 16, 128, sbase + L::B1, L::NB1, 256, 128, SS * 16, SS / 16, id, false);
-      tc::mma_commit(&bar);
+      tc::mma_commit<SPLIT>(&bar);
     }
     wait_mma();
 
@@ -642,11 +642,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 3: U = Q E / N -> TMEM cols [0, 2N).
-    if (tid == 0) {
+    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
       const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
       mma_chain<SPLIT>(tmem, sbase + L::OP, L::NOP, 256, 128, 2 * N * 16, sbase + L::B3, L::NB3, 256, 128,
                        2 * N * 16, 2 * N / 16, id, false);
-      tc::mma_commit(&bar);
+      tc::mma_commit<SPLIT>(&bar);
     }
     wait_mma();
 
@@ -676,13 +676,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
-    if (tid == 0) {
+    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt)
         mma_chain<SPLIT>(tmem + rt * N, sbase + L::OP + rt * L::A4_BYTES, L::NOP, 32 * 128, 128 * 16, 128,
                          sbase + L::B4, L::NB4, 256, 128, N * 16, N / 16, id, false);
-      tc::mma_commit(&bar);
+      tc::mma_commit<SPLIT>(&bar);
     }
     wait_mma();
 
