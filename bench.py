@@ -41,6 +41,13 @@ WORKLOAD = ("1024x1024 uint8 pairs, 0.03 ppp, shear 6/2 px; 64->32->16 px @50%, 
             "median validation tol 2 + 2 revalidated spring replacements; smoothn GCV; float32")
 FRAME = (1024, 1024)
 DISTINCT = 16
+# Arithmetic of the correlation DFTs per form (fields, fits, validation and
+# deformation are float32; smoothn's GCV float64 in every form).
+DTYPE_OF_FORM = {
+    "fft": "f32",
+    "tensor": "f16 operands, f32 accumulation (tcgen05 kind::f16)",
+    "tensor_split": "f16 hi/lo operand pairs, 3 products per stage, f32 accumulation (tcgen05 kind::f16)",
+}
 
 
 def parse_args():
@@ -50,13 +57,15 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--pairs", type=int, default=128, help="pairs per step per GPU")
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--dft", choices=["fft", "tensor", "tensor_split"], default="tensor",
+    ap.add_argument("--dft", choices=["fft", "tensor", "tensor_split", "tensor_refined"], default="tensor",
                     help="correlation engine of the chosen form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default correlation launch variants instead of autotuning them per pass")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip timing the other tensor forms (fp16, hi/lo split, refined) beside the chosen one")
     ap.add_argument("--no-split", action="store_true",
                     help="skip timing the hi/lo split tensor form beside the fp16 tensor form")
     ap.add_argument("--serve", action="store_true",
@@ -111,6 +120,32 @@ def _make_precision_pair(k):
 
     a, b, _, _ = synthetic.config_case(3, k)
     return a, b
+
+
+def _oracle_case(args):
+    """Float64 oracle fields of pair k of workload cfg (optionally resized):
+    (u, v, seconds)."""
+    cfg, k, shape = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, ROOT)
+    from oracle.piv_oracle import OraclePIV
+    from openpiv_gpu import synthetic
+
+    a, b, _, piv = synthetic.config_case(cfg, k, shape=None if shape is None else tuple(shape))
+    piv = dict(piv)
+    piv["dtype_f"] = "float64"
+    mss = piv.pop("min_search_size")
+    t = time.perf_counter()
+    u, v = OraclePIV(a.shape, mss, **piv)(a, b)
+    return u, v, time.perf_counter() - t
+
+
+def _rms(u, v, u64, v64):
+    import numpy as np
+
+    return float(np.sqrt(np.mean((np.asarray(u, dtype=np.float64) - u64) ** 2 +
+                                 (np.asarray(v, dtype=np.float64) - v64) ** 2)))
 
 
 def _precision_oracle(args):
@@ -421,15 +456,19 @@ def run_gpu(args):
         ms_p = max_over_ranks(ms_p, dist)
         plain = {"pairs_per_s": B * world / (ms_p / args.steps * 1e-3), "ms_per_step": ms_p / args.steps}
         plain["chosen_over_plain"] = value / plain["pairs_per_s"]
-    split = None
-    proc_split = None
-    if args.dft == "tensor" and not args.no_split:
-        proc_split = make("tensor_split")
-        ms_s, _, _ = graph_time(proc_split)
-        ms_s = max_over_ranks(ms_s, dist)
-        split = {"pairs_per_s": B * world / (ms_s / args.steps * 1e-3), "ms_per_step": ms_s / args.steps}
+    # The other tensor forms, timed the same way.
+    others, other_procs = {}, {}
+    for form in ("tensor", "tensor_split", "tensor_refined"):
+        if form == args.dft or args.dft == "fft" or args.no_others or (form == "tensor_split" and args.no_split):
+            continue
+        other_procs[form] = make(form)
+        ms_o, _, _ = graph_time(other_procs[form])
+        ms_o = max_over_ranks(ms_o, dist)
+        others[form] = {"pairs_per_s": B * world / (ms_o / args.steps * 1e-3), "ms_per_step": ms_o / args.steps}
         if plain:
-            split["over_plain"] = split["pairs_per_s"] / plain["pairs_per_s"]
+            others[form]["over_plain"] = others[form]["pairs_per_s"] / plain["pairs_per_s"]
+    split = others.get("tensor_split")
+    proc_split = other_procs.get("tensor_split")
 
     # Stage breakdown (CUDA events inside the run, same stream).
     plan = proc.plan_handle(fa, B)
@@ -464,7 +503,7 @@ def run_gpu(args):
     peaks = measured_peaks()
     traffic_w = ncu_traffic()
     on_tensor = N == 2 * f.search_size and (
-        (args.dft == "tensor" and f.search_size in (16, 32, 64)) or
+        (args.dft in ("tensor", "tensor_refined") and f.search_size in (16, 32, 64)) or
         (args.dft == "tensor_split" and f.search_size in (16, 32)))
     if on_tensor:
         peak = peaks.get("bf16_tflops", 1900.0)
@@ -512,23 +551,29 @@ def run_gpu(args):
     e2e = {"value": B * world * args.steps / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": int(2 * B * FRAME[0] * FRAME[1]),
            "d2h_bytes_per_step": int(B * m * n * (8 + 8 + 1 + 1))}
 
-    # Accuracy of pair 0 against the float64 oracle (and the float32 parity oracle).
+    # Accuracy of every form timed here: pair 0 against the float64 oracle and
+    # the float32 parity oracle (the reference algorithm), and the near-tie
+    # windows (integer peaks the engine does not resolve) of a whole batch.
     accuracy = None
     if rank == 0 and not args.no_accuracy and cpu is not None:
         (_, u64, v64), (_, u32, v32) = cpu.map(_oracle_pair, [(0, "float64"), (0, "float32")])
         rms = lambda a, b, c, d: float(np.sqrt(np.mean((a - b) ** 2 + (c - d) ** 2)))
-        gu, gv = res_u[0].astype(np.float64), res_v[0].astype(np.float64)
-        accuracy = {"form": args.dft, "rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64),
-                    "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
-                    "max_px_vs_fp32_oracle": float(max(np.abs(gu - u32).max(), np.abs(gv - v32).max()))}
+
+        def form_accuracy(p):
+            pu, pv = p.run_batch(fa, fb)
+            ties = p.near_ties()
+            gu, gv = pu[0].cpu().numpy(), pv[0].cpu().numpy()
+            return {"rms_px_vs_fp64_oracle": rms(gu, u64, gv, v64), "rms_px_vs_fp32_oracle": rms(gu, u32, gv, v32),
+                    "max_px_vs_fp32_oracle": float(max(np.abs(gu - u32).max(), np.abs(gv - v32).max())),
+                    "near_ties_per_pass": ties, "windows_per_pass": [B * f.n_wins for f in p.piv_fields]}
+
+        forms = {args.dft: form_accuracy(proc)}
         if proc_plain is not None:
-            pu, pv = proc_plain.run_batch(fa[:1], fb[:1])
-            pu, pv = pu[0].cpu().numpy(), pv[0].cpu().numpy()
-            accuracy["plain_rms_px_vs_fp64_oracle"] = rms(pu, u64, pv, v64)
-        if proc_split is not None:
-            su, sv = proc_split.run_batch(fa[:1], fb[:1])
-            su, sv = su[0].cpu().numpy(), sv[0].cpu().numpy()
-            accuracy["split_rms_px_vs_fp64_oracle"] = rms(su, u64, sv, v64)
+            forms["fft"] = form_accuracy(proc_plain)
+        for form, p in other_procs.items():
+            forms[form] = form_accuracy(p)
+        accuracy = dict(forms[args.dft], form=args.dft, forms=forms,
+                        pair="pair 0 of the step against the oracles; near ties over the whole step")
 
     cpu_baseline = None
     if cpu is not None:
@@ -543,12 +588,12 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded particle images)",
+            "vs_baseline": None, "dtype": DTYPE_OF_FORM[args.dft], "data": "synthetic (seeded particle images)",
             "config": {"workload": WORKLOAD, "pairs_per_step": B, "distinct_pairs": DISTINCT, "frame": list(FRAME),
                        "form": args.dft, "graph": True,
                        "l2": "inputs larger than L2 (B x 2 MiB frames + 8 MiB float frames per pair per pass)"},
             "windows_per_s": value * windows_per_pair, "windows_per_pair": windows_per_pair,
-            "plain_form": plain, "split_form": split,
+            "plain_form": plain, "split_form": split, "other_forms": others,
             "tuning": {"form": [t["name"] for t in proc.tuning()],
                        "default_ms": [t["ms"][0] for t in proc.tuning()],
                        "tuned_ms": [None if t["ms"][t["variant"]] is None else t["ms"][t["variant"]]
@@ -594,6 +639,11 @@ def run_serve(args):
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
     picks = rng.integers(len(shapes), size=args.requests)
     frames = [pool_by_shape[tuple(shapes[i])][j % per_shape] for j, i in enumerate(picks)]
+    # Accuracy: the first pair of every size against the float64 oracle, run
+    # on the host cores while the GPU serves.
+    oracle_pool = mp.get_context("spawn").Pool(len(shapes))
+    acc_jobs = {tuple(sh): oracle_pool.apply_async(_oracle_case, ((5, 100 + i, sh),)) for i, sh in enumerate(shapes)}
+    first_pair = {tuple(sh): pool_by_shape[tuple(sh)][0] for sh in shapes}
     settings = dict(synthetic.CONFIGS[5]["piv"])
     server = PIVServer(settings, max_batch=8, slots_per_shape=2, dft=args.dft)
     for shape in shapes:  # lanes, plans and first launches outside the timed run
@@ -619,6 +669,14 @@ def run_serve(args):
         lat.append(time.perf_counter() - t0 - t_arr)
     plain_secs = time.perf_counter() - t0
     lat = np.array(lat)
+    # The first pair of every size through the same server and lanes.
+    acc_reqs = {sh: server.submit(*first_pair[sh]) for sh in first_pair}
+    server.drain()
+    accuracy = {}
+    for sh, job in acc_jobs.items():
+        u64, v64, secs_o = job.get()
+        accuracy[f"{sh[1]}x{sh[0]}"] = _rms(acc_reqs[sh].u, acc_reqs[sh].v, u64, v64)
+    oracle_pool.close()
     line = {
         "metric": "serving pairs/s with p50/p99 latency (Poisson arrivals, 5 frame sizes, 64->32->16 px three-pass PIV)",
         "value": len(done) / secs, "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True,
@@ -631,6 +689,11 @@ def run_serve(args):
                    "validation, 2 revalidated spring replacements, smoothn GCV; float32",
                    "data": "synthetic (2 seeded pairs per size, reused)"},
         "device_status": max(l.proc.status() for l in server.lanes.values()),
+        "accuracy": {"rms_px_vs_fp64_oracle": accuracy,
+                     "case": "the first pair of every size, served by the same loop, against the float64 oracle"},
+        "continuous_batching": {"max_batches_in_flight": server.max_in_flight,
+                                "overlapping_batch_pairs": server.overlapping_batches(),
+                                "held_for_memory": server.held_for_memory},
     }
     print(json.dumps(line), flush=True)
 
@@ -652,6 +715,13 @@ def run_mixed(args):
 
     with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
         pairs = pool.map(_make_mixed_pair, range(64))
+    # Accuracy: the first pair of every size against the float64 oracle, on
+    # the host cores while the GPU runs.
+    first = {}
+    for k, (a, _) in enumerate(pairs):
+        first.setdefault(a.shape, k)
+    oracle_pool = mp.get_context("spawn").Pool(len(first))
+    acc_jobs = {sh: oracle_pool.apply_async(_oracle_case, ((4, k, None),)) for sh, k in first.items()}
     _build.build()
     torch.cuda.set_device(0)
     settings = dict(synthetic.CONFIGS[4]["piv"])
@@ -671,12 +741,22 @@ def run_mixed(args):
         e1.record(batch.stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.steps
+        res = batch.results()
         out[form] = {"pairs_per_s": 64 / (ms * 1e-3), "ms_per_submission": ms,
+                     "rms_px_vs_fp64_oracle": {f"{sh[1]}x{sh[0]}": (res[k], sh) for sh, k in first.items()},
                      "windows_per_s": batch.windows / (ms * 1e-3), "windows": batch.windows,
                      "device_status": batch.status(), "kernel_nodes": batch.kernel_nodes,
                      "schedule": batch.schedule, "schedule_ms": batch.schedule_ms}
         del batch
         torch.cuda.empty_cache()
+    for sh, job in acc_jobs.items():
+        u64, v64, _ = job.get()
+        for form in out:
+            acc = out[form]["rms_px_vs_fp64_oracle"]
+            key = f"{sh[1]}x{sh[0]}"
+            (gu, gv), _ = acc[key]
+            acc[key] = _rms(gu, gv, u64, v64)
+    oracle_pool.close()
     line = {
         "metric": "frame pairs/s of one mixed-size submission (64 pairs, 4 sizes, 64->32->16 px three-pass PIV)",
         "value": out[args.dft]["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
@@ -710,6 +790,10 @@ def run_precision(args):
     with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
         pairs = pool.map(_make_precision_pair, range(16))
         acc_cases = pool.map(_precision_oracle, [(k, acc_shape) for k in range(4)])
+    # One full-size pair (pair 0 of the timed batch) against the float64
+    # oracle, on a host core while the GPU runs.
+    oracle_pool = mp.get_context("spawn").Pool(1)
+    full_job = oracle_pool.apply_async(_oracle_case, ((3, 0, None),))
     import __graft_entry__
 
     __graft_entry__.build()
@@ -755,6 +839,7 @@ def run_precision(args):
         clocks = sampler.stop()
         ms = e0.elapsed_time(e1) / args.steps
         windows = sum(f.n_wins for f in proc.piv_fields)
+        full_uv = (u[0].cpu().numpy(), v[0].cpu().numpy())
         errs = []
         for a, b, u64, v64 in acc_cases:
             small = PIVGPU(acc_shape, mss, **kw, dft=form)
@@ -762,22 +847,29 @@ def run_precision(args):
             errs.append(float(np.mean((gu[0] - u64) ** 2 + (gv[0] - v64) ** 2)))
         out[form] = {"pairs_per_s": B / (ms * 1e-3), "ms_per_step": ms, "windows_per_s": B * windows / (ms * 1e-3),
                      "windows_per_pair": windows, "kernels_per_step": nk.value,
-                     "rms_px_vs_fp64_oracle": float(np.sqrt(np.mean(errs))),
+                     "rms_px_vs_fp64_oracle": float(np.sqrt(np.mean(errs))), "full_uv": full_uv,
                      "tuning": [t["name"] for t in proc.tuning()], "device_status": proc.status(), "clocks": clocks}
         del proc
         torch.cuda.empty_cache()
+    u64, v64, oracle_s = full_job.get()
+    oracle_pool.close()
+    for form in out:
+        gu, gv = out[form].pop("full_uv")
+        out[form]["rms_px_vs_fp64_oracle_full_pair"] = _rms(gu, gv, u64, v64)
     chosen = out["tensor_split"]
     line = {
         "metric": "frame pairs/s (2048x2048, 32->16 px two-pass PIV at 75% overlap, precision form) on 1 GB300",
         "value": chosen["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "form": "tensor_split", "dtype": "f32",
+        "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "form": "tensor_split", "dtype": DTYPE_OF_FORM["tensor_split"],
         "data": "synthetic (seeded particle images)", "chosen": chosen, "fp16_tensor_form": out["tensor"],
         "plain_form": out["fft"], "chosen_over_plain": chosen["pairs_per_s"] / out["fft"]["pairs_per_s"],
         "config": {"workload": "16 resident 2048x2048 uint8 pairs, 0.05 ppp, 8-mode streamfunction flow up to 8 px; "
                                "32 -> 16 px at 75%, n_fft 2, median validation, 2 revalidated spring replacements; "
                                "float32", "graph": True,
-                   "accuracy_case": f"4 pairs of {acc_shape[0]}x{acc_shape[1]} with the same particle model, flow "
-                                    "and settings against the float64 oracle",
+                   "accuracy_case": f"rms_px_vs_fp64_oracle: 4 pairs of {acc_shape[0]}x{acc_shape[1]} with the same "
+                                    "particle model, flow and settings against the float64 oracle; "
+                                    "rms_px_vs_fp64_oracle_full_pair: pair 0 of the timed batch (2048x2048) "
+                                    f"against the float64 oracle ({oracle_s:.0f} s on one host core)",
                    "l2": "inputs larger than L2 (16 x 8 MiB frames + 32 MiB float frames per pair)"},
     }
     print(json.dumps(line), flush=True)

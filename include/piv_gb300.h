@@ -54,6 +54,12 @@ extern "C" {
 #define PIV_REPLACE_MEDIAN 1
 #define PIV_REPLACE_MEAN 2
 
+/* Flag bits of smoothn per pair (the conditions of SmoothnGPU's log
+ * messages, gpu_smoothn.py:218-222, 429-439). */
+#define PIV_SMOOTH_S_LOWER 1     /* GCV: log10(s) within 0.1 of its lower bound */
+#define PIV_SMOOTH_S_UPPER 2     /* GCV: log10(s) within 0.1 of its upper bound */
+#define PIV_SMOOTH_MAX_ITERS 4   /* the weighted iteration reached its last allowed step (100) */
+
 /* Correlation engines. */
 #define PIV_DFT_FFT32 0          /* in-shared-memory FFT in the correlation float type */
 #define PIV_DFT_TENSOR 1         /* tcgen05 tensor-core DFT: FP16 operands, FP32 accumulation
@@ -62,6 +68,10 @@ extern "C" {
 #define PIV_DFT_TENSOR_SPLIT 2   /* as PIV_DFT_TENSOR with every operand split into FP16 hi and
                                     lo parts and three products per stage (compensated);
                                     search 16 or 32 px, other passes use the FFT */
+#define PIV_DFT_TENSOR_REFINED 3 /* PIV_DFT_TENSOR's maps give each window's integer peak, then
+                                    the five values of the subpixel fit are recomputed in float32
+                                    by direct sums from the frames (float32 FFT accuracy of the
+                                    fit; same passes as PIV_DFT_TENSOR, others use the FFT) */
 
 /* Settings of one PIV iteration, the per-pass tuple entries of
  * PIVGPU.__init__ (gpu_process.py:497-546) expanded per iteration as the
@@ -141,6 +151,19 @@ int piv_plan_run(piv_plan* plan, int n_pairs, const void* frames_a, const void* 
  * is then reset). Synchronises `stream`. No counterpart in the reference,
  * whose CuPy calls have no device-side waits. */
 int piv_plan_status(piv_plan* plan, int* status, void* stream);
+
+/* Near ties of the correlation peaks of the last run, per iteration (counts
+ * over all pairs; counts[k] for iteration k, up to `capacity` entries). A
+ * window is a near tie when its second-largest correlation value, at another
+ * lag (lags without window overlap read as zero), is within tol * |peak| of
+ * the peak, tol being the engine's map accuracy: 2^-17 for the float32 FFT
+ * and the hi/lo split tensor engines, 2^-40 for the float64 FFT, 2^-9 for the
+ * fp16-operand tensor engine. Its integer peak location is then not resolved
+ * by the engine and may differ from the reference's first argmax
+ * (gpu_process.py:1248-1254); every other window's integer peak is expected
+ * to be identical. Masked windows are never near ties. The per-window flags
+ * are in piv_iteration_view.near_tie. Synchronises `stream`. */
+int piv_plan_near_ties(piv_plan* plan, int* counts, int capacity, void* stream);
 
 /* Autotuner (no counterpart in the reference, whose correlation is one cuFFT
  * call per pass). Runs the plan once on the given frames, then times every
@@ -224,6 +247,8 @@ typedef struct piv_iteration_view {
     const double* smooth_p;                 /* [pairs], NaN when no smoothing ran */
     const int* peak_i; const int* peak_j;   /* integer peak of each window (shifted map) */
     const void* s2n;                        /* [pairs][m][n] or NULL */
+    const uint8_t* near_tie;                /* [pairs][m][n]: 1 where the peak is a near tie (piv_plan_near_ties) */
+    const int* smooth_flags;                /* [pairs]: PIV_SMOOTH_* bits of this iteration's smoothing (0 when none ran) */
 } piv_iteration_view;
 int piv_plan_iteration_view(const piv_plan* plan, int iter, piv_iteration_view* out);
 
@@ -344,15 +369,27 @@ int piv_replace(int m, int n, int n_pairs, double* u, double* v, uint8_t* val, c
 int piv_smoothn(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double s,
                 double* p_out, void* stream);
 
+/* piv_smoothn that also writes, per pair, the PIV_SMOOTH_* flags behind
+ * SmoothnGPU's log messages (gpu_smoothn.py:218-222, 429-439) to flags_out
+ * (device [n_pairs]). */
+int piv_smoothn_flags(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double s,
+                      double* p_out, int* flags_out, void* stream);
+
 /* piv_smoothn for callers that cannot allocate device memory while they run
  * (a fixed memory budget handed over at start-up, a real-time loop that must
  * not wait on the allocator, a host framework that owns every allocation).
  * No counterpart in the reference. Same arguments and results as
  * piv_smoothn, but the scratch is a fixed 4 MiB device array inside the
- * library (for example 4 pairs of 128 x 128 fields); larger requests fail with
- * PIV_E_ARG and a message. It calls no allocator. The first call on a device
- * looks up the array's device address, so make that first call before any
- * stream capture. Calls share the array: calls that overlap on the GPU (other
+ * library (for example 4 pairs of 128 x 128 fields, or 2 pairs of 127 x 127
+ * fields with a field mask, whose weighted iteration keeps more per pair);
+ * larger requests, and shapes beyond 2^31 elements or 65535 pairs, fail with
+ * PIV_E_ARG and a message. It calls no allocator. Each call made outside
+ * stream capture looks up the array's device address in the current context
+ * (so calls after a device reset use the reloaded array); a call made while
+ * `stream` is being captured reuses the address of the device's last
+ * uncaptured call, so make the first call on a device (and the first after a
+ * device reset) before any stream capture. Calls share the array and find it
+ * holding the previous call's contents: calls that overlap on the GPU (other
  * streams, other threads) race and must be serialised by the caller. */
 int piv_smoothn_noalloc(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double s,
                         double* p_out, void* stream);

@@ -118,8 +118,10 @@ struct IterState {
   uint8_t* val0 = nullptr;
   uint8_t* val = nullptr;
   double* smooth_p = nullptr;
+  int* smooth_flags = nullptr;
   int* peak_i = nullptr;
   int* peak_j = nullptr;
+  uint8_t* near_tie = nullptr;  // per window: near tie of the correlation peak
   void* s2n = nullptr;
   uint8_t* field_mask = nullptr;
   // Correlation launch variant (0 = default; set by piv_plan_autotune or
@@ -150,6 +152,8 @@ struct piv_plan {
   void* smooth_scratch = nullptr;
   double* rms_stats = nullptr;
   int* status = nullptr;      // device status word of bounded device-side waits
+  int* tie_counts = nullptr;  // [n_iters] near-tie windows of the last run per iteration
+  int* tie_list = nullptr;    // refined tensor form: near-tie windows of a pass (max_pairs * max windows) + count
   uint8_t* outliers = nullptr;
   double* u_final = nullptr;
   double* v_final = nullptr;
@@ -319,7 +323,7 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
   if (cfg->max_pairs <= 0) return set_error(PIV_E_ARG, "max_pairs must be positive");
   if (pixel_bytes(cfg->pixel_type) == 0) return set_error(PIV_E_ARG, "unknown pixel_type %d", cfg->pixel_type);
   if (cfg->dtype != PIV_DTYPE_F32 && cfg->dtype != PIV_DTYPE_F64) return set_error(PIV_E_ARG, "unknown dtype");
-  if (cfg->dft_mode < PIV_DFT_FFT32 || cfg->dft_mode > PIV_DFT_TENSOR_SPLIT)
+  if (cfg->dft_mode < PIV_DFT_FFT32 || cfg->dft_mode > PIV_DFT_TENSOR_REFINED)
     return set_error(PIV_E_ARG, "unknown dft_mode %d", cfg->dft_mode);
   if (!(cfg->dt > 0) || !(cfg->scaling_par > 0)) return set_error(PIV_E_ARG, "dt and scaling_par must be > 0");
   piv_plan* p = new piv_plan();
@@ -368,8 +372,11 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
     if ((rc = plan_alloc_t(p, &s.val0, cnt))) break;
     if ((rc = plan_alloc_t(p, &s.val, cnt))) break;
     if ((rc = plan_alloc_t(p, &s.smooth_p, (size_t)P))) break;
+    if ((rc = plan_alloc_t(p, &s.smooth_flags, (size_t)P))) break;
+    cudaMemset(s.smooth_flags, 0, sizeof(int) * P);
     if ((rc = plan_alloc_t(p, &s.peak_i, cnt))) break;
     if ((rc = plan_alloc_t(p, &s.peak_j, cnt))) break;
+    if ((rc = plan_alloc_t(p, &s.near_tie, cnt))) break;
     if (!isnan(it.s2n_tol) && (rc = plan_alloc(p, &s.s2n, cnt * tsz))) break;
     if (cfg->mask) {
       std::vector<uint8_t> fm(s.mn);
@@ -411,6 +418,11 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
     rc = plan_alloc_t(p, &p->status, 1);
     if (rc == PIV_OK) cudaMemset(p->status, 0, sizeof(int));
   }
+  if (rc == PIV_OK) {
+    rc = plan_alloc_t(p, &p->tie_counts, (size_t)cfg->n_iters);
+    if (rc == PIV_OK) cudaMemset(p->tie_counts, 0, sizeof(int) * cfg->n_iters);
+  }
+  if (rc == PIV_OK && cfg->dft_mode == PIV_DFT_TENSOR_REFINED) rc = plan_alloc_t(p, &p->tie_list, max_mn * P + 1);
   if (rc == PIV_OK) {
     const size_t cnt = p->st.back().mn * P;
     rc = plan_alloc_t(p, &p->outliers, cnt);
@@ -459,6 +471,8 @@ int piv_plan_iteration_view(const piv_plan* p, int iter, piv_iteration_view* v) 
   v->peak_i = s.peak_i;
   v->peak_j = s.peak_j;
   v->s2n = s.s2n;
+  v->near_tie = s.near_tie;
+  v->smooth_flags = s.smooth_flags;
   return PIV_OK;
 }
 
@@ -516,6 +530,7 @@ static int run_begin(piv_plan* p, int n_pairs, const void* frames_a, const void*
   }
   x.fa = frames_a;
   x.fb = frames_b;
+  PIV_TRY(cuda_ok(cudaMemsetAsync(p->tie_counts, 0, sizeof(int) * p->st.size(), s), "near-tie counters"));
   if (frames_on_host || p->frame_mask) {
     const cudaMemcpyKind kind = frames_on_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     PIV_TRY(cuda_ok(cudaMemcpyAsync(p->stage_a, frames_a, n_pairs * hw * pb, kind, s), "frame copy"));
@@ -613,6 +628,12 @@ static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
   c.scratch_bytes = p->corr_scratch_bytes;
   c.maps = nullptr;
   c.status = p->status;
+  c.near_tie = st.near_tie;
+  c.tie_count = p->tie_counts + k;
+  if (p->tie_list) {
+    c.tie_list = p->tie_list + 1;
+    c.tie_list_count = p->tie_list;
+  }
   st.corr = c;
   st.corr_valid = true;
   return PIV_OK;
@@ -667,7 +688,7 @@ static int run_post(piv_plan* p, int k, RunCtx& x, cudaStream_t s) {
   mark(p, x, k * PIV_STAGES + 4, s);
   if (k != n_it - 1) {
     PIV_TRY(smoothn(st.g.m, st.g.n, n_pairs, st.u_rep, st.v_rep, st.u_out, st.v_out, st.field_mask,
-                    it.smoothing_par, st.smooth_p, p->smooth_scratch, s));
+                    it.smoothing_par, st.smooth_p, p->smooth_scratch, s, st.smooth_flags));
     mark(p, x, k * PIV_STAGES + 5, s);
   }
   return PIV_OK;
@@ -803,10 +824,18 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
   if (correlate_tensor_supported(c, dft_mode)) {
     PIV_TRY(cuda_ok(cudaMallocAsync((void**)&c.status, sizeof(int), s), "cudaMallocAsync"));
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
+    int* peaks = nullptr;  // the refined form reads the peaks back: device peaks when the caller wants none
+    const size_t cnt = (size_t)n_pairs * g->m * g->n;
+    if (dft_mode == PIV_DFT_TENSOR_REFINED && (!c.peak_i || !c.peak_j)) {
+      PIV_TRY(cuda_ok(cudaMallocAsync((void**)&peaks, 2 * cnt * sizeof(int), s), "cudaMallocAsync"));
+      if (!c.peak_i) c.peak_i = peaks;
+      if (!c.peak_j) c.peak_j = peaks + cnt;
+    }
     int rc = correlate_tensor(c, dft_mode, 0, s);
     int st = 0;
     cudaMemcpyAsync(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(c.status, s);
+    if (peaks) cudaFreeAsync(peaks, s);
     cudaStreamSynchronize(s);
     if (rc == PIV_OK && st != 0) rc = set_error(st, "tensor correlation: a bounded wait gave up");
     return rc;
@@ -950,13 +979,28 @@ int piv_replace(int m, int n, int n_pairs, double* u, double* v, uint8_t* val, c
 
 int piv_smoothn(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double sp, double* p_out,
                 void* stream) {
+  return piv_smoothn_flags(m, n, n_pairs, u, v, field_mask, sp, p_out, nullptr, stream);
+}
+
+int piv_smoothn_flags(int m, int n, int n_pairs, double* u, double* v, const uint8_t* field_mask, double sp,
+                      double* p_out, int* flags_out, void* stream) {
   if (!u || !v) return set_error(PIV_E_ARG, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
   void* scratch = nullptr;
   PIV_TRY(cuda_ok(cudaMallocAsync(&scratch, smoothn_scratch_bytes(m, n, n_pairs), s), "cudaMallocAsync"));
-  int rc = smoothn(m, n, n_pairs, u, v, u, v, field_mask, sp, p_out, scratch, s);
+  int rc = smoothn(m, n, n_pairs, u, v, u, v, field_mask, sp, p_out, scratch, s, flags_out);
   cudaFreeAsync(scratch, s);
   return rc;
+}
+
+int piv_plan_near_ties(piv_plan* plan, int* counts, int capacity, void* stream) {
+  if (!plan || !counts) return set_error(PIV_E_ARG, "NULL argument");
+  const int n = (int)plan->st.size() < capacity ? (int)plan->st.size() : capacity;
+  if (n <= 0) return PIV_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  PIV_TRY(cuda_ok(cudaMemcpyAsync(counts, plan->tie_counts, sizeof(int) * n, cudaMemcpyDeviceToHost, s),
+                  "near-tie copy"));
+  return cuda_ok(cudaStreamSynchronize(s), "stream synchronize");
 }
 
 int piv_plan_status(piv_plan* plan, int* status, void* stream) {
@@ -1060,7 +1104,8 @@ int piv_plan_variant_name(const piv_plan* p, int iter, int variant, char* buf, s
     if (correlate_tensor_variant_describe(c, p->cfg.dft_mode, variant, &per_sm, &async) != PIV_OK)
       return set_error(PIV_E_ARG, "variant %d out of range", variant);
     snprintf(buf, len, "tensor%s ss=%d N=%d, %d CTA/SM, %s staging",
-             p->cfg.dft_mode == PIV_DFT_TENSOR_SPLIT ? " hi/lo" : "", c.ss, c.fft_size, per_sm,
+             p->cfg.dft_mode == PIV_DFT_TENSOR_SPLIT ? " hi/lo"
+             : p->cfg.dft_mode == PIV_DFT_TENSOR_REFINED ? " refined" : "", c.ss, c.fft_size, per_sm,
              async ? "async" : "sync");
   } else {
     int r1 = 0, r2 = 0, wpc = 0, nt = 0;
@@ -1212,6 +1257,10 @@ static int batch_enqueue(piv_batch* b, const int* n_pairs, const void* const* fr
           q.peak_i = c.peak_i;
           q.peak_j = c.peak_j;
           q.win_mask = c.win_mask;
+          q.near_tie = c.near_tie;
+          q.tie_count = c.tie_count;
+          q.tie_list = c.tie_list;
+          q.tie_list_count = c.tie_list_count;
           q.win0 = m.seg_windows;
           q.height = c.height;
           q.width = c.width;

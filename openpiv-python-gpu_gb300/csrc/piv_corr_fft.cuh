@@ -79,6 +79,26 @@ PIV_D void warp_argmax(T& v, int& i) {
   }
 }
 
+// warp_argmax that also carries the second-largest value `s` (the largest
+// value at any other position): merging (v, i, s) with (v2, i2, s2), the
+// loser's best competes with the winner's second.
+template <typename T>
+PIV_D void warp_argmax2(T& v, int& i, T& s) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const T v2 = __shfl_xor_sync(0xffffffffu, v, off);
+    const int i2 = __shfl_xor_sync(0xffffffffu, i, off);
+    const T s2 = __shfl_xor_sync(0xffffffffu, s, off);
+    if (argmax_better(v2, i2, v, i)) {
+      s = s2 > v ? s2 : v;
+      v = v2;
+      i = i2;
+    } else if (v2 > s) {
+      s = v2;
+    }
+  }
+}
+
 template <typename T>
 PIV_D T warp_sum(T v) {
 #pragma unroll
@@ -106,17 +126,19 @@ PIV_D T corr_at(const Cplx<T>* w, int i, int j, int ss) {
 
 // Block-wide argmax per window over the shifted map, optionally excluding a
 // box of half width `box` (wrapped modulo N) around (bi[w], bj[w]). Results in
-// out_v[w], out_i[w]. All threads must call.
+// out_v[w], out_i[w]; with out_s (part_s then holds one value per warp), also
+// the second-largest value out_s[w], the largest at any other position. All
+// threads must call.
 template <class C, int N = C::N, typename T = typename C::T>
 PIV_D void window_argmax(const Cplx<T>* buf, int ss, int box, const int* bi, const int* bj, T* part_v,
-                         int* part_i, T* out_v, int* out_i) {
+                         int* part_i, T* out_v, int* out_i, T* part_s = nullptr, T* out_s = nullptr) {
   using L = FftLayout<C>;
   constexpr int WPC = L::WPC, NW = L::NW;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if constexpr (WPC >= NW) {
     for (int w = warp; w < WPC; w += NW) {
       const Cplx<T>* wb = buf + w * L::WIN;
-      T bv = -INFINITY;
+      T bv = -INFINITY, sv = -INFINITY;
       int bidx = 0x7fffffff;
       for (int f = lane; f < N * N; f += 32) {
         const int i = f / N, j = f % N;
@@ -127,10 +149,16 @@ PIV_D void window_argmax(const Cplx<T>* buf, int ss, int box, const int* bi, con
           if (di >= -box && di <= box && dj >= -box && dj <= box) continue;
         }
         T v = corr_at<N, T>(wb, i, j, ss);
-        if (argmax_better(v, f, bv, bidx)) { bv = v; bidx = f; }
+        if (argmax_better(v, f, bv, bidx)) { sv = bv; bv = v; bidx = f; }
+        else if (v > sv) sv = v;
       }
-      warp_argmax(bv, bidx);
-      if (lane == 0) { out_v[w] = bv; out_i[w] = bidx; }
+      if (out_s) warp_argmax2(bv, bidx, sv);
+      else warp_argmax(bv, bidx);
+      if (lane == 0) {
+        out_v[w] = bv;
+        out_i[w] = bidx;
+        if (out_s) out_s[w] = sv;
+      }
     }
     __syncthreads();
   } else {
@@ -138,7 +166,7 @@ PIV_D void window_argmax(const Cplx<T>* buf, int ss, int box, const int* bi, con
     const int w = warp / WPW, sub = warp % WPW;
     const Cplx<T>* wb = buf + w * L::WIN;
     constexpr int CHUNK = N * N / WPW;
-    T bv = -INFINITY;
+    T bv = -INFINITY, sv = -INFINITY;
     int bidx = 0x7fffffff;
     for (int f = sub * CHUNK + lane; f < (sub + 1) * CHUNK; f += 32) {
       const int i = f / N, j = f % N;
@@ -149,23 +177,35 @@ PIV_D void window_argmax(const Cplx<T>* buf, int ss, int box, const int* bi, con
         if (di >= -box && di <= box && dj >= -box && dj <= box) continue;
       }
       T v = corr_at<N, T>(wb, i, j, ss);
-      if (argmax_better(v, f, bv, bidx)) { bv = v; bidx = f; }
+      if (argmax_better(v, f, bv, bidx)) { sv = bv; bv = v; bidx = f; }
+      else if (v > sv) sv = v;
     }
-    warp_argmax(bv, bidx);
-    if (lane == 0) { part_v[warp] = bv; part_i[warp] = bidx; }
+    if (out_s) warp_argmax2(bv, bidx, sv);
+    else warp_argmax(bv, bidx);
+    if (lane == 0) {
+      part_v[warp] = bv;
+      part_i[warp] = bidx;
+      if (out_s) part_s[warp] = sv;
+    }
     __syncthreads();
     if (threadIdx.x < WPC) {
       const int ww = threadIdx.x;
       T v = part_v[ww * WPW];
       int i = part_i[ww * WPW];
+      T s2 = out_s ? part_s[ww * WPW] : (T)-INFINITY;
       for (int s = 1; s < WPW; ++s) {
-        if (argmax_better(part_v[ww * WPW + s], part_i[ww * WPW + s], v, i)) {
-          v = part_v[ww * WPW + s];
+        const T pv = part_v[ww * WPW + s];
+        if (argmax_better(pv, part_i[ww * WPW + s], v, i)) {
+          if (out_s) s2 = fmax(part_s[ww * WPW + s], v);
+          v = pv;
           i = part_i[ww * WPW + s];
+        } else if (out_s) {
+          s2 = fmax(s2, pv);
         }
       }
       out_v[ww] = v;
       out_i[ww] = i;
+      if (out_s) out_s[ww] = s2;
     }
     __syncthreads();
   }
@@ -238,8 +278,10 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
 
   const int ss = a.ss, pad = (N - ss) / 2, sp = a.spacing, nf = a.n;
   const int n_wins = a.m * a.n;
-  const long long total = (long long)a.n_pairs * n_wins;
+  // A window list selects the windows (slot s -> window win_list[s]).
+  const long long total = a.win_list ? (long long)*a.win_count : (long long)a.n_pairs * n_wins;
   const int n_tiles = (int)((total + WPC - 1) / WPC);
+  auto win_id = [&](long long slot) -> long long { return a.win_list ? (long long)a.win_list[slot] : slot; };
   const long long frame_elems = (long long)a.height * a.width;
   const int inner0 = (a.ss - a.ws) / 2, inner1 = a.ss - inner0;  // shrink: A's window rows/cols
   const bool normalize = a.normalize || pad != 0;
@@ -255,8 +297,8 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
     const long long g0 = (long long)tile * WPC;
     __syncthreads();
     if (tid < WPC) {
-      const long long g = g0 + tid;
-      int ok = g < total;
+      int ok = g0 + tid < total;
+      const long long g = ok ? win_id(g0 + tid) : 0;
       long long base = 0;
       if (ok) {
         const int pair = (int)(g / n_wins), k = (int)(g % n_wins);
@@ -390,12 +432,17 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
       T* mo = reinterpret_cast<T*>(a.maps);
       for (int e = tid; e < WPC * N * N; e += NT) {
         const int w = e / (N * N), f = e % (N * N);
-        if (g0 + w < total) mo[(g0 + w) * N * N + f] = corr_at<N, T>(buf + w * L::WIN, f / N, f % N, ss);
+        if (g0 + w < total) mo[win_id(g0 + w) * N * N + f] = corr_at<N, T>(buf + w * L::WIN, f / N, f % N, ss);
       }
     }
 
-    // First peak (first occurrence in row-major order of the shifted map).
-    window_argmax<C>(buf, ss, -1, nullptr, nullptr, part_v, part_i, pval, peak);
+    // First peak (first occurrence in row-major order of the shifted map) and,
+    // for the near-tie test, the second-largest value (into the slots of the
+    // window means, which the fill no longer needs).
+    const bool ties = a.near_tie || a.tie_count;
+    T* second = means;
+    window_argmax<C>(buf, ss, -1, nullptr, nullptr, part_v, part_i, pval, peak, part_v + NW,
+                     ties ? second : nullptr);
     if (tid < WPC) {
       pi[tid] = peak[tid] / N;
       pj[tid] = peak[tid] % N;
@@ -405,7 +452,7 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
     // Subpixel fit and displacement.
     if (tid < WPC && g0 + tid < total) {
       const int w = tid;
-      const long long g = g0 + w;
+      const long long g = win_id(g0 + w);
       const Cplx<T>* wb = buf + w * L::WIN;
       const int i = pi[w], j = pj[w];
       T isp = (T)i, jsp = (T)j;
@@ -446,6 +493,12 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
       }
       if (a.peak_i) a.peak_i[g] = i;
       if (a.peak_j) a.peak_j[g] = j;
+      if (ties) {
+        const T best = pval[w], gap = best - second[w];
+        const bool tie = valid[w] && !(gap > (T)a.tie_tol * (best < 0 ? -best : best));
+        if (a.near_tie) a.near_tie[g] = tie ? 1 : 0;
+        if (tie && a.tie_count) atomicAdd(a.tie_count, 1);
+      }
     }
 
     // Signal-to-noise ratio.
@@ -474,7 +527,7 @@ __global__ void __launch_bounds__(C::NT) k_corr_fft(CorrArgs a, Cplx<T>* gbuf) {
       }
       __syncthreads();
       if (tid < WPC && g0 + tid < total) {
-        const long long g = g0 + tid;
+        const long long g = win_id(g0 + tid);
         const T p1 = pval[tid], q2 = p2[tid];
         T s = 0;
         if (valid[tid]) {
@@ -519,7 +572,9 @@ static int launch_corr_fft(const CorrArgs& a, cudaStream_t stream) {
       return set_error(PIV_E_ARG, "correlation with fft_size %d needs %zu bytes of device scratch", C::N, bytes);
     gbuf = reinterpret_cast<Cplx<T>*>(a.scratch);
   }
-  k_corr_fft<C><<<grid, L::NT, L::SMEM, stream>>>(a, gbuf);
+  CorrArgs b = a;
+  b.tie_tol = sizeof(T) == 8 ? kTieTolF64 : kTieTolF32;
+  k_corr_fft<C><<<grid, L::NT, L::SMEM, stream>>>(b, gbuf);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_cuda_error(e, "k_corr_fft launch");
   return PIV_OK;

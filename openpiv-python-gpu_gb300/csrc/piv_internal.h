@@ -25,6 +25,10 @@ struct CorrSeg {
   int* peak_i;
   int* peak_j;
   const uint8_t* win_mask;
+  uint8_t* near_tie;  // per window: 1 where the top two map values are within the engine's tie tolerance; may be NULL
+  int* tie_count;     // incremented once per near-tie window; may be NULL
+  int* tie_list;      // refined form: scratch [n_pairs m n] for the near-tie windows' indices, and their count
+  int* tie_list_count;
   long long win0;
   int height, width, spacing, m, n, x_offset, y_offset, n_pairs;
 };
@@ -53,6 +57,24 @@ struct CorrArgs {
   size_t scratch_bytes;
   void* maps;           // optional [windows][N][N] output of the shifted correlation maps
   int* status;          // device word set to PIV_E_TIMEOUT when a bounded wait gives up (tensor engine)
+  // Near ties: a window whose second-largest map value (at another lag; lags
+  // without window overlap read as zero) is within tie_tol * |peak| of the
+  // peak gets near_tie[window] = 1 and one increment of *tie_count (both may
+  // be NULL). The engine launchers set tie_tol to the engine's map accuracy
+  // (kTieTol*): such a window's integer peak is not resolved by the engine.
+  uint8_t* near_tie;
+  int* tie_count;
+  float tie_tol;
+  // FFT engine: with win_list, only the windows win_list[0 .. *win_count)
+  // (window indices pair-major, as the outputs are indexed) are correlated.
+  const int* win_list;
+  const int* win_count;
+  // Refined tensor form: scratch for the near-tie windows' indices (n_pairs m
+  // n ints) and their count; when set, those windows are correlated again by
+  // the float32 FFT engine, which resolves their integer peaks (NULL: they
+  // keep the fp16 maps' peaks and are counted as near ties).
+  int* tie_list;
+  int* tie_list_count;
   // Multi-geometry launch (tensor engines): n_segs > 0 segments replace the
   // single geometry above (frames, sizes, outputs, mask; the window and search
   // sizes, pixel type and settings are shared), covering seg_windows windows
@@ -61,6 +83,13 @@ struct CorrArgs {
   long long seg_windows;
   CorrSeg segs[kMaxCorrSegs];
 };
+
+// Relative tie tolerances of the engines (map error relative to the map
+// maximum, with margin): float32 FFT and hi/lo split tensor products ~1e-6,
+// float64 FFT ~1e-15, fp16-operand tensor products ~6e-4.
+constexpr float kTieTolF32 = 1.0f / 131072.0f;        // 2^-17
+constexpr float kTieTolF64 = 1.0f / 1099511627776.0f;  // 2^-40
+constexpr float kTieTolF16 = 1.0f / 512.0f;            // 2^-9
 
 // Launch variants (tile shape, radix split, CTAs per SM, staging) of the two
 // engines; variant 0 is the default, and an out-of-range variant runs it.
@@ -73,6 +102,16 @@ int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t 
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode);
 int correlate_tensor_variant_count(const CorrArgs& a, int dft_mode);
 int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int variant, int* per_sm, int* async);
+// Peak refinement after a tensor-core pass (float32 fields, n_fft 2, window =
+// search size of 16, 32 or 64 px, no S2N): the five values of the subpixel
+// stencil around each window's integer peak (peak_i / peak_j, as the engine
+// wrote them) are recomputed in float32 from the frames by direct sums, and
+// u, v are rewritten from them.
+bool refine_supported(const CorrArgs& a);
+int refine_peaks(const CorrArgs& a, cudaStream_t stream);
+// Indices of the windows with near_tie set into list (window order not
+// kept), their number into *count (reset first).
+int compact_near_ties(const uint8_t* near_tie, long long windows, int* list, int* count, cudaStream_t stream);
 // One bounded mbarrier wait that nothing completes; writes PIV_E_TIMEOUT to *status_dev.
 int bounded_wait_probe(uint32_t max_polls, int* status_dev, cudaStream_t stream);
 
@@ -139,8 +178,10 @@ int combine_fields(int count, const void* u_corr, const void* v_corr, int corr_d
 
 // smoothn.
 size_t smoothn_scratch_bytes(int m, int n, int n_pairs);
+// flags (device [n_pairs], may be NULL) receives the PIV_SMOOTH_* bits of each pair.
 int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out, double* v_out,
-            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream);
+            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream,
+            int* flags = nullptr);
 
 // Final scaling u * scaling_par / dt (gpu_process.py:847-849).
 int scale_fields(int count, const double* u, const double* v, double scaling, double dt, int fp32, double* uo,

@@ -17,6 +17,7 @@
 
 #include "piv_common.cuh"
 #include "piv_internal.h"
+#include "piv_lbfgsb1.cuh"
 
 namespace piv {
 
@@ -43,14 +44,19 @@ static size_t weighted_pair_bytes(size_t mn) { return align_up(11 * mn * 8 + mn 
 // The DCT matrices of the weighted path as hi/lo float pairs (2 (m^2 + n^2) floats).
 static size_t weighted_matrix_bytes(int m, int n) { return align_up(2 * ((size_t)m * m + (size_t)n * n) * 4); }
 
-size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
+// Scratch of the unweighted path (no field mask) and of the weighted path.
+static size_t smoothn_scratch_bytes_path(int m, int n, int n_pairs, bool weighted_path) {
   const size_t mn = (size_t)m * n;
   const size_t shared = align_up((size_t)m * m * 8) + align_up((size_t)n * n * 8) + align_up(mn * 8) +
                         align_up((size_t)n_pairs * 8);
-  const size_t plain = align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared +
-                       align_up(mn * n_pairs * 4) + align_up(mn * 4) + align_up((size_t)m * m * 8) +
-                       align_up((size_t)n * n * 8);
-  const size_t weighted = shared + weighted_matrix_bytes(m, n) + weighted_pair_bytes(mn) * n_pairs;
+  if (weighted_path) return shared + weighted_matrix_bytes(m, n) + weighted_pair_bytes(mn) * n_pairs;
+  return align_up(2 * mn * n_pairs * 8) * 2 + align_up(mn * n_pairs * 8) + shared + align_up(mn * n_pairs * 4) +
+         align_up(mn * 4) + align_up((size_t)m * m * 8) + align_up((size_t)n * n * 8);
+}
+
+size_t smoothn_scratch_bytes(int m, int n, int n_pairs) {
+  const size_t plain = smoothn_scratch_bytes_path(m, n, n_pairs, false);
+  const size_t weighted = smoothn_scratch_bytes_path(m, n, n_pairs, true);
   return plain > weighted ? plain : weighted;
 }
 
@@ -284,6 +290,19 @@ __global__ void k_f2(long long mn, int n_pairs, const double* __restrict__ fd, d
 
 static constexpr int kGcvThreads = 512;
 
+// Flags of SmoothnGPU's log messages (gpu_smoothn.py:218-222, 429-439): with
+// GCV, the smoothing parameter within 0.1 (in log10) of its lower or else its
+// upper bound; the iteration reaching its last allowed step.
+PIV_D int smooth_flags(bool is_auto, double p, double pmin, double pmax, bool last_iter) {
+  int f = 0;
+  if (is_auto) {
+    if (fabs(p - pmin) < 0.1) f |= PIV_SMOOTH_S_LOWER;
+    else if (fabs(p - pmax) < 0.1) f |= PIV_SMOOTH_S_UPPER;
+  }
+  if (last_iter) f |= PIV_SMOOTH_MAX_ITERS;
+  return f;
+}
+
 // 1/d for d >= 1 from the float32 reciprocal and two Newton steps in float64:
 // within an ulp or two of the rounded quotient, at a fraction of the cost of
 // a float64 division (float64 throughput on this GPU is low).
@@ -295,91 +314,19 @@ PIV_D double rcp_fast(double d) {
   return fma(r, e, r);
 }
 
-struct GcvEval {
-  const double* f2;
-  const double* lam2;
-  const float* f2f;
-  const float* lam2f;
-  long long mn;
-  double n_finite;
-  int n_fields;
-};
-
-// GCV score at p (gpu_smoothn.py:353-372, w_mean > 0.9 branch). All threads call.
-PIV_D double gcv_score(const GcvEval& g, double p, double* red) {
-  const double s = pow(10.0, p);
-  double rss = 0.0, tr = 0.0;
-  for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
-    const double gm = rcp_fast(1.0 + s * g.lam2[e]);
-    const double d = gm - 1.0;
-    rss += g.f2[e] * d * d;
-    tr += gm;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    rss += __shfl_xor_sync(~0u, rss, o);
-    tr += __shfl_xor_sync(~0u, tr, o);
-  }
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) { red[w] = rss; red[32 + w] = tr; }
-  __syncthreads();
-  double trss = 0.0, ttr = 0.0;
-  for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
-  const double q = 1.0 - ttr / (double)g.mn;
-  return trss / g.n_finite / (q * q) / g.n_fields;
-}
-
-// Finite-difference gradient as the reference's L-BFGS-B call computes it
-// (absolute step 1e-8, backward at the upper bound).
-PIV_D double gcv_grad(const GcvEval& g, double p, double f0, double pmax, double* red) {
-  const double h = 1e-8;
-  if (p + h <= pmax) return (gcv_score(g, p + h, red) - f0) / h;
-  return (f0 - gcv_score(g, p - h, red)) / h;
-}
-
-// GCV score with float32 terms and float64 sums: 1 - gamma = s l / (1 + s l)
-// is formed directly (no cancellation), so every term is a product of
-// positive factors within a few float32 ulps; the rounding errors of the
-// terms are independent, and their sum over the field stays near 1e-9 of the
-// score. s = 10^p is formed once per CTA in float64. Used to rank the scan
-// points and for the bounded local search; the gradient test, which divides
-// score differences by 1e-8, uses the float64 score.
-PIV_D double gcv_score_fast(const GcvEval& g, double p, double* red) {
-  if (threadIdx.x == 0) red[64] = pow(10.0, p);
-  __syncthreads();
-  const float s = (float)red[64];
-  float rss = 0.f, tr = 0.f;
-  for (long long e = threadIdx.x; e < g.mn; e += blockDim.x) {
-    const float sl = s * g.lam2f[e];
-    const float d = sl * __frcp_rn(1.0f + sl);  // 1 - gamma
-    rss = fmaf(g.f2f[e] * d, d, rss);
-    tr += d;
-  }
-  double drss = rss, dtr = tr;
-  for (int o = 16; o > 0; o >>= 1) {
-    drss += __shfl_xor_sync(~0u, drss, o);
-    dtr += __shfl_xor_sync(~0u, dtr, o);
-  }
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) { red[w] = drss; red[32 + w] = dtr; }
-  __syncthreads();
-  double trss = 0.0, ttr = 0.0;
-  for (int k = 0; k < nw; ++k) { trss += red[k]; ttr += red[32 + k]; }
-  const double q = ttr / (double)g.mn;
-  return trss / g.n_finite / (q * q) / g.n_fields;
-}
-
 // One CTA per pair. Every thread takes part in the sums of each score; the
-// search itself (scan bookkeeping, gradient test, Brent's iteration: scalar
-// float64 work) runs in warp 0 alone, which announces each next point as
-// s = 10^p in shared memory. Float64 runs at a small fraction of the float32
-// rate on this GPU, so the search is not repeated by all 16 warps. The
-// operations and their order are those of gcv_score / gcv_score_fast.
+// search itself (scan bookkeeping and the L-BFGS-B steps: scalar float64
+// work) runs in warp 0 alone, which announces each next point as s = 10^p in
+// shared memory. Float64 runs at a small fraction of the float32 rate on this
+// GPU, so the search is not repeated by all 16 warps. The fast score (float32
+// terms, float64 sums: 1 - gamma = s l / (1 + s l) formed without
+// cancellation, each term within a few float32 ulps, the score within ~1e-9)
+// only ranks the scan points; the L-BFGS-B evaluations, whose difference
+// quotients divide score differences by 1e-8, use the float64 score.
 __global__ void __launch_bounds__(kGcvThreads)
 k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __restrict__ lam2,
       const float* __restrict__ f2f, const float* __restrict__ lam2f, double pmin, double pmax,
-      double* __restrict__ p_out) {
+      double* __restrict__ p_out, int* __restrict__ flags) {
   __shared__ double red[64];
   __shared__ double sh_s;  // 10^p of the next score
   __shared__ int sh_go;    // warp 0's decision for the next step
@@ -447,96 +394,66 @@ k_gcv(int m, int n, int n_pairs, const double* __restrict__ f2, const double* __
     }
     return f;
   };
-  // Announces p (thread 0) and makes it visible; the barrier also orders the
-  // previous score's reads of red[] before the next score's writes.
-  auto announce = [&](double p) {
-    if (threadIdx.x == 0) sh_s = pow(10.0, p);
+  // Announces p (thread 0) and whether the search goes on, and makes both
+  // visible; the barrier also orders the previous score's reads of red[]
+  // before the next score's writes.
+  auto announce = [&](double p, bool go) {
+    if (threadIdx.x == 0) {
+      sh_s = pow(10.0, p);
+      sh_go = go;
+    }
     __syncthreads();
   };
-  // 10-point scan (gpu_smoothn.py:182-188), ranked with the fast score; the
-  // best point is scored in float64 for the gradient test.
-  double best_p = pmin, best_f = INFINITY;
+  // 10-point scan (gpu_smoothn.py:182-188), ranked with the fast score; when
+  // other points score within 1e-6 of the best, those points are scored
+  // again in float64 and the first minimum among them is kept (np.argmin).
+  double fast[10];
+  double best_f = INFINITY;
   for (int k = 0; k < 10; ++k) {
     const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
-    announce(pk);
-    const double fk = score_fast();
-    if (k == 0 || fk < best_f) { best_f = fk; best_p = pk; }
+    announce(pk, true);
+    fast[k] = score_fast();
+    if (fast[k] < best_f) best_f = fast[k];
   }
-  double p = best_p;
-  announce(p);
-  const double f0 = score();
-  // Finite-difference gradient as the reference's L-BFGS-B call computes it
-  // (absolute step 1e-8, backward at the upper bound).
-  const double h = 1e-8;
-  const bool fwd = p + h <= pmax;
-  announce(fwd ? p + h : p - h);
-  const double fh = score();
-  if (threadIdx.x == 0) {
-    const double g0 = fwd ? (fh - f0) / h : (f0 - fh) / h;
-    const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
-    sh_go = !(fabs(pg) <= 1e-5);
-  }
-  announce(p);  // also publishes sh_go
-  if (sh_go) {
-    // Brent's bounded minimisation on the bracket around the scan point.
-    const double step = (pmax - pmin) / 9.0;
-    double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
-    const double cg = 0.3819660112501051;
-    const double fs = score_fast();
-    double x = p, w = p, v = p, fx = fs, fw = fs, fv = fs, d = 0.0, e = 0.0;
-    for (int it = 0; it < 200; ++it) {
-      double u = 0.0;
-      if (w0) {
-        const double xm = 0.5 * (a + b);
-        const double tol1 = 1e-8 * fabs(x) + 1e-10, tol2 = 2.0 * tol1;
-        const bool done = fabs(x - xm) <= tol2 - 0.5 * (b - a);
-        if (!done) {
-          bool golden = true;
-          if (fabs(e) > tol1) {
-            double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
-            q = 2.0 * (q - r);
-            if (q > 0) pp = -pp;
-            q = fabs(q);
-            const double etemp = e;
-            e = d;
-            if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
-              d = pp / q;
-              const double uu = x + d;
-              if (uu - a < tol2 || b - uu < tol2) d = xm >= x ? tol1 : -tol1;
-              golden = false;
-            }
-          }
-          if (golden) {
-            e = (x >= xm) ? a - x : b - x;
-            d = cg * e;
-          }
-          u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
-        }
-        if (lane == 0) {
-          sh_go = !done;
-          if (!done) sh_s = pow(10.0, u);
-        }
-      }
-      __syncthreads();
-      if (!sh_go) break;
-      const double fu = score_fast();
-      if (w0) {
-        if (fu <= fx) {
-          if (u >= x) a = x; else b = x;
-          v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
-        } else {
-          if (u < x) a = u; else b = u;
-          if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
-          else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
-        }
-      }
+  unsigned near_best = 0;  // scan points within 1e-6 of the best fast score (warp 0)
+  for (int k = 0; k < 10; ++k)
+    if (fast[k] <= best_f + 1e-6 * fabs(best_f)) near_best |= 1u << k;
+  if (threadIdx.x == 0) sh_go = __popc(near_best) > 1 ? (int)near_best : 0;
+  __syncthreads();
+  const unsigned rescore = (unsigned)sh_go;
+  double p0 = pmin;
+  if (rescore) {
+    double best64 = INFINITY;
+    for (int k = 0; k < 10; ++k) {
+      if (!((rescore >> k) & 1u)) continue;
+      const double pk = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
+      announce(pk, true);
+      const double fk = score();
+      if (fk < best64) { best64 = fk; p0 = pk; }
     }
-    p = x;
-    // A minimum within the tolerance of a bound sits on the bound (a projected method lands there).
-    if (p - pmin < 1e-9) p = pmin;
-    if (pmax - p < 1e-9) p = pmax;
+  } else {
+    for (int k = 9; k >= 0; --k)
+      if (fast[k] == best_f) p0 = ((double)k * (1.0 / 9.0)) * (pmax - pmin) + pmin;
   }
-  if (threadIdx.x == 0) p_out[pair] = p;
+  // L-BFGS-B from the scan point (gpu_smoothn.py:191-193), its scalar state
+  // in warp 0; every evaluation is the float64 score at the point and at its
+  // forward-difference neighbour.
+  Lb1 lb;
+  lb_init(lb, p0, pmin, pmax);
+  for (int ev = 0; ev < kLbMaxEvals; ++ev) {
+    const double xt = lb.xt, xs = lb_fd_point(xt, pmin, pmax);
+    announce(xt, !lb.done);
+    if (!sh_go) break;
+    const double f = score();
+    announce(xs, true);
+    const double fh = score();
+    if (w0) lb_feed(lb, f, (fh - f) / (xs - xt));
+  }
+  const double p = lb.x;
+  if (threadIdx.x == 0) {
+    p_out[pair] = p;
+    if (flags) flags[pair] = smooth_flags(true, p, pmin, pmax, false);
+  }
 }
 
 // fd *= gamma(p) for both fields of each pair. Grid: x over the 2 mn
@@ -678,8 +595,10 @@ PIV_D double sw_gcv(const SwCtx& c, double p) {
   return rss / c.n_finite / (q * q) / 2.0;
 }
 
-// The search of k_gcv (scan on the first call, then the projected-gradient
-// stopping test and Brent's bounded minimisation around the start point).
+// The search of k_gcv: the 10-point scan on the first call (float64 scores,
+// np.argmin's first minimum), then L-BFGS-B from the start point
+// (gpu_smoothn.py:179-193). Every thread runs the same scalar steps on the
+// same scores (sw_gcv returns the CTA's sums to every thread).
 PIV_D double sw_search(const SwCtx& c, double p, bool have_p, double pmin, double pmax) {
   if (!have_p) {
     double best_f = INFINITY;
@@ -689,59 +608,23 @@ PIV_D double sw_search(const SwCtx& c, double p, bool have_p, double pmin, doubl
       if (k == 0 || fk < best_f) { best_f = fk; p = pk; }
     }
   }
-  const double f0 = sw_gcv(c, p);
-  const double h = 1e-8;
-  const double g0 = p + h <= pmax ? (sw_gcv(c, p + h) - f0) / h : (f0 - sw_gcv(c, p - h)) / h;
-  const double pg = g0 < 0 ? fmax(p - pmax, g0) : fmin(p - pmin, g0);
-  if (fabs(pg) <= 1e-5) return p;
-  const double step = (pmax - pmin) / 9.0;
-  double a = fmax(pmin, p - step), b = fmin(pmax, p + step);
-  const double cg = 0.3819660112501051;
-  double x = p, w = p, v = p, fx = f0, fw = f0, fv = f0, d = 0.0, e = 0.0;
-  for (int it = 0; it < 200; ++it) {
-    const double xm = 0.5 * (a + b);
-    const double tol1 = 1e-11 * fabs(x) + 1e-13, tol2 = 2.0 * tol1;
-    if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
-    bool golden = true;
-    if (fabs(e) > tol1) {
-      double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), pp = (x - v) * q - (x - w) * r;
-      q = 2.0 * (q - r);
-      if (q > 0) pp = -pp;
-      q = fabs(q);
-      const double etemp = e;
-      e = d;
-      if (!(fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x))) {
-        d = pp / q;
-        const double u = x + d;
-        if (u - a < tol2 || b - u < tol2) d = xm >= x ? tol1 : -tol1;
-        golden = false;
-      }
-    }
-    if (golden) {
-      e = (x >= xm) ? a - x : b - x;
-      d = cg * e;
-    }
-    const double u = fabs(d) >= tol1 ? x + d : x + (d >= 0 ? tol1 : -tol1);
-    const double fu = sw_gcv(c, u);
-    if (fu <= fx) {
-      if (u >= x) a = x; else b = x;
-      v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
-    } else {
-      if (u < x) a = u; else b = u;
-      if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
-      else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
-    }
+  Lb1 lb;
+  lb_init(lb, p, pmin, pmax);
+  for (int ev = 0; ev < kLbMaxEvals && !lb.done; ++ev) {
+    const double x = lb.xt, xs = lb_fd_point(x, pmin, pmax);
+    const double f = sw_gcv(c, x);
+    const double fh = sw_gcv(c, xs);
+    lb_feed(lb, f, (fh - f) / (xs - x));
   }
-  if (x - pmin < 1e-9) x = pmin;
-  if (pmax - x < 1e-9) x = pmax;
-  return x;
+  return lb.x;
 }
 
 __global__ void __launch_bounds__(kSwThreads)
 k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double* u_out, double* v_out,
                    const uint8_t* __restrict__ mask,
                    double fixed_p, int is_auto, double pmin, double pmax, DfMats mats,
-                   const double* __restrict__ lam2, unsigned char* scratch, size_t pair_bytes, double* p_out) {
+                   const double* __restrict__ lam2, unsigned char* scratch, size_t pair_bytes, double* p_out,
+                   int* flags) {
   __shared__ double red[32];
   __shared__ int s_flag;
   const int pair = blockIdx.x, mn = m * n, tid = threadIdx.x, nt = blockDim.x;
@@ -829,7 +712,9 @@ k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double*
   const double rf = weighted ? 1.75 : 1.0;
   double p = fixed_p;
   bool have_p = !is_auto;
+  int k_last = 0;  // index of the last iteration run
   for (int k = 0; k < 100; ++k) {
+    k_last = k;
     for (int e = tid; e < 2 * mn; e += nt) {
       const double wv = c.w[e % mn];
       c.t[e] = wv * (c.f[e] - c.z[e]) + c.z[e];
@@ -868,11 +753,12 @@ k_smoothn_weighted(int m, int n, const double* u_in, const double* v_in, double*
     v_out[off + e] = in_mask ? 0.0 : c.z[mn + e];
   }
   if (tid == 0 && p_out) p_out[pair] = p;
+  if (tid == 0 && flags) flags[pair] = smooth_flags(is_auto != 0, p, pmin, pmax, k_last == 99);
 }
 
 static int smoothn_weighted(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out,
                             double* v_out, const uint8_t* field_mask, double s, double* p_out, void* scratch,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, int* flags) {
   const size_t mn = (size_t)m * n;
   char* p = (char*)scratch;
   double* cm = (double*)p; p += align_up((size_t)m * m * 8);
@@ -900,20 +786,23 @@ static int smoothn_weighted(int m, int n, int n_pairs, const double* u_in, const
   }
   k_smoothn_weighted<<<n_pairs, kSwThreads, 0, stream>>>(m, n, u_in, v_in, u_out, v_out, field_mask,
                                                           is_auto ? 0.0 : log10(s), is_auto ? 1 : 0, pmin, pmax, mats,
-                                                          lam2, (unsigned char*)p, weighted_pair_bytes(mn), p_out);
+                                                          lam2, (unsigned char*)p, weighted_pair_bytes(mn), p_out,
+                                                          flags);
   return check("k_smoothn_weighted");
 }
 
 int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, double* u_out, double* v_out,
-            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream) {
+            const uint8_t* field_mask, double s, double* p_out, void* scratch, cudaStream_t stream, int* flags) {
   const long long mn = (long long)m * n;
   if (n_pairs == 0 || mn == 0) return PIV_OK;
+  if (flags && (mn < 2 || (!field_mask && s > 0))) cudaMemsetAsync(flags, 0, sizeof(int) * n_pairs, stream);
   if (mn < 2) {
     cudaMemcpyAsync(u_out, u_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
     cudaMemcpyAsync(v_out, v_in, mn * n_pairs * 8, cudaMemcpyDeviceToDevice, stream);
     return check("smoothn copy");
   }
-  if (field_mask) return smoothn_weighted(m, n, n_pairs, u_in, v_in, u_out, v_out, field_mask, s, p_out, scratch, stream);
+  if (field_mask)
+    return smoothn_weighted(m, n, n_pairs, u_in, v_in, u_out, v_out, field_mask, s, p_out, scratch, stream, flags);
   SmoothScratch sc = carve(scratch, m, n, n_pairs);
   const int bs = 256;
   k_dct_matrix<<<(m * m + bs - 1) / bs, bs, 0, stream>>>(m, sc.cm);
@@ -943,7 +832,8 @@ int smoothn(int m, int n, int n_pairs, const double* u_in, const double* v_in, d
     const double pmin = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_max)) / 4.0 / a_max, 2.0) - 1.0) / 16.0);
     const double pmax = log10((pow((1.0 + sqrt(1.0 + 8.0 * a_min)) / 4.0 / a_min, 2.0) - 1.0) / 16.0);
     k_f2<<<(unsigned)((mn * n_pairs + bs - 1) / bs), bs, 0, stream>>>(mn, n_pairs, sc.tmp, sc.f2, sc.f2f);
-    k_gcv<<<n_pairs, kGcvThreads, 0, stream>>>(m, n, n_pairs, sc.f2, sc.lam2, sc.f2f, sc.lam2f, pmin, pmax, sc.p);
+    k_gcv<<<n_pairs, kGcvThreads, 0, stream>>>(m, n, n_pairs, sc.f2, sc.lam2, sc.f2f, sc.lam2f, pmin, pmax, sc.p,
+                                               flags);
     pvec = sc.p;
     rc = check("k_gcv");
     if (rc) return rc;
@@ -984,12 +874,18 @@ namespace piv {
 // in a fixed device array of this file, sized for modest fields. Every GPU
 // that loads the library holds the array until the process exits.
 // ---------------------------------------------------------------------------
-static constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB: e.g. 4 pairs of 128 x 128 fields
+// 4 MiB: e.g. 4 pairs of 128 x 128 fields, or with a field mask 2 pairs of
+// 127 x 127 (the weighted path keeps more per pair).
+static constexpr size_t kNoAllocScratchBytes = 4u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch, looked up once per device. In host code
-// the array's name is only a host-side stand-in, never a device address.
-static void* noalloc_scratch_address(int* rc) {
+// Device address of g_noalloc_scratch in the current context. In host code
+// the array's name is only a host-side stand-in, never a device address. The
+// address is looked up on every call made outside stream capture (so a call
+// after a device reset, which reloads the module at a new address, gets the
+// new one) and remembered per device for calls made while `stream` is being
+// captured, which reuse the address of the device's last uncaptured call.
+static void* noalloc_scratch_address(cudaStream_t stream, int* rc) {
   static std::mutex mu;
   static void* addr[64] = {nullptr};
   int dev = 0;
@@ -1002,8 +898,20 @@ static void* noalloc_scratch_address(int* rc) {
     *rc = set_error(PIV_E_UNSUPPORTED, "device index %d out of range", dev);
     return nullptr;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) {
+    *rc = set_cuda_error(e, "cudaStreamIsCapturing");
+    return nullptr;
+  }
   std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+  if (cap != cudaStreamCaptureStatusNone) {
+    if (!addr[dev]) {
+      *rc = set_error(PIV_E_ARG,
+                      "piv_smoothn_noalloc: the first call on device %d must come before any stream capture", dev);
+      return nullptr;
+    }
+  } else {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
@@ -1023,14 +931,22 @@ extern "C" int piv_smoothn_noalloc(int m, int n, int n_pairs, double* u, double*
   using namespace piv;
   if (!u || !v) return set_error(PIV_E_ARG, "NULL argument");
   if (m <= 0 || n <= 0 || n_pairs <= 0) return set_error(PIV_E_ARG, "empty field (m=%d, n=%d, pairs=%d)", m, n, n_pairs);
-  const size_t need = smoothn_scratch_bytes(m, n, n_pairs);
+  // The kernels index with 32-bit products m n, m m and n n and launch one
+  // block row per pair: refuse shapes beyond those before sizing the scratch
+  // (whose 64-bit byte counts then cannot wrap).
+  const long long lim = 1LL << 31;
+  if ((long long)m * n >= lim || (long long)m * m >= lim || (long long)n * n >= lim || n_pairs > 65535)
+    return set_error(PIV_E_ARG, "piv_smoothn_noalloc: field %d x %d with %d pair(s) is beyond the kernels' limits",
+                     m, n, n_pairs);
+  const bool weighted = field_mask != nullptr && (long long)m * n >= 2;
+  const size_t need = smoothn_scratch_bytes_path(m, n, n_pairs, weighted);
   if (need > kNoAllocScratchBytes)
     return set_error(PIV_E_ARG,
-                     "piv_smoothn_noalloc: %d pair(s) of %d x %d fields need %zu bytes of scratch, more than its "
+                     "piv_smoothn_noalloc: %d pair(s) of %d x %d %sfields need %zu bytes of scratch, more than its "
                      "fixed %zu bytes; use piv_smoothn or fewer/smaller fields",
-                     n_pairs, m, n, need, kNoAllocScratchBytes);
+                     n_pairs, m, n, weighted ? "masked " : "", need, kNoAllocScratchBytes);
   int rc = PIV_OK;
-  void* scratch = noalloc_scratch_address(&rc);
+  void* scratch = noalloc_scratch_address((cudaStream_t)stream, &rc);
   if (!scratch) return rc;
   return smoothn(m, n, n_pairs, u, v, u, v, field_mask, s, p_out, scratch, (cudaStream_t)stream);
 }

@@ -32,6 +32,7 @@
 #include <algorithm>
 
 #include "piv_common.cuh"
+#include "piv_corr_common.cuh"
 #include "piv_internal.h"
 #include "piv_tcgen05.cuh"
 
@@ -150,25 +151,47 @@ PIV_D unsigned long long peak_key(float best, int idx) {
 }
 PIV_D int peak_index(unsigned long long key) { return (int)~(unsigned)key; }
 
-// Subpixel peak (gpu_process.py:1256-1294) from the five map values.
-PIV_D void subpixel_fit(int subpixel, int pi_, int pj, float c, float cd, float cu, float cl, float cr, float& isp,
-                        float& jsp) {
-  const float eps = 1e-7f;
-  isp = (float)pi_;
-  jsp = (float)pj;
-  if (subpixel == PIV_SUBPIXEL_GAUSSIAN) {
-    if (c > 0 && cd > 0 && cu > 0 && cl > 0 && cr > 0) {
-      c = logf(c); cd = logf(cd); cu = logf(cu); cl = logf(cl); cr = logf(cr);
-      isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-      jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
+// Order-preserving 32-bit key of a float (unsigned comparison of keys orders
+// the values; -0 folded into +0) and its inverse.
+PIV_D unsigned fkey(float x) {
+  const unsigned b = __float_as_uint(x + 0.0f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+PIV_D float fkey_inv(unsigned k) { return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k); }
+constexpr unsigned kKeyNegInf = 0x007fffffu;  // fkey(-inf)
+
+// Near-tie test of the windows of a tile, run by the 32 lanes of one warp
+// (W windows, 32 / W lanes each): the second-largest map value of window ww
+// is the larger of sec_key[ww] (the largest row maximum over the rows other
+// than the peak row) and the largest value of the peak row other than the
+// peak, read from prow(ww) (natural columns; shifted column j at natural
+// column j ^ N/2; lags without window overlap read as zero). Returns, in lane
+// l < W, whether window l's top two values are within tol * |peak|.
+template <int N, int W, class PeakOf, class RowOf>
+PIV_D bool tile_near_ties(int lane, const unsigned* sec_key, float tol, PeakOf peak_of, RowOf row_of) {
+  constexpr int HN = N / 2, GL = 32 / W, PER = N / GL;
+  static_assert(PER % 4 == 0, "whole float4 chunks per lane");
+  const int ww = lane / GL, seg = lane % GL;
+  const int pidx = peak_of(ww), pi_ = pidx / N, pj = pidx % N;
+  const float* prow = row_of(ww);
+  float sec = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < PER; k += 4) {
+    const float4 q4 = *reinterpret_cast<const float4*>(prow + seg * PER + k);
+    const float x4[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int j = (seg * PER + k + e) ^ HN;
+      const float x = (pi_ == 0 || j == 0) ? 0.f : x4[e];
+      if (j != pj) sec = fmaxf(sec, x);
     }
-  } else if (subpixel == PIV_SUBPIXEL_PARABOLIC) {
-    isp = add_rn((float)pi_, div_rn(mul_rn(0.5f, sub_rn(cd, cu)), add_rn(add_rn(sub_rn(cd, mul_rn(2.f, c)), cu), eps)));
-    jsp = add_rn((float)pj, div_rn(mul_rn(0.5f, sub_rn(cl, cr)), add_rn(add_rn(sub_rn(cl, mul_rn(2.f, c)), cr), eps)));
-  } else {
-    isp = add_rn((float)pi_, div_rn(sub_rn(cu, cd), add_rn(add_rn(add_rn(cd, c), cu), eps)));
-    jsp = add_rn((float)pj, div_rn(sub_rn(cr, cl), add_rn(add_rn(add_rn(cl, c), cr), eps)));
   }
+#pragma unroll
+  for (int o = 1; o < GL; o <<= 1) sec = fmaxf(sec, __shfl_xor_sync(0xffffffffu, sec, o));
+  sec = fmaxf(sec, fkey_inv(sec_key[ww]));
+  const float best = (pi_ == 0 || pj == 0) ? 0.f : prow[pj ^ HN];
+  const bool tie = !(best - sec > tol * fabsf(best));
+  return __shfl_sync(0xffffffffu, tie ? 1 : 0, (lane % W) * GL) != 0;
 }
 
 // Byte offset of element (r, k) in a no-swizzle K-major tile with K columns.
@@ -289,39 +312,11 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
   return q;
 }
 
-// The launch's segment table in shared memory (one segment built from the
-// single geometry of `a` when a.n_segs == 0); returns the segment count. All
-// threads call it; it ends with a barrier.
-PIV_D int load_segments(const CorrArgs& a, CorrSeg* seg_s) {
-  const int n = a.n_segs > 0 ? a.n_segs : 1;
-  if ((int)threadIdx.x < n) {
-    CorrSeg q;
-    if (a.n_segs > 0) {
-#pragma unroll
-      for (int k = 0; k < kMaxCorrSegs; ++k)  // static indices keep the table in parameter space
-        if (k == (int)threadIdx.x) q = a.segs[k];
-    } else {
-      q.frame_a = a.frame_a;
-      q.frame_b = a.frame_b;
-      q.u = a.u;
-      q.v = a.v;
-      q.peak_i = a.peak_i;
-      q.peak_j = a.peak_j;
-      q.win_mask = a.win_mask;
-      q.win0 = 0;
-      q.height = a.height;
-      q.width = a.width;
-      q.spacing = a.spacing;
-      q.m = a.m;
-      q.n = a.n;
-      q.x_offset = a.x_offset;
-      q.y_offset = a.y_offset;
-      q.n_pairs = a.n_pairs;
-    }
-    seg_s[threadIdx.x] = q;
-  }
-  __syncthreads();
-  return n;
+// Whether any segment asks for near-tie flags or counts.
+PIV_D bool any_tie_output(const CorrSeg* seg_s, int n_seg) {
+  bool any = false;
+  for (int k = 0; k < n_seg; ++k) any = any || seg_s[k].near_tie != nullptr || seg_s[k].tie_count != nullptr;
+  return any;
 }
 
 // ASYNC: float32 frames whose window rows start on 16-byte boundaries. The
@@ -346,6 +341,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float pk_val[W][NPART];
   __shared__ int pk_idx[W][NPART];
+  __shared__ unsigned sec_key[W];    // per window: key of the largest row maximum outside the peak row
 
   const int tid = threadIdx.x;
   const int t = tid & 127;           // TMEM lane (row of the tile) of this thread
@@ -472,12 +468,16 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     }
   };
 
-  if (tid < W) window_setup(blockIdx.x, 0);
+  if (tid < W) {
+    window_setup(blockIdx.x, 0);
+    sec_key[tid] = kKeyNegInf;
+  }
   __syncthreads();
   if (ASYNC) {
     stage_async(0);
     cp_async_commit();
   }
+  const bool ties = any_tie_output(seg_s, n_seg);
 
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
     // Subpixel fit and outputs of window ww with flat peak index pidx (its
     // neighbour rows in nbrow).
-    auto finish = [&](int ww, int pidx) {
+    auto finish = [&](int ww, int pidx, bool tie) {
       const int pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
@@ -719,7 +719,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
+      tie = tie && win_valid[sl][ww];
+      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
     };
+    auto peak_row = [&](int ww) { return nbrow + (ww * 3 + 1) * N; };
     if constexpr (N == 32 && TPL == 1) {
       // One window per warp and row tile (N = 32 rows): the warp finds its
       // window's peak by shuffles and the lanes of the rows next to it store
@@ -741,6 +745,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         first_max<N>(rowc, best, bj);
         int idx = i * N + bj;
         if (i == 0) { best = 0.f; idx = 0; }
+        const float rbest = best;
         warp_first_max(best, idx);
         if (a.maps && g0 + w < total) {
           const int ue = -sc_e[0][w] - sc_e[1][w];
@@ -749,7 +754,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
         }
         const int pi_ = idx / N, pj = idx % N;
-        if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1) {
+        if (ties) {  // the window's rows are this warp's: its largest row maximum outside the peak row
+          const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(rbest));
+          if (lane == 0) sec_key[w] = k;
+        }
+        if ((ties && i == pi_) || (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1)) {
           float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
 #pragma unroll
           for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
@@ -757,8 +766,12 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         if (lane == 0) pk_idx[w][0] = idx;
       }
       __syncthreads();
-      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
+      bool tie = false;
+      if (ties && warp == 0)
+        tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return pk_idx[ww][0]; }, peak_row);
+      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0], tie);
     } else {
+      float rbest[2 / TPL];  // this thread's row maxima
 #pragma unroll
       for (int ri = 0; ri < 2 / TPL; ++ri) {
         const int rt = TPL == 2 ? half : ri;
@@ -777,6 +790,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         first_max<N>(rowc, best, bj);
         int idx = i * N + bj;
         if (i == 0) { best = 0.f; idx = 0; }
+        rbest[ri] = best;
         warp_first_max(best, idx);
         if (lane == 0) {
           pk_val[w][r / 32] = best;
@@ -809,7 +823,12 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         const int rt = TPL == 2 ? half : ri;
         const int m = rt * 128 + t, w = m / N, r = m % N, i = r ^ HN;
         const int pidx = window_peak(w), pi_ = pidx / N, pj = pidx % N;
-        const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
+        if (ties) {  // the warp's largest row maximum outside the peak row (a warp's rows share a window)
+          const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(rbest[ri]));
+          if (lane == 0) atomicMax(&sec_key[w], k);
+        }
+        const bool mine = (ties && i == pi_) ||
+                          (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
         if (__any_sync(0xffffffffu, mine)) {
           float v[N];
 #pragma unroll
@@ -825,7 +844,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
       }
       __syncthreads();
-      if (tid < W && g0 + tid < total) finish(tid, window_peak(tid));
+      bool tie = false;
+      if (ties && warp == 0) tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, window_peak, peak_row);
+      if (tid < W && g0 + tid < total) finish(tid, window_peak(tid), tie);
+    }
+    if (warp == 0) {  // after the last reads (above, warp 0); ready for the next tile
+      __syncwarp();
+      if (lane < W) sec_key[lane] = kKeyNegInf;
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -885,6 +910,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   __shared__ int win_seg[2][W];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ unsigned long long pk_key[W];  // per window: the running first maximum (peak_key)
+  __shared__ unsigned sec_key[W];           // per window: key of the largest half-row maximum outside the peak row
 
   const int tid = threadIdx.x;
   const int q = tid >> 7, t = tid & 127;
@@ -998,13 +1024,17 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     for (int c = 0; c < 2; ++c) cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
   };
 
-  if (tid < W) pk_key[tid] = 0ull;
-  if (tid < W) window_setup(blockIdx.x, 0);
+  if (tid < W) {
+    pk_key[tid] = 0ull;
+    sec_key[tid] = kKeyNegInf;
+    window_setup(blockIdx.x, 0);
+  }
   __syncthreads();
   if (ASYNC) {
     stage_async(0);
     cp_async_commit();
   }
+  const bool ties = any_tie_output(seg_s, n_seg);
 
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
@@ -1218,6 +1248,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     const int w = q & 1, ch = q >> 1, i = t ^ HN;
     const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
+    float hbest;  // maximum of this thread's half row
     {
       float v[64];
 #pragma unroll
@@ -1231,6 +1262,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       first_max<64>(v, best, bk);
       int idx = i * N + 64 * ch + bk;
       if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
+      hbest = best;
       warp_first_max(best, idx);
       if (lane == 0) atomicMax(&pk_key[w], peak_key(best, idx));
       if (a.maps && g0 + w < total) {
@@ -1243,7 +1275,12 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     __syncthreads();
     {
       const int pidx = peak_index(pk_key[w]), pi_ = pidx / N, pj = pidx % N;
-      const bool mine = pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1;
+      if (ties) {  // the warp's largest half-row maximum outside the peak row (a warp's rows share a window)
+        const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(hbest));
+        if (lane == 0) atomicMax(&sec_key[w], k);
+      }
+      const bool mine = (ties && i == pi_) ||
+                        (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
       if (__any_sync(0xffffffffu, mine)) {
         float v[64];
 #pragma unroll
@@ -1259,6 +1296,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
     }
     __syncthreads();
+    bool tie = false;
+    if (ties && warp == 0)
+      tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return peak_index(pk_key[ww]); },
+                                 [&](int ww) { return nbrow + (ww * 3 + 1) * N; });
     if (tid < W && g0 + tid < total) {
       const int ww = tid;
       const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
@@ -1285,8 +1326,17 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
+      tie = tie && win_valid[sl][ww];
+      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
     }
-    if (tid < W) pk_key[tid] = 0ull;  // after its last read (above, same thread); ready for the next tile
+    if (warp == 0) {  // after the last reads (above, warp 0); ready for the next tile
+      __syncwarp();
+      if (lane < W) {
+        pk_key[lane] = 0ull;
+        sec_key[lane] = kKeyNegInf;
+      }
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -1322,7 +1372,9 @@ static int launch_tc64_t(const CorrArgs& a, cudaStream_t stream) {
   }
   int grid = sm_count();
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc64<ASYNC><<<grid, Tc64::NT, Tc64::SMEM, stream>>>(a, a.status);
+  CorrArgs b = a;
+  b.tie_tol = kTieTolF16;
+  k_corr_tc64<ASYNC><<<grid, Tc64::NT, Tc64::SMEM, stream>>>(b, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc64 launch");
 }
@@ -1368,13 +1420,15 @@ int bounded_wait_probe(uint32_t max_polls, int* status_dev, cudaStream_t stream)
 }
 
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
-  if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT) return false;
+  if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT && dft_mode != PIV_DFT_TENSOR_REFINED)
+    return false;
+  if (dft_mode == PIV_DFT_TENSOR_REFINED && !refine_supported(a)) return false;
   if (a.n_segs < 0 || a.n_segs > kMaxCorrSegs) return false;
   if (a.n_segs == 0 && (long long)a.n_pairs * a.m * a.n >= (1LL << 31)) return false;
   for (int k = 0; k < a.n_segs; ++k)
     if ((long long)a.segs[k].n_pairs * a.segs[k].m * a.segs[k].n >= (1LL << 31)) return false;
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
-         (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode == PIV_DFT_TENSOR));
+         (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode != PIV_DFT_TENSOR_SPLIT));
 }
 
 // Resident CTAs per SM the 16/32-px engine allows (TMEM, registers, shared
@@ -1455,7 +1509,9 @@ static int launch_tc_t(const CorrArgs& a, int per_sm, cudaStream_t stream) {
   const int k = per_sm <= 0 || per_sm > cfg->max_per_sm ? cfg->max_per_sm : per_sm;
   int grid = sm_count() * k;
   if (grid > n_tiles) grid = n_tiles;
-  k_corr_tc<SS, ASYNC, SPLIT><<<grid, L::NT, tc_smem_for(*cfg, k, L::SMEM), stream>>>(a, a.status);
+  CorrArgs b = a;
+  b.tie_tol = SPLIT ? kTieTolF32 : kTieTolF16;
+  k_corr_tc<SS, ASYNC, SPLIT><<<grid, L::NT, tc_smem_for(*cfg, k, L::SMEM), stream>>>(b, a.status);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_corr_tc launch");
 }
@@ -1498,9 +1554,51 @@ int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int varia
   return PIV_OK;
 }
 
+static int correlate_tensor_maps(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream);
+
+// The refined form: the fp16 engine's maps give the integer peaks, then the
+// subpixel stencil is recomputed in float32 (refine_peaks). Windows whose two
+// largest fp16 values are within the fp16 tie tolerance (their fp16 peak may
+// not be the float32 map's first maximum) are correlated again by the float32
+// FFT engine, when the caller gives a list buffer; the near-tie flags and
+// counts are then those of the FFT engine on those windows.
 int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream) {
   if (!correlate_tensor_supported(a, dft_mode))
     return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
+  if (dft_mode != PIV_DFT_TENSOR_REFINED) return correlate_tensor_maps(a, dft_mode, variant, stream);
+  const int n = a.n_segs > 0 ? a.n_segs : 1;
+  bool rerun = true;
+  for (int k = 0; k < n; ++k) {
+    const CorrSeg* q = a.n_segs > 0 ? &a.segs[k] : nullptr;
+    rerun = rerun && (q ? q->near_tie && q->tie_list && q->tie_list_count
+                        : a.near_tie && a.tie_list && a.tie_list_count);
+  }
+  CorrArgs m = a;  // with a re-run, the fp16 pass flags its near ties but counts none
+  if (rerun) {
+    m.tie_count = nullptr;
+    for (int k = 0; k < a.n_segs; ++k) m.segs[k].tie_count = nullptr;
+  }
+  int rc = correlate_tensor_maps(m, PIV_DFT_TENSOR, variant, stream);
+  if (rc == PIV_OK) rc = refine_peaks(m, stream);
+  for (int k = 0; rerun && rc == PIV_OK && k < n; ++k) {
+    CorrArgs f = a;  // one frame geometry at a time
+    f.n_segs = 0;
+    if (a.n_segs > 0) {
+      const CorrSeg& q = a.segs[k];
+      f.frame_a = q.frame_a; f.frame_b = q.frame_b; f.u = q.u; f.v = q.v; f.peak_i = q.peak_i; f.peak_j = q.peak_j;
+      f.win_mask = q.win_mask; f.near_tie = q.near_tie; f.tie_count = q.tie_count; f.tie_list = q.tie_list;
+      f.tie_list_count = q.tie_list_count; f.height = q.height; f.width = q.width; f.spacing = q.spacing;
+      f.m = q.m; f.n = q.n; f.x_offset = q.x_offset; f.y_offset = q.y_offset; f.n_pairs = q.n_pairs;
+    }
+    rc = compact_near_ties(f.near_tie, (long long)f.n_pairs * f.m * f.n, f.tie_list, f.tie_list_count, stream);
+    f.win_list = f.tie_list;
+    f.win_count = f.tie_list_count;
+    if (rc == PIV_OK) rc = correlate_fft(f, 0, stream);
+  }
+  return rc;
+}
+
+static int correlate_tensor_maps(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream) {
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   if (total == 0) return PIV_OK;
   if (!a.status) return set_error(PIV_E_ARG, "tensor correlation needs a device status word");

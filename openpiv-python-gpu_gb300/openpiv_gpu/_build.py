@@ -10,7 +10,7 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(ROOT, "csrc")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libpiv_gb300.so")
-SOURCES = ["piv_correlate.cu", "piv_correlate_f64.cu", "piv_tensor.cu", "piv_deform.cu", "piv_validate.cu", "piv_smoothn.cu", "piv_abi.cu"]
+SOURCES = ["piv_correlate.cu", "piv_correlate_f64.cu", "piv_tensor.cu", "piv_refine.cu", "piv_deform.cu", "piv_validate.cu", "piv_smoothn.cu", "piv_abi.cu"]
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -25,8 +25,9 @@ DTYPE = {"float32": 0, "float64": 1}
 SUBPIXEL = {"gaussian": 0, "parabolic": 1, "centroid": 2}
 S2N = {"peak2peak": 0, "peak2mean": 1, "peak2energy": 2}
 REPLACE = {"spring": 0, "median": 1, "mean": 2}
-DFT = {"fft": 0, "tensor": 1, "tensor_split": 2}
+DFT = {"fft": 0, "tensor": 1, "tensor_split": 2, "tensor_refined": 3}
 STAGES = ("predictor", "deform", "correlate", "validate", "replace", "smooth")
+SMOOTH_S_LOWER, SMOOTH_S_UPPER, SMOOTH_MAX_ITERS = 1, 2, 4
 
 HEADER = os.path.join(os.path.dirname(_build.ROOT), "include", "piv_gb300.h")
 
@@ -58,7 +59,7 @@ class PivGeometry(ctypes.Structure):
 class PivIterationView(ctypes.Structure):
     _fields_ = [("m", c_int), ("n", c_int)] + [(name, c_void_p) for name in (
         "u_corr", "v_corr", "up", "vp", "u_rep", "v_rep", "u_out", "v_out", "val0", "smooth_p", "peak_i",
-        "peak_j", "s2n")]
+        "peak_j", "s2n", "near_tie", "smooth_flags")]
 
 
 _SIGNATURES = {
@@ -70,6 +71,7 @@ _SIGNATURES = {
     "piv_plan_iteration_view": (c_int, [c_void_p, c_int, POINTER(PivIterationView)]),
     "piv_plan_destroy": (None, [c_void_p]),
     "piv_plan_status": (c_int, [c_void_p, POINTER(c_int), c_void_p]),
+    "piv_plan_near_ties": (c_int, [c_void_p, POINTER(c_int), c_int, c_void_p]),
     "piv_plan_autotune": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     "piv_plan_tuning": (c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(ctypes.c_float), c_int]),
     "piv_plan_variant_name": (c_int, [c_void_p, c_int, c_int, ctypes.c_char_p, c_size_t]),
@@ -111,6 +113,8 @@ _SIGNATURES = {
                             c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_int, c_int,
                             c_void_p]),
     "piv_smoothn": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p]),
+    "piv_smoothn_flags": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
+                                  c_void_p]),
     "piv_smoothn_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_void_p,
                                     c_void_p]),
 }

@@ -8,6 +8,7 @@ Device arrays are torch CUDA tensors where the reference returns CuPy arrays.
 """
 
 import ctypes
+import logging
 import math
 from math import ceil, log2, prod
 
@@ -15,6 +16,7 @@ import numpy as np
 
 from . import DTYPE_f, DTYPE_i
 from . import _lib
+from . import gpu_smoothn
 from .gpu_smoothn import SMOOTHING_PAR
 from .gpu_validation import (ALLOWED_REPLACING_METHODS, MAD_TOL, MEAN_TOL, MEDIAN_TOL, REPLACING_METHOD,
                              REPLACING_SIZE, RMS_TOL, S2N_TOL, VALIDATION_SIZE)
@@ -308,7 +310,11 @@ class PIVGPU:
     in one launch). ``dft`` selects the correlation engine: "fft" (plain
     float FFT), "tensor" (tcgen05 DFT on fp16 operands where available) or
     "tensor_split" (tcgen05 DFT on fp16 hi/lo operand pairs, three products
-    per stage, for 16 and 32 px passes; the FFT elsewhere). With
+    per stage, for 16 and 32 px passes; the FFT elsewhere) or
+    "tensor_refined" (the "tensor" maps give each window's integer peak, and
+    the five values of the subpixel fit are recomputed in float32 by direct
+    sums from the frames: the float32 FFT form's fit at nearly the fp16
+    form's cost). With
     ``autotune=True`` the first run of each plan times every launch variant
     of each pass's correlation engine on that run's frames (radix split and
     tile shape of the FFT engine, CTAs per SM and staging of the tensor
@@ -535,6 +541,7 @@ class PIVGPU:
         self._last = (plan, B, fa, fb)
         self.init_val_locations = val.bool()
         self.val_locations = out.bool()
+        self._log_smoothing(plan, B)
         if host_out:
             u, v = u.numpy(), v.numpy()
             self.init_val_locations = self.init_val_locations.numpy()
@@ -652,6 +659,33 @@ class PIVGPU:
             worst = worst or st.value
         return worst
 
+    def _log_smoothing(self, plan, n_pairs):
+        """SmoothnGPU's log messages for every smoothing of the run (the
+        PIV_SMOOTH_* flags of each pair); read only when INFO is enabled."""
+        if not gpu_smoothn._log.isEnabledFor(logging.INFO):
+            return
+        lib = _lib.lib()
+        for k in range(len(self._iterations) - 1):
+            view = _lib.PivIterationView()
+            _lib.check(lib.piv_plan_iteration_view(plan, k, ctypes.byref(view)))
+            flags = (ctypes.c_int * n_pairs)()
+            _lib.check(lib.piv_memcpy(ctypes.addressof(flags), view.smooth_flags, 4 * n_pairs, 0, None))
+            for f in flags:
+                gpu_smoothn.log_flags(int(f), (view.m, view.n))
+
+    def near_ties(self):
+        """Near-tie windows of the last run per iteration (summed over its
+        pairs): windows whose two largest correlation values are within the
+        engine's map accuracy, so that their integer peak may differ from the
+        reference's first argmax (see piv_plan_near_ties)."""
+        if self._last is None:
+            return []
+        plan = self._last[0]
+        n = len(self._iterations)
+        counts = (ctypes.c_int * n)()
+        _lib.check(_lib.lib().piv_plan_near_ties(plan, counts, n, _torch().cuda.current_stream().cuda_stream))
+        return [int(c) for c in counts]
+
     def plan_handle(self, frames, n_pairs):
         """The C plan used for frames like ``frames`` and up to n_pairs pairs."""
         _, pt, _ = self._frames(frames)
@@ -708,6 +742,8 @@ class PIVGPU:
                 d["vp"] = fetch(view.vp, np.float64).reshape(m, n)
             if view.s2n:
                 d["s2n"] = fetch(view.s2n, ft).reshape(m, n)
+            if view.near_tie:
+                d["near_tie"] = fetch(view.near_tie, np.uint8).reshape(m, n).astype(bool)
             out.append(d)
         return out
 

@@ -5,10 +5,15 @@ way PIVGPU uses it: order 2, non-robust, equal weights, two fields sharing
 one smoothing parameter chosen by GCV when ``s`` is None.
 """
 
+import logging
+from math import log10, sqrt
+
 import numpy as np
 
 from . import DTYPE_f
 from . import _lib
+
+_log = logging.getLogger(__name__)
 
 # Default settings (gpu_smoothn.py:16-35).
 SMOOTHING_WEIGHTS = None
@@ -27,6 +32,33 @@ def _torch():
     import torch
 
     return torch
+
+
+def p_bounds(shape):
+    """Bounds of p = log10(s) for order 2 (gpu_smoothn.py:320-338)."""
+    h_min = 1e-3
+    h_max = 1 - h_min
+    rank = sum(1 for d in shape if d != 1)
+    a_max, a_min = h_max ** (2 / rank), h_min ** (2 / rank)
+    p_min = log10((((1 + sqrt(1 + 8 * a_max)) / 4 / a_max) ** 2 - 1) / 16)
+    p_max = log10((((1 + sqrt(1 + 8 * a_min)) / 4 / a_min) ** 2 - 1) / 16)
+    return p_min, p_max
+
+
+def log_flags(flags, shape, max_iters=MAX_SMOOTHING_ITERS):
+    """Logs SmoothnGPU's messages (gpu_smoothn.py:218-222, 429-439) for the
+    PIV_SMOOTH_* flag word of one smoothing."""
+    if flags & (_lib.SMOOTH_S_LOWER | _lib.SMOOTH_S_UPPER):
+        p_min, p_max = p_bounds(shape)
+        if flags & _lib.SMOOTH_S_LOWER:
+            _log.info('The lower bound for s ({:.3f}) has been reached. '
+                      'Put s as an input variable if required.'.format(10 ** p_min))
+        else:
+            _log.info('The upper bound for s ({:.3f}) has been reached. '
+                      'Put s as an input variable if required.'.format(10 ** p_max))
+    if flags & _lib.SMOOTH_MAX_ITERS:
+        _log.info('The maximum number of iterations ({:d}) has been exceeded. '
+                  'Increase max_iters option or decrease tol_z value.'.format(max_iters))
 
 
 class SmoothnGPU:
@@ -60,10 +92,13 @@ class SmoothnGPU:
             self._mask = torch.as_tensor(np.asarray(self.mask)).to(device="cuda", dtype=torch.uint8).contiguous()
             mask_ptr = self._mask.data_ptr()
         p = torch.empty(1, dtype=torch.float64, device="cuda")
+        flags = torch.zeros(1, dtype=torch.int32, device="cuda")
         s = float("nan") if self.s is None else float(self.s)
-        _lib.check(_lib.lib().piv_smoothn(m, n, 1, u.data_ptr(), v.data_ptr(), mask_ptr, s, p.data_ptr(),
-                                          torch.cuda.current_stream().cuda_stream))
+        _lib.check(_lib.lib().piv_smoothn_flags(m, n, 1, u.data_ptr(), v.data_ptr(), mask_ptr, s, p.data_ptr(),
+                                                flags.data_ptr(), torch.cuda.current_stream().cuda_stream))
         self.p = float(p.item())
+        self.flags = int(flags.item())
+        log_flags(self.flags, self.f_shape)
         if self.s is None:
             self.s = float(10.0 ** self.p)
         return [u] if len(fields) == 1 else [u, v]

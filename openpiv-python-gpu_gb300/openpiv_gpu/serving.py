@@ -56,6 +56,8 @@ class _Slot:
         self.index = index
         self.stream = torch.cuda.Stream()
         self.event = torch.cuda.Event()
+        self.t_start = None  # timing events of the batch in flight (device interval)
+        self.t_end = None
         self.batch = []
         self.inputs = None
         self.outputs = None
@@ -109,6 +111,15 @@ class PIVServer:
         self.done = []
         self._next_id = 0
         self._lane_bytes = {}
+        # Evidence of continuous batching: the most batches in flight at
+        # once, the requests held back for lack of device memory, and each
+        # batch's device interval (ms after the server's reference event).
+        self.max_in_flight = 0
+        self.held_for_memory = 0
+        self.intervals = []
+        torch = _torch()
+        self._t0 = torch.cuda.Event(enable_timing=True)
+        self._t0.record()
 
     # -- requests ----------------------------------------------------------
     def submit(self, frame_a, frame_b, t_arrival=None):
@@ -149,6 +160,8 @@ class PIVServer:
             for s in lane.slots:
                 if s.busy() and s.event.query():
                     now = time.perf_counter()
+                    self.intervals.append((lane.shape, self._t0.elapsed_time(s.t_start),
+                                           self._t0.elapsed_time(s.t_end)))
                     u, v = s.outputs[0], s.outputs[1]
                     for k, req in enumerate(s.batch):
                         req.u = u[k].numpy().copy()
@@ -185,6 +198,7 @@ class PIVServer:
                     free, _ = torch.cuda.mem_get_info()
                 if free - need < self.hbm_reserve:
                     kept.append(req)
+                    self.held_for_memory += 1
                     continue
                 lane = _Lane(shape, self.settings, self.max_batch, self.slots_per_shape, self.dft)
                 self.lanes[shape] = lane
@@ -218,13 +232,32 @@ class PIVServer:
                     req.t_dispatch = now
                 plan = lane.proc._plan(_lib.PIXEL["u8"], self.max_batch, slot=s.index)
                 u, v, val, out = s.outputs
+                torch = _torch()
+                s.t_start = torch.cuda.Event(enable_timing=True)
+                s.t_end = torch.cuda.Event(enable_timing=True)
+                s.t_start.record(s.stream)
                 _lib.check(lib.piv_plan_run(plan, len(batch), ia.ctypes.data, ib.ctypes.data, 1, u.data_ptr(),
                                             v.data_ptr(), val.data_ptr(), out.data_ptr(), 2, s.stream.cuda_stream))
+                s.t_end.record(s.stream)
                 s.event.record(s.stream)
                 s.batch = batch
                 lane.last_used = now
+        in_flight = sum(s.busy() for lane in self.lanes.values() for s in lane.slots)
+        self.max_in_flight = max(self.max_in_flight, in_flight)
 
     # -- reporting ---------------------------------------------------------
+    def overlapping_batches(self):
+        """Pairs of completed batches whose device intervals (first to last
+        operation of the run on its slot's stream) overlap in time."""
+        iv = sorted(self.intervals, key=lambda t: t[1])
+        count = 0
+        for i in range(len(iv)):
+            for j in range(i + 1, len(iv)):
+                if iv[j][1] >= iv[i][2]:
+                    break
+                count += 1
+        return count
+
     def latency_stats(self):
         lat = np.array([r.latency for r in self.done if r.latency is not None])
         if lat.size == 0:

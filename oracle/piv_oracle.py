@@ -724,6 +724,8 @@ class OraclePIV:
             tr["i_peak"], tr["j_peak"] = i1, j1
             tr["peak_gap"] = peak_gap(corr, i1, j1)
             tr["fragile"] = fragile_windows(corr, i1, j1, it["subpixel_method"], fld.search_size)
+            # The Gaussian-stencil rule alone (no tie rule): a fit that reads a lag without overlap.
+            tr["stencil"] = fragile_windows(corr, i1, j1, it["subpixel_method"], fld.search_size, tie_tol=0.0)
             uc_flat = j_sp - N // 2
             vc_flat = i_sp - N // 2
             if sel is not None:

@@ -174,4 +174,6 @@ def run_reference(ref_root):
 
 
 if __name__ == "__main__":
-    run_reference(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the openpiv-python-gpu source tree>")
+    run_reference(sys.argv[1])

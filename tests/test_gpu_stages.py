@@ -416,11 +416,16 @@ TC_CASES = [(16, "gaussian", "u8", (256, 288), "tensor"), (32, "gaussian", "f32"
             (64, "gaussian", "u8", (256, 288), "tensor"), (64, "parabolic", "f32", (256, 288), "tensor"),
             (64, "gaussian", "u8", (256, 300), "tensor"),
             (16, "gaussian", "u8", (256, 288), "tensor_split"), (32, "gaussian", "f32", (256, 288), "tensor_split"),
-            (16, "parabolic", "f32", (256, 300), "tensor_split"), (32, "centroid", "u8", (256, 300), "tensor_split")]
+            (16, "parabolic", "f32", (256, 300), "tensor_split"), (32, "centroid", "u8", (256, 300), "tensor_split"),
+            (16, "gaussian", "u8", (256, 288), "tensor_refined"), (32, "gaussian", "f32", (256, 288), "tensor_refined"),
+            (64, "gaussian", "u8", (256, 288), "tensor_refined"), (64, "parabolic", "f32", (256, 300), "tensor_refined"),
+            (16, "centroid", "u16", (256, 300), "tensor_refined"), (32, "parabolic", "u8", (256, 300), "tensor_refined")]
 
 # Per engine: relative tie tolerance of the two largest map values, RMS and
 # maximum displacement error (px) against the float64 oracle.
-TC_TOL = {"tensor": (5e-3, 0.01, 0.1), "tensor_split": (1e-4, 1e-4, 2e-3)}
+TC_TOL = {"tensor": (5e-3, 0.01, 0.1), "tensor_split": (1e-4, 1e-4, 2e-3),
+          # refined: integer peaks from the fp16 maps (their tie resolution), fit values in float32
+          "tensor_refined": (5e-3, 1e-4, 2e-3)}
 
 
 @pytest.mark.parametrize("ss,subpix,pixel,shape,dft", TC_CASES)
@@ -430,7 +435,9 @@ def test_tensor_correlation_accuracy(env, ss, subpix, pixel, shape, dft):
     accuracy of the tensor form), integer peaks equal except where the two
     largest map values are within fp16 resolution (relative 5e-3) or the
     window is fragile. hi/lo split operands ("tensor_split"): RMS within
-    1e-4 px, ties within relative 1e-4."""
+    1e-4 px, ties within relative 1e-4. fp16 maps with the fit's five values
+    recomputed in float32 ("tensor_refined", without the near-tie re-run of
+    a plan): peaks as the fp16 form, RMS within 1e-4 px."""
     torch, _lib, lib = env
     tie_tol, rms_tol, max_tol = TC_TOL[dft]
     fa, fb = _frames(300 + ss, shape, n_pairs=3)
@@ -510,16 +517,22 @@ def test_tensor_pipeline_accuracy():
     mss = piv.pop("min_search_size")
     ut, vt = PIVGPU(a.shape, mss, **piv, dft="tensor")(a, b)
     us, vs = PIVGPU(a.shape, mss, **piv, dft="tensor_split")(a, b)
+    ur, vr = PIVGPU(a.shape, mss, **piv, dft="tensor_refined")(a, b)
     uf, vf = PIVGPU(a.shape, mss, **piv, dft="fft")(a, b)
     piv64 = dict(piv)
     piv64["dtype_f"] = "float64"
     u64, v64 = OraclePIV(a.shape, mss, **piv64)(a, b)
-    ut, vt, us, vs, uf, vf = (x.cpu().numpy() for x in (ut, vt, us, vs, uf, vf))
+    ut, vt, us, vs, uf, vf, ur, vr = (x.cpu().numpy() for x in (ut, vt, us, vs, uf, vf, ur, vr))
+    rms_r = float(np.sqrt(np.mean((ur - u64) ** 2 + (vr - v64) ** 2)))
+    max_rf = float(max(np.abs(ur - uf).max(), np.abs(vr - vf).max()))
     rms_t = float(np.sqrt(np.mean((ut - u64) ** 2 + (vt - v64) ** 2)))
     rms_s = float(np.sqrt(np.mean((us - u64) ** 2 + (vs - v64) ** 2)))
     rms_f = float(np.sqrt(np.mean((uf - u64) ** 2 + (vf - v64) ** 2)))
-    print(f"pipeline rms vs float64 oracle: tensor {rms_t:.2e} px, tensor_split {rms_s:.2e} px, fft {rms_f:.2e} px")
+    print(f"pipeline rms vs float64 oracle: tensor {rms_t:.2e} px, tensor_split {rms_s:.2e} px, "
+          f"tensor_refined {rms_r:.2e} px (max {max_rf:.1e} px from fft), fft {rms_f:.2e} px")
     assert rms_t < 0.01
+    assert rms_r < 1e-4
+    assert max_rf < 1e-3
     assert rms_s < 1e-4
     assert rms_f < 1e-4
 

@@ -28,7 +28,7 @@ def _case(name):
     return a, b, piv
 
 
-@pytest.mark.parametrize("dft,tol", [("tensor", 0.01), ("tensor_split", 1e-4)])
+@pytest.mark.parametrize("dft,tol", [("tensor", 0.01), ("tensor_split", 1e-4), ("tensor_refined", 1e-4)])
 @pytest.mark.parametrize("name", ["mask", "overlap75", "nonsquare", "u16", "uncentred"])
 def test_tensor_forms_match_oracle(name, dft, tol):
     from openpiv_gpu import _build
