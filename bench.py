@@ -47,6 +47,8 @@ DTYPE_OF_FORM = {
     "fft": "f32",
     "tensor": "f16 operands, f32 accumulation (tcgen05 kind::f16)",
     "tensor_split": "f16 hi/lo operand pairs, 3 products per stage, f32 accumulation (tcgen05 kind::f16)",
+    "tensor_refined": "f16 operands, f32 accumulation (tcgen05 kind::f16) for the integer peak; f32 direct sums "
+                      "for the subpixel fit; near ties on the f32 FFT",
 }
 
 
@@ -503,8 +505,7 @@ def run_gpu(args):
     peaks = measured_peaks()
     traffic_w = ncu_traffic()
     on_tensor = N == 2 * f.search_size and (
-        (args.dft in ("tensor", "tensor_refined") and f.search_size in (16, 32, 64)) or
-        (args.dft == "tensor_split" and f.search_size in (16, 32)))
+        args.dft in ("tensor", "tensor_refined", "tensor_split") and f.search_size in (16, 32, 64))
     if on_tensor:
         peak = peaks.get("bf16_tflops", 1900.0)
         unit, bound = "TFLOP/s", "tensor"
@@ -521,7 +522,8 @@ def run_gpu(args):
                 "peak_source": src, "launch_ms": corr[dom],
                 "algorithmic_flops_per_window": corr_flops(f.search_size, N)}
     if on_tensor:
-        roofline["executed_tflops"] = (n_win * tc_executed_flops(f.search_size, N, args.dft == "tensor_split")
+        roofline["executed_tflops"] = (n_win * tc_executed_flops(f.search_size, N, args.dft == "tensor_split"
+                                                                 and f.search_size in (16, 32))
                                        / (corr[dom] * 1e-3) / 1e12)
         roofline["executed_frac"] = roofline["executed_tflops"] / peak
     if roofline["traffic"]:

@@ -66,8 +66,10 @@ extern "C" {
                                     (float32 passes with search 16, 32 or 64 px and n_fft 2;
                                     other passes use the FFT) */
 #define PIV_DFT_TENSOR_SPLIT 2   /* as PIV_DFT_TENSOR with every operand split into FP16 hi and
-                                    lo parts and three products per stage (compensated);
-                                    search 16 or 32 px, other passes use the FFT */
+                                    lo parts and three products per stage (compensated) for
+                                    search 16 or 32 px; 64-px passes take the refined path of
+                                    PIV_DFT_TENSOR_REFINED (float32 accuracy as well); other
+                                    passes use the FFT */
 #define PIV_DFT_TENSOR_REFINED 3 /* PIV_DFT_TENSOR's maps give each window's integer peak, then
                                     the five values of the subpixel fit are recomputed in float32
                                     by direct sums from the frames (float32 FFT accuracy of the
@@ -274,6 +276,16 @@ int piv_plan_graph_launch(piv_plan* plan, void* stream);
 #define PIV_STAGES 6
 int piv_plan_set_timing(piv_plan* plan, int enable);
 int piv_plan_stage_times(piv_plan* plan, float* ms, int capacity, int* runs);
+
+/* Index checks of a checked build of this library (compiled with
+ * -DPIV_BOUNDS_CHECK; a test and debugging aid, no counterpart in the
+ * reference): *checked = 1 in such a build, where every shared-memory store,
+ * asynchronous copy, TMEM load, window read and result write of the
+ * tensor-core correlation and peak refinement kernels is checked against its
+ * buffer, and a failed check skips the access and is counted; *violations
+ * receives the count since the last call (then reset). The normal build
+ * gives *checked = 0, *violations = 0. Synchronises the device. */
+int piv_bounds_check(int* checked, int* violations);
 
 /* Copies the message of the last failure on this thread into buf. */
 int piv_last_error(char* buf, size_t len);

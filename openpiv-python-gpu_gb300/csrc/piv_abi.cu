@@ -154,6 +154,7 @@ struct piv_plan {
   int* status = nullptr;      // device status word of bounded device-side waits
   int* tie_counts = nullptr;  // [n_iters] near-tie windows of the last run per iteration
   int* tie_list = nullptr;    // refined tensor form: near-tie windows of a pass (max_pairs * max windows) + count
+  float* win_means = nullptr; // refined tensor form: window means of a pass (max_pairs * max windows * 2)
   uint8_t* outliers = nullptr;
   double* u_final = nullptr;
   double* v_final = nullptr;
@@ -422,7 +423,13 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
     rc = plan_alloc_t(p, &p->tie_counts, (size_t)cfg->n_iters);
     if (rc == PIV_OK) cudaMemset(p->tie_counts, 0, sizeof(int) * cfg->n_iters);
   }
-  if (rc == PIV_OK && cfg->dft_mode == PIV_DFT_TENSOR_REFINED) rc = plan_alloc_t(p, &p->tie_list, max_mn * P + 1);
+  bool refine_buffers = cfg->dft_mode == PIV_DFT_TENSOR_REFINED;
+  for (int k = 0; k < cfg->n_iters; ++k)  // the split form's 64-px passes take the refined path
+    refine_buffers = refine_buffers || (cfg->dft_mode == PIV_DFT_TENSOR_SPLIT && p->iters[k].search_size == 64);
+  if (rc == PIV_OK && refine_buffers) {
+    rc = plan_alloc_t(p, &p->tie_list, max_mn * P + 1);
+    if (rc == PIV_OK) rc = plan_alloc_t(p, &p->win_means, 2 * max_mn * P);
+  }
   if (rc == PIV_OK) {
     const size_t cnt = p->st.back().mn * P;
     rc = plan_alloc_t(p, &p->outliers, cnt);
@@ -633,6 +640,7 @@ static int run_pre(piv_plan* p, int k, RunCtx& x, cudaStream_t s, CorrArgs& c) {
   if (p->tie_list) {
     c.tie_list = p->tie_list + 1;
     c.tie_list_count = p->tie_list;
+    c.win_means = p->win_means;
   }
   st.corr = c;
   st.corr_valid = true;
@@ -826,7 +834,8 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
     cudaMemsetAsync(c.status, 0, sizeof(int), s);
     int* peaks = nullptr;  // the refined form reads the peaks back: device peaks when the caller wants none
     const size_t cnt = (size_t)n_pairs * g->m * g->n;
-    if (dft_mode == PIV_DFT_TENSOR_REFINED && (!c.peak_i || !c.peak_j)) {
+    if ((dft_mode == PIV_DFT_TENSOR_REFINED || (dft_mode == PIV_DFT_TENSOR_SPLIT && c.ss == 64)) &&
+        (!c.peak_i || !c.peak_j)) {
       PIV_TRY(cuda_ok(cudaMallocAsync((void**)&peaks, 2 * cnt * sizeof(int), s), "cudaMallocAsync"));
       if (!c.peak_i) c.peak_i = peaks;
       if (!c.peak_j) c.peak_j = peaks + cnt;
@@ -993,6 +1002,16 @@ int piv_smoothn_flags(int m, int n, int n_pairs, double* u, double* v, const uin
   return rc;
 }
 
+int piv_bounds_check(int* checked, int* violations) {
+  if (!checked || !violations) return set_error(PIV_E_ARG, "NULL argument");
+  PIV_TRY(cuda_ok(cudaDeviceSynchronize(), "device synchronize"));
+  const int a = bounds_violations_tensor(), b = bounds_violations_refine();
+  if (a == -2 || b == -2) return set_error(PIV_E_CUDA, "bounds counters could not be read");
+  *checked = a >= 0 ? 1 : 0;
+  *violations = (a > 0 ? a : 0) + (b > 0 ? b : 0);
+  return PIV_OK;
+}
+
 int piv_plan_near_ties(piv_plan* plan, int* counts, int capacity, void* stream) {
   if (!plan || !counts) return set_error(PIV_E_ARG, "NULL argument");
   const int n = (int)plan->st.size() < capacity ? (int)plan->st.size() : capacity;
@@ -1104,7 +1123,7 @@ int piv_plan_variant_name(const piv_plan* p, int iter, int variant, char* buf, s
     if (correlate_tensor_variant_describe(c, p->cfg.dft_mode, variant, &per_sm, &async) != PIV_OK)
       return set_error(PIV_E_ARG, "variant %d out of range", variant);
     snprintf(buf, len, "tensor%s ss=%d N=%d, %d CTA/SM, %s staging",
-             p->cfg.dft_mode == PIV_DFT_TENSOR_SPLIT ? " hi/lo"
+             p->cfg.dft_mode == PIV_DFT_TENSOR_SPLIT ? (c.ss == 64 ? " refined (split form)" : " hi/lo")
              : p->cfg.dft_mode == PIV_DFT_TENSOR_REFINED ? " refined" : "", c.ss, c.fft_size, per_sm,
              async ? "async" : "sync");
   } else {
@@ -1261,6 +1280,7 @@ static int batch_enqueue(piv_batch* b, const int* n_pairs, const void* const* fr
           q.tie_count = c.tie_count;
           q.tie_list = c.tie_list;
           q.tie_list_count = c.tie_list_count;
+          q.win_means = c.win_means;
           q.win0 = m.seg_windows;
           q.height = c.height;
           q.width = c.width;

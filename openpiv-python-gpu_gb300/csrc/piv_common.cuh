@@ -53,6 +53,44 @@ template <typename T> PIV_D T load_pixel(const void* base, int pixel_type, long 
 
 PIV_HD int div_up(int a, int b) { return (a + b - 1) / b; }
 
+// Index checks of the checked build (compiled with -DPIV_BOUNDS_CHECK, see
+// piv_bounds_check): a failed check counts a violation in this translation
+// unit's device counter and the guarded access is skipped. In the normal
+// build every check is the constant true and compiles away.
+#ifdef PIV_BOUNDS_CHECK
+static __device__ int g_bounds_violations;
+PIV_D bool in_bounds(bool ok) {
+  if (!ok) atomicAdd(&g_bounds_violations, 1);
+  return ok;
+}
+// Whether [p, p + bytes) lies in the CTA's dynamic shared memory.
+PIV_D bool in_dyn_smem(const void* p, unsigned bytes) {
+  extern __shared__ __align__(16) unsigned char piv_dyn_smem[];
+  unsigned size;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(size));
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p), b = (unsigned)__cvta_generic_to_shared(piv_dyn_smem);
+  return in_bounds(a >= b && a + bytes <= b + size);
+}
+#else
+PIV_D constexpr bool in_bounds(bool) { return true; }
+PIV_D constexpr bool in_dyn_smem(const void*, unsigned) { return true; }
+#endif
+// Host side: the device counter of the checked build's translation unit
+// (read and reset); -1 in the normal build.
+#define PIV_DEFINE_BOUNDS_COUNTER(fn)                                                     \
+  int fn() {                                                                              \
+    PIV_BOUNDS_COUNTER_BODY                                                               \
+  }
+#ifdef PIV_BOUNDS_CHECK
+#define PIV_BOUNDS_COUNTER_BODY                                                           \
+  int v = 0, z = 0;                                                                       \
+  if (cudaMemcpyFromSymbol(&v, g_bounds_violations, sizeof(int)) != cudaSuccess) return -2; \
+  if (cudaMemcpyToSymbol(g_bounds_violations, &z, sizeof(int)) != cudaSuccess) return -2;   \
+  return v;
+#else
+#define PIV_BOUNDS_COUNTER_BODY return -1;
+#endif
+
 // Number of SMs of the current device (cached per process).
 int sm_count();
 

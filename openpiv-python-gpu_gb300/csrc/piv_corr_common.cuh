@@ -52,6 +52,7 @@ PIV_D int load_segments(const CorrArgs& a, CorrSeg* seg_s) {
       q.tie_count = a.tie_count;
       q.tie_list = a.tie_list;
       q.tie_list_count = a.tie_list_count;
+      q.win_means = a.win_means;
       q.win0 = 0;
       q.height = a.height;
       q.width = a.width;

@@ -29,6 +29,7 @@ struct CorrSeg {
   int* tie_count;     // incremented once per near-tie window; may be NULL
   int* tie_list;      // refined form: scratch [n_pairs m n] for the near-tie windows' indices, and their count
   int* tie_list_count;
+  float* win_means;   // refined form: [n_pairs m n][2] window means of frames a and b (written by the engine)
   long long win0;
   int height, width, spacing, m, n, x_offset, y_offset, n_pairs;
 };
@@ -75,6 +76,9 @@ struct CorrArgs {
   // keep the fp16 maps' peaks and are counted as near ties).
   int* tie_list;
   int* tie_list_count;
+  // Refined tensor form: the fp16 engine writes each window's mean of frame a
+  // and of frame b here ([n_pairs m n][2]), and the refinement reads them.
+  float* win_means;
   // Multi-geometry launch (tensor engines): n_segs > 0 segments replace the
   // single geometry above (frames, sizes, outputs, mask; the window and search
   // sizes, pixel type and settings are shared), covering seg_windows windows
@@ -109,6 +113,11 @@ int correlate_tensor_variant_describe(const CorrArgs& a, int dft_mode, int varia
 // u, v are rewritten from them.
 bool refine_supported(const CorrArgs& a);
 int refine_peaks(const CorrArgs& a, cudaStream_t stream);
+// Violations counted by the checked build's index checks in the tensor-core
+// and refinement kernels since the last call (the counters are reset); -1 in
+// the normal build, -2 when the counter cannot be read.
+int bounds_violations_tensor();
+int bounds_violations_refine();
 // Indices of the windows with near_tie set into list (window order not
 // kept), their number into *count (reset first).
 int compact_near_ties(const uint8_t* near_tie, long long windows, int* list, int* count, cudaStream_t stream);

@@ -15,9 +15,10 @@
 // FFT form's up to float32 rounding of the sums, at a cost of 5 ss^2 products
 // per window.
 //
-// Work split: a group of G = ss^2 / 16 threads per window, each thread one
-// row y and 16 columns; the window means and the five sums are reduced over
-// the group (warp shuffles, and shared memory across warps for ss = 64).
+// Work split: a group of ss threads per window, each thread one column
+// sliding down the rows; the window means come from the engine (or are
+// summed here), the five sums are reduced over the group (warp shuffles, and
+// shared memory across warps for ss = 64).
 #include <math.h>
 
 #include "piv_common.cuh"
@@ -59,16 +60,19 @@ PIV_D void group_sum(float (&v)[K], float* part) {
 }
 
 template <typename P>
-PIV_D float px(const void* frame, long long idx) {
-  return (float)__ldg(reinterpret_cast<const P*>(frame) + idx);
+PIV_D float px(const P* p) {
+  return (float)__ldg(p);
 }
 
+// One window by a group of SS threads, thread x taking column x of frame a:
+// row y of a meets rows y + di - 1, y + di and y + di + 1 of b at column
+// x + dj and row y + di at columns x + dj -+ 1, in chunks of 8 rows whose
+// values are all loaded before they are used (the loads of a chunk are in
+// flight together; consecutive threads read consecutive columns).
 template <int SS, typename P>
-PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int t,
+PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int x,
                          float* part) {
-  constexpr int CH = SS / 16, G = SS * CH, HN = SS;
-  constexpr int N = 2 * SS;
-  const int y = t / CH, x0 = (t % CH) * 16;
+  constexpr int G = SS, HN = SS, N = 2 * SS;
   int sg = 0;
   long long loc = 0, base = 0;
   bool ok = active;
@@ -83,55 +87,75 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
     if (q->win_mask && q->win_mask[k]) ok = false;
     base = pair * (long long)q->height * q->width + (long long)(wr * q->spacing + q->y_offset) * q->width +
            wc * q->spacing + q->x_offset;
+    if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * q->width + SS <=
+                                           (long long)q->n_pairs * q->height * q->width))
+      ok = false;
   }
-  const void* fa = q->frame_a;
-  const void* fb = q->frame_b;
   const int width = q->width;
-  // The thread's 16 pixels of row y of both windows, and the window means.
-  float av[16], sums[2] = {0.f, 0.f};
-#pragma unroll
-  for (int x = 0; x < 16; ++x) {
-    av[x] = ok ? px<P>(fa, base + (long long)y * width + x0 + x) : 0.f;
-    sums[0] += av[x];
-    sums[1] += ok ? px<P>(fb, base + (long long)y * width + x0 + x) : 0.f;
+  const P* fa = reinterpret_cast<const P*>(q->frame_a) + (ok ? base : 0);
+  const P* fb = reinterpret_cast<const P*>(q->frame_b) + (ok ? base : 0);
+  // Window means: written by the engine, or summed here.
+  float ma = 0.f, mb = 0.f;
+  if (q->win_means) {
+    if (ok) {
+      ma = q->win_means[2 * loc];
+      mb = q->win_means[2 * loc + 1];
+    }
+  } else {
+    float sums[2] = {0.f, 0.f};
+    if (ok)
+      for (int y = 0; y < SS; ++y) {
+        sums[0] += px<P>(fa + y * width + x);
+        sums[1] += px<P>(fb + y * width + x);
+      }
+    group_sum<G, 2>(sums, part);
+    ma = sums[0] / (float)(SS * SS);
+    mb = sums[1] / (float)(SS * SS);
   }
-  group_sum<G, 2>(sums, part);
-  const float ma = sums[0] / (float)(SS * SS), mb = sums[1] / (float)(SS * SS);
   // The engine's integer peak: shifted (i, j), lag (i - N/2, j - N/2).
-  int pi_ = 0, pj = 0;
+  int pi_ = HN, pj = HN;
   if (ok) {
     pi_ = q->peak_i[loc];
     pj = q->peak_j[loc];
   }
   const int di = pi_ - HN, dj = pj - HN;
-  // b - mean b at window-relative (r, c); zero outside the window.
-  auto bv = [&](int r, int c) -> float {
-    return (ok && r >= 0 && r < SS && c >= 0 && c < SS) ? px<P>(fb, base + (long long)r * width + c) - mb : 0.f;
+  const int xb = x + dj;  // this thread's column of b
+  const bool cm = ok && (unsigned)(xb - 1) < (unsigned)SS, c0 = ok && (unsigned)xb < (unsigned)SS,
+             cp = ok && (unsigned)(xb + 1) < (unsigned)SS;
+  // b - mean b at (row r, column xb + dc) of the window; zero outside it.
+  auto bval = [&](int r, int dc, bool col_ok) -> float {
+    return (col_ok && (unsigned)r < (unsigned)SS) ? px<P>(fb + r * width + xb + dc) - mb : 0.f;
   };
-  // Sums of the stencil: 0 = (di, dj), 1 = (di - 1, dj), 2 = (di + 1, dj),
-  // 3 = (di, dj - 1), 4 = (di, dj + 1).
-  float c5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  {
-    float row[18];  // b row y + di, columns x0 + dj - 1 .. x0 + dj + 16
+  // Chunks of R rows: every value of a chunk is loaded before any is used,
+  // so that the chunk's loads are in flight together.
+  constexpr int R = 8;
+  float s_c = 0.f, s_d = 0.f, s_u = 0.f, s_l = 0.f, s_r = 0.f;
+#pragma unroll 1
+  for (int y0 = 0; y0 < SS; y0 += R) {
+    float av[R], bc[R + 2], bl[R], br[R];
 #pragma unroll
-    for (int x = 0; x < 18; ++x) row[x] = bv(y + di, x0 + dj - 1 + x);
+    for (int k = 0; k < R; ++k) av[k] = ok ? px<P>(fa + (y0 + k) * width + x) : 0.f;
 #pragma unroll
-    for (int x = 0; x < 16; ++x) {
-      const float ap = av[x] - ma;
-      c5[0] = fmaf(ap, row[x + 1], c5[0]);
-      c5[3] = fmaf(ap, row[x], c5[3]);
-      c5[4] = fmaf(ap, row[x + 2], c5[4]);
+    for (int k = 0; k < R + 2; ++k) bc[k] = bval(y0 + k + di - 1, 0, c0);  // rows y0 + di - 1 .. y0 + di + R
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      bl[k] = bval(y0 + k + di, -1, cm);
+      br[k] = bval(y0 + k + di, 1, cp);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const float ap = ok ? av[k] - ma : 0.f;
+      s_c = fmaf(ap, bc[k + 1], s_c);
+      s_d = fmaf(ap, bc[k], s_d);
+      s_u = fmaf(ap, bc[k + 2], s_u);
+      s_l = fmaf(ap, bl[k], s_l);
+      s_r = fmaf(ap, br[k], s_r);
     }
   }
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const int r = y + di + (s == 0 ? -1 : 1);
-#pragma unroll
-    for (int x = 0; x < 16; ++x) c5[1 + s] = fmaf(av[x] - ma, bv(r, x0 + dj + x), c5[1 + s]);
-  }
-  // Masked threads contribute zeros; keep the reductions uniform.
+  // Stencil sums: c (di, dj), cd (di - 1), cu (di + 1), cl (dj - 1), cr (dj + 1).
+  float c5[5] = {s_c, s_d, s_u, s_l, s_r};
   group_sum<G, 5>(c5, part);
-  if (!ok || t != 0) return;
+  if (!ok || x != 0 || !in_bounds(loc >= 0 && loc < (long long)q->n_pairs * q->m * q->n)) return;
   float isp = (float)pi_, jsp = (float)pj;
   if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1)
     subpixel_fit(a.subpixel, pi_, pj, c5[0], c5[1], c5[2], c5[3], c5[4], isp, jsp);
@@ -141,22 +165,22 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
 
 template <int SS, typename P>
 __global__ void __launch_bounds__(kRefineThreads) k_refine(CorrArgs a) {
-  constexpr int G = SS * SS / 16, WPB = kRefineThreads / G;
+  constexpr int G = SS, WPB = kRefineThreads / G;
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float part[kRefineThreads / 32 * 5];
   const int n_seg = load_segments(a, seg_s);
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
-  const int wl = threadIdx.x / G, t = threadIdx.x % G;
+  const int wl = threadIdx.x / G, x = threadIdx.x % G;
   // The loop bound is the same for every thread of the block (group sums).
   for (long long g0 = (long long)blockIdx.x * WPB; g0 < total; g0 += (long long)gridDim.x * WPB) {
     const long long g = g0 + wl;
-    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, t, part);
+    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, x, part);
   }
 }
 
 template <int SS>
 int launch_refine_ss(const CorrArgs& a, cudaStream_t stream) {
-  constexpr int G = SS * SS / 16, WPB = kRefineThreads / G;
+  constexpr int G = SS, WPB = kRefineThreads / G;
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   long long blocks = (total + WPB - 1) / WPB;
   const long long cap = (long long)sm_count() * 8;
@@ -179,6 +203,8 @@ __global__ void k_compact_ties(const uint8_t* __restrict__ flags, long long wind
 }
 
 }  // namespace
+
+PIV_DEFINE_BOUNDS_COUNTER(bounds_violations_refine)
 
 int compact_near_ties(const uint8_t* near_tie, long long windows, int* list, int* count, cudaStream_t stream) {
   cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), stream);

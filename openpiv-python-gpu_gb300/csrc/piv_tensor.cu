@@ -98,6 +98,15 @@ PIV_D void cp_async16(uint32_t smem_addr, const void* gmem) {
 }
 // 16 bytes from gmem, or (valid false) 16 zero bytes without a global read.
 PIV_D void cp_async16_zfill(uint32_t smem_addr, const void* gmem, bool valid) {
+#ifdef PIV_BOUNDS_CHECK
+  {
+    extern __shared__ __align__(16) unsigned char piv_dyn_smem[];
+    unsigned size;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(size));
+    const unsigned b = (unsigned)__cvta_generic_to_shared(piv_dyn_smem);
+    if (!in_bounds(smem_addr >= b && smem_addr + 16 <= b + size)) return;
+  }
+#endif
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr), "l"(gmem), "r"(valid ? 16 : 0)
                : "memory");
 }
@@ -205,6 +214,7 @@ PIV_D uint32_t off_mn(int m, int k, int R) {
 
 // Eight fp32 values -> eight fp16 in one 16-byte store.
 PIV_D void st8(unsigned char* base, uint32_t off, const float* v) {
+  if (!in_dyn_smem(base + off, 16)) return;
   uint4 q;
   __half2 h0 = __floats2half2_rn(v[0], v[1]), h1 = __floats2half2_rn(v[2], v[3]);
   __half2 h2 = __floats2half2_rn(v[4], v[5]), h3 = __floats2half2_rn(v[6], v[7]);
@@ -216,6 +226,7 @@ PIV_D void st8(unsigned char* base, uint32_t off, const float* v) {
 }
 
 PIV_D void sth(unsigned char* base, uint32_t off, float v) {
+  if (!in_dyn_smem(base + off, 2)) return;
   *reinterpret_cast<__half*>(base + off) = __float2half_rn(v);
 }
 
@@ -232,6 +243,7 @@ PIV_D void st8s(unsigned char* base, int lo, uint32_t off, const float* v) {
 
 template <bool SPLIT>
 PIV_D void sths(unsigned char* base, int lo, uint32_t off, float v) {
+  if (!in_dyn_smem(base + off, 2) || (SPLIT && !in_dyn_smem(base + lo + off, 2))) return;
   const __half h = __float2half_rn(v);
   *reinterpret_cast<__half*>(base + off) = h;
   if (SPLIT) *reinterpret_cast<__half*>(base + lo + off) = __float2half_rn(v - __half2float(h));
@@ -401,6 +413,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base_s;
+  // TMEM loads of the CTA's allocation (checked build: columns inside it).
+  auto tld = [&](uint32_t addr, float (&v)[16]) {
+    if (in_bounds(((addr - tmem) & 0xffffu) + 16 <= (uint32_t)L::TCOLS)) tc::tmem_ld16(addr, v);
+  };
   const uint32_t sbase = tc::smem_u32(sm);
   uint32_t phase = 0;
 
@@ -444,6 +460,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       if (q.win_mask) ok = q.win_mask[k] == 0;
       base = pair * (long long)q.height * q.width + (long long)(wr * q.spacing + q.y_offset) * q.width +
              wc * q.spacing + q.x_offset;
+      if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * q.width + SS <=
+                                             (long long)q.n_pairs * q.height * q.width))
+        ok = 0;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
@@ -527,7 +546,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         const float s = pow2i(e);
 #pragma unroll
         for (int x = 0; x < SS; ++x) r[x] *= s;
-        if (y == 0) sc_e[f][w] = e;
+        if (y == 0) {
+          sc_e[f][w] = e;
+          const CorrSeg& sq = seg_s[win_seg[sl][w]];
+          if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
+        }
 #pragma unroll
         for (int x = 0; x < SS; x += 8) st8s<SPLIT>(sm + L::OP + f * L::A1_BYTES, L::NOP, off_k(t, x, SS), r + x);
       }
@@ -570,12 +593,12 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
       };
       float b0[16], b1[16];
-      tc::tmem_ld16(col_src(0), b0);
+      tld(col_src(0), b0);
       tc::tmem_ld_wait();
       tc::reg_fence(b0);
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        if (k + 1 < K) tc::tmem_ld16(col_src(k + 1), (k & 1) ? b0 : b1);
+        if (k + 1 < K) tld(col_src(k + 1), (k & 1) ? b0 : b1);
         put(k, (k & 1) ? b1 : b0);
         if (k + 1 < K) {
           tc::tmem_ld_wait();
@@ -612,10 +635,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       for (int gi = 0; gi < HN / TPL; gi += 8) {
         const int g0 = half * (HN / TPL) + gi;
         float ea[16], eb[16], oa[16], ob[16];
-        tc::tmem_ld16(tmem + lane_sel + 0 * N + 2 * g0, ea);
-        tc::tmem_ld16(tmem + lane_sel + 1 * N + 2 * g0, eb);
-        tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
-        tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
+        tld(tmem + lane_sel + 0 * N + 2 * g0, ea);
+        tld(tmem + lane_sel + 1 * N + 2 * g0, eb);
+        tld(tmem + lane_sel + 2 * N + 2 * g0, oa);
+        tld(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
         tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
         float qr0[8], qi0[8], qr1[8], qi1[8];
@@ -659,7 +682,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         float v[N];
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + part * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tld(tmem + lane_sel + part * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
         if (SPLIT) {
@@ -710,6 +733,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       const long long gl = win_loc[sl][ww];
       float* uo = reinterpret_cast<float*>(sq.u);
       float* vo = reinterpret_cast<float*>(sq.v);
+      if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
       if (win_valid[sl][ww]) {
         uo[gl] = sub_rn(jsp, (float)HN);
         vo[gl] = sub_rn(isp, (float)HN);
@@ -734,7 +758,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         float v[N];
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tld(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
         float rowc[N];
@@ -760,8 +784,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
         if ((ties && i == pi_) || (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1)) {
           float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
+          if (in_dyn_smem(dst, N * 4))
 #pragma unroll
-          for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+            for (int c4 = 0; c4 < N / 4; ++c4)
+              dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
         }
         if (lane == 0) pk_idx[w][0] = idx;
       }
@@ -779,7 +805,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         float v[N];
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tld(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
         float rowc[N];
@@ -833,13 +859,15 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           float v[N];
 #pragma unroll
           for (int c0 = 0; c0 < N; c0 += 16)
-            tc::tmem_ld16(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+            tld(tmem + lane_sel + rt * N + c0, *reinterpret_cast<float(*)[16]>(v + c0));
           tc::tmem_ld_wait();
           tc::reg_fence(v);
           if (mine) {
             float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N);
+            if (in_dyn_smem(dst, N * 4))
 #pragma unroll
-            for (int c4 = 0; c4 < N / 4; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+              for (int c4 = 0; c4 < N / 4; ++c4)
+                dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
           }
         }
       }
@@ -963,6 +991,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base_s;
+  // TMEM loads of the CTA's allocation (checked build: columns inside it).
+  auto tld = [&](uint32_t addr, float (&v)[16]) {
+    if (in_bounds(((addr - tmem) & 0xffffu) + 16 <= (uint32_t)L::TCOLS)) tc::tmem_ld16(addr, v);
+  };
   const uint32_t sbase = tc::smem_u32(sm);
   uint32_t phase = 0;
 
@@ -1005,6 +1037,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       if (q.win_mask) ok = q.win_mask[k] == 0;
       base = pair * (long long)q.height * q.width + (long long)(wr * q.spacing + q.y_offset) * q.width +
              wc * q.spacing + q.x_offset;
+      if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * q.width + SS <=
+                                             (long long)q.n_pairs * q.height * q.width))
+        ok = 0;
     }
     win_valid[sl][tid] = ok;
     win_base[sl][tid] = base;
@@ -1086,7 +1121,11 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       const float s = pow2i(e);
 #pragma unroll
       for (int x = 0; x < 32; ++x) r[x] *= s;
-      if (h == 0 && y == 0) sc_e[f][w] = e;
+      if (h == 0 && y == 0) {
+        sc_e[f][w] = e;
+        const CorrSeg& sq = seg_s[win_seg[sl][w]];
+        if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
+      }
 #pragma unroll
       for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     }
@@ -1116,7 +1155,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       float v[64];
 #pragma unroll
       for (int c0 = 0; c0 < 64; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tld(tmem + lane_sel + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
       tc::reg_fence(v);
 #pragma unroll
@@ -1163,10 +1202,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       for (int gc = 0; gc < 16; gc += 8) {
         const int g0 = 16 * q + gc;
         float ea[16], eb[16], oa[16], ob[16];
-        tc::tmem_ld16(tmem + lane_sel + 0 * N + 2 * g0, ea);
-        tc::tmem_ld16(tmem + lane_sel + 1 * N + 2 * g0, eb);
-        tc::tmem_ld16(tmem + lane_sel + 2 * N + 2 * g0, oa);
-        tc::tmem_ld16(tmem + lane_sel + 3 * N + 2 * g0, ob);
+        tld(tmem + lane_sel + 0 * N + 2 * g0, ea);
+        tld(tmem + lane_sel + 1 * N + 2 * g0, eb);
+        tld(tmem + lane_sel + 2 * N + 2 * g0, oa);
+        tld(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
         tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
         float qr0[8], qi0[8], qr1[8], qi1[8];
@@ -1217,7 +1256,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       float v[64];
 #pragma unroll
       for (int c0 = 0; c0 < 64; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tld(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
       tc::reg_fence(v);
 #pragma unroll
@@ -1253,7 +1292,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       float v[64];
 #pragma unroll
       for (int c0 = 0; c0 < 64; c0 += 16)
-        tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tld(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
       tc::tmem_ld_wait();
       tc::reg_fence(v);
       if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
@@ -1285,13 +1324,15 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
         float v[64];
 #pragma unroll
         for (int c0 = 0; c0 < 64; c0 += 16)
-          tc::tmem_ld16(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tld(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
         if (mine) {
           float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N + s0);
+          if (in_dyn_smem(dst, 64 * 4))
 #pragma unroll
-          for (int c4 = 0; c4 < 16; ++c4) dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+            for (int c4 = 0; c4 < 16; ++c4)
+              dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
         }
       }
     }
@@ -1317,6 +1358,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       const long long gl = win_loc[sl][ww];
       float* uo = reinterpret_cast<float*>(sq.u);
       float* vo = reinterpret_cast<float*>(sq.v);
+      if (in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) {
       if (win_valid[sl][ww]) {
         uo[gl] = sub_rn(jsp, (float)HN);
         vo[gl] = sub_rn(isp, (float)HN);
@@ -1329,6 +1371,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       tie = tie && win_valid[sl][ww];
       if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
       if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
+      }
     }
     if (warp == 0) {  // after the last reads (above, warp 0); ready for the next tile
       __syncwarp();
@@ -1422,13 +1465,18 @@ int bounded_wait_probe(uint32_t max_polls, int* status_dev, cudaStream_t stream)
 bool correlate_tensor_supported(const CorrArgs& a, int dft_mode) {
   if (dft_mode != PIV_DFT_TENSOR && dft_mode != PIV_DFT_TENSOR_SPLIT && dft_mode != PIV_DFT_TENSOR_REFINED)
     return false;
-  if (dft_mode == PIV_DFT_TENSOR_REFINED && !refine_supported(a)) return false;
+  // The refined form, and the split form's 64-px passes (which take the
+  // refined path: the split engine's operands do not fit beside 64-px
+  // constants), need the refinement.
+  if ((dft_mode == PIV_DFT_TENSOR_REFINED || (dft_mode == PIV_DFT_TENSOR_SPLIT && a.ss == 64)) &&
+      !refine_supported(a))
+    return false;
   if (a.n_segs < 0 || a.n_segs > kMaxCorrSegs) return false;
   if (a.n_segs == 0 && (long long)a.n_pairs * a.m * a.n >= (1LL << 31)) return false;
   for (int k = 0; k < a.n_segs; ++k)
     if ((long long)a.segs[k].n_pairs * a.segs[k].m * a.segs[k].n >= (1LL << 31)) return false;
   return a.dtype == PIV_DTYPE_F32 && a.s2n == nullptr && a.ws == a.ss && a.fft_size == 2 * a.ss &&
-         (a.ss == 16 || a.ss == 32 || (a.ss == 64 && dft_mode != PIV_DFT_TENSOR_SPLIT));
+         (a.ss == 16 || a.ss == 32 || a.ss == 64);
 }
 
 // Resident CTAs per SM the 16/32-px engine allows (TMEM, registers, shared
@@ -1565,7 +1613,8 @@ static int correlate_tensor_maps(const CorrArgs& a, int dft_mode, int variant, c
 int correlate_tensor(const CorrArgs& a, int dft_mode, int variant, cudaStream_t stream) {
   if (!correlate_tensor_supported(a, dft_mode))
     return set_error(PIV_E_UNSUPPORTED, "tensor correlation: unsupported pass");
-  if (dft_mode != PIV_DFT_TENSOR_REFINED) return correlate_tensor_maps(a, dft_mode, variant, stream);
+  const bool refined = dft_mode == PIV_DFT_TENSOR_REFINED || (dft_mode == PIV_DFT_TENSOR_SPLIT && a.ss == 64);
+  if (!refined) return correlate_tensor_maps(a, dft_mode, variant, stream);
   const int n = a.n_segs > 0 ? a.n_segs : 1;
   bool rerun = true;
   for (int k = 0; k < n; ++k) {
@@ -1619,5 +1668,7 @@ static int correlate_tensor_maps(const CorrArgs& a, int dft_mode, int variant, c
   if (split) return async ? launch_tc_t<32, true, true>(a, per_sm, stream) : launch_tc_t<32, false, true>(a, per_sm, stream);
   return async ? launch_tc_t<32, true, false>(a, per_sm, stream) : launch_tc_t<32, false, false>(a, per_sm, stream);
 }
+
+PIV_DEFINE_BOUNDS_COUNTER(bounds_violations_tensor)
 
 }  // namespace piv

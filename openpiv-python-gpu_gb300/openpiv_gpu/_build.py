@@ -10,6 +10,9 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(ROOT, "csrc")
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libpiv_gb300.so")
+# The checked build (index checks in the tensor-core and refinement kernels,
+# see piv_bounds_check): a test and debugging aid, built only on request.
+CHECKED_PATH = os.path.join(LIB_DIR, "checked", "libpiv_gb300_checked.so")
 SOURCES = ["piv_correlate.cu", "piv_correlate_f64.cu", "piv_tensor.cu", "piv_refine.cu", "piv_deform.cu", "piv_validate.cu", "piv_smoothn.cu", "piv_abi.cu"]
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -22,10 +25,10 @@ def _nvcc():
     return "nvcc"
 
 
-def _stale():
-    if not os.path.exists(LIB_PATH):
+def _stale(path=LIB_PATH):
+    if not os.path.exists(path):
         return True
-    t = os.path.getmtime(LIB_PATH)
+    t = os.path.getmtime(path)
     for f in os.listdir(CSRC):
         if f.endswith((".cu", ".cuh", ".h")) and os.path.getmtime(os.path.join(CSRC, f)) > t:
             return True
@@ -37,18 +40,22 @@ def _stale():
     return False
 
 
-def build(force=False, verbose=False):
-    """Compiles every translation unit in parallel and links the shared library."""
-    if not force and not _stale():
-        return LIB_PATH
-    os.makedirs(LIB_DIR, exist_ok=True)
-    obj_dir = os.path.join(LIB_DIR, "obj")
+def build(force=False, verbose=False, checked=False):
+    """Compiles every translation unit in parallel and links the shared
+    library (``checked``: the checked build, with -DPIV_BOUNDS_CHECK)."""
+    path = CHECKED_PATH if checked else LIB_PATH
+    if not force and not _stale(path):
+        return path
+    out_dir = os.path.dirname(path)
+    os.makedirs(out_dir, exist_ok=True)
+    obj_dir = os.path.join(out_dir, "obj")
     os.makedirs(obj_dir, exist_ok=True)
     nvcc = _nvcc()
+    flags = NVCC_FLAGS + (["-DPIV_BOUNDS_CHECK"] if checked else [])
 
     def compile_one(src):
         obj = os.path.join(obj_dir, src.replace(".cu", ".o"))
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -58,13 +65,13 @@ def build(force=False, verbose=False):
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB_PATH + ".tmp"
+    tmp = path + ".tmp"
     cmd = [nvcc, "-shared", "--cudart", "static", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, path)
+    return path
 
 
 if __name__ == "__main__":

@@ -95,6 +95,7 @@ _SIGNATURES = {
     "piv_plan_set_timing": (c_int, [c_void_p, c_int]),
     "piv_plan_stage_times": (c_int, [c_void_p, POINTER(ctypes.c_float), c_int, POINTER(c_int)]),
     "piv_last_error": (c_int, [ctypes.c_char_p, c_size_t]),
+    "piv_bounds_check": (c_int, [POINTER(c_int), POINTER(c_int)]),
     "piv_memcpy": (c_int, [c_void_p, c_void_p, c_size_t, c_int, c_void_p]),
     "piv_field_geometry": (c_int, [c_int, c_int, c_int, c_int, c_double, c_int, POINTER(PivGeometry)]),
     "piv_correlate": (c_int, [POINTER(PivGeometry), c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int,
@@ -158,6 +159,20 @@ def load(path=None):
 
 def lib():
     return _lib if _lib is not None else load()
+
+
+def load_checked():
+    """Loads the checked build (``_build.build(checked=True)``) as a separate
+    library with the same signatures; it shares no state with ``lib()``."""
+    path = _build.CHECKED_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with openpiv_gpu._build.build(checked=True)")
+    checked = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(checked, name)
+        fn.restype = res
+        fn.argtypes = args
+    return checked
 
 
 def last_error():

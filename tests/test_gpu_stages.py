@@ -417,6 +417,7 @@ TC_CASES = [(16, "gaussian", "u8", (256, 288), "tensor"), (32, "gaussian", "f32"
             (64, "gaussian", "u8", (256, 300), "tensor"),
             (16, "gaussian", "u8", (256, 288), "tensor_split"), (32, "gaussian", "f32", (256, 288), "tensor_split"),
             (16, "parabolic", "f32", (256, 300), "tensor_split"), (32, "centroid", "u8", (256, 300), "tensor_split"),
+            (64, "gaussian", "u8", (256, 288), "tensor_split"),
             (16, "gaussian", "u8", (256, 288), "tensor_refined"), (32, "gaussian", "f32", (256, 288), "tensor_refined"),
             (64, "gaussian", "u8", (256, 288), "tensor_refined"), (64, "parabolic", "f32", (256, 300), "tensor_refined"),
             (16, "centroid", "u16", (256, 300), "tensor_refined"), (32, "parabolic", "u8", (256, 300), "tensor_refined")]
@@ -443,7 +444,7 @@ def test_tensor_correlation_accuracy(env, ss, subpix, pixel, shape, dft):
     fa, fb = _frames(300 + ss, shape, n_pairs=3)
     g = _geom(_lib, lib, shape, ss, 0.5)
     N = 2 * ss
-    dt = np.float32 if pixel == "f32" else np.uint8
+    dt = {"f32": np.float32, "u16": np.uint16}.get(pixel, np.uint8)
     da, db = torch.as_tensor(fa.astype(dt)).cuda(), torch.as_tensor(fb.astype(dt)).cuda()
     u = torch.empty((3, g.m, g.n), dtype=torch.float32, device="cuda")
     v = torch.empty_like(u)
