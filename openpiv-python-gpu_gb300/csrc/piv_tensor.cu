@@ -497,12 +497,29 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     cp_async_commit();
   }
   const bool ties = any_tie_output(seg_s, n_seg);
+  // Near-tie flag of window `lane` of the current tile (lanes < W of the
+  // calling warp; tile_near_ties's result) to the window's outputs.
+  int cur_sl = 0;
+  long long cur_g0 = 0;
+  auto write_near_ties = [&](bool tie) {
+    if (lane >= W || cur_g0 + lane >= total) return;
+    const CorrSeg& sq = seg_s[win_seg[cur_sl][lane]];
+    const long long gl = win_loc[cur_sl][lane];
+    tie = tie && win_valid[cur_sl][lane];
+    if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
+    if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+    if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
+  };
 
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
     const long long g0 = (long long)tile * W;
     if (ASYNC) cp_async_wait_all();
     __syncthreads();
+    // The previous tile's epilogue has finished with the near-tie keys.
+    if (tid < W) sec_key[tid] = kKeyNegInf;
+    cur_sl = sl;
+    cur_g0 = g0;
 
     // ---- Staging: thread (half, t = (w, y)) takes row y of window w of its frames.
     {
@@ -715,7 +732,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
     // Subpixel fit and outputs of window ww with flat peak index pidx (its
     // neighbour rows in nbrow).
-    auto finish = [&](int ww, int pidx, bool tie) {
+    auto finish = [&](int ww, int pidx) {
       const int pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
@@ -743,9 +760,6 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
-      tie = tie && win_valid[sl][ww];
-      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
-      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
     };
     auto peak_row = [&](int ww) { return nbrow + (ww * 3 + 1) * N; };
     if constexpr (N == 32 && TPL == 1) {
@@ -792,10 +806,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         if (lane == 0) pk_idx[w][0] = idx;
       }
       __syncthreads();
-      bool tie = false;
-      if (ties && warp == 0)
-        tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return pk_idx[ww][0]; }, peak_row);
-      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0], tie);
+      // The near-tie flags in warp 1 while warp 0 fits.
+      if (ties && warp == 1)
+        write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return pk_idx[ww][0]; },
+                                             peak_row));
+      if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
     } else {
       float rbest[2 / TPL];  // this thread's row maxima
 #pragma unroll
@@ -872,13 +887,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
       }
       __syncthreads();
-      bool tie = false;
-      if (ties && warp == 0) tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, window_peak, peak_row);
-      if (tid < W && g0 + tid < total) finish(tid, window_peak(tid), tie);
-    }
-    if (warp == 0) {  // after the last reads (above, warp 0); ready for the next tile
-      __syncwarp();
-      if (lane < W) sec_key[lane] = kKeyNegInf;
+      // The near-tie flags in warp 1 while warp 0 fits.
+      if (ties && warp == 1) write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, window_peak, peak_row));
+      if (tid < W && g0 + tid < total) finish(tid, window_peak(tid));
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -1070,12 +1081,32 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     cp_async_commit();
   }
   const bool ties = any_tie_output(seg_s, n_seg);
+  // Near-tie flag of window `lane` of the current tile (lanes < W of the
+  // calling warp; tile_near_ties's result) to the window's outputs.
+  int cur_sl = 0;
+  long long cur_g0 = 0;
+  auto write_near_ties = [&](bool tie) {
+    if (lane >= W || cur_g0 + lane >= total) return;
+    const CorrSeg& sq = seg_s[win_seg[cur_sl][lane]];
+    const long long gl = win_loc[cur_sl][lane];
+    tie = tie && win_valid[cur_sl][lane];
+    if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
+    if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+    if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
+  };
 
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
     const long long g0 = (long long)tile * W;
     if (ASYNC) cp_async_wait_all();
     __syncthreads();
+    // The previous tile's epilogue has finished with the peak and near-tie keys.
+    if (tid < W) {
+      pk_key[tid] = 0ull;
+      sec_key[tid] = kKeyNegInf;
+    }
+    cur_sl = sl;
+    cur_g0 = g0;
 
     // ---- Staging: thread (q, t) takes half h = q >> 1 of row y of window w of frame f = q & 1.
     {
@@ -1337,10 +1368,10 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
     }
     __syncthreads();
-    bool tie = false;
-    if (ties && warp == 0)
-      tie = tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return peak_index(pk_key[ww]); },
-                                 [&](int ww) { return nbrow + (ww * 3 + 1) * N; });
+    // The near-tie flags in warp 1 while warp 0 fits.
+    if (ties && warp == 1)
+      write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return peak_index(pk_key[ww]); },
+                                           [&](int ww) { return nbrow + (ww * 3 + 1) * N; }));
     if (tid < W && g0 + tid < total) {
       const int ww = tid;
       const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
@@ -1368,16 +1399,6 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
-      tie = tie && win_valid[sl][ww];
-      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
-      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
-      }
-    }
-    if (warp == 0) {  // after the last reads (above, warp 0); ready for the next tile
-      __syncwarp();
-      if (lane < W) {
-        pk_key[lane] = 0ull;
-        sec_key[lane] = kKeyNegInf;
       }
     }
     tc::fence_before_sync();
