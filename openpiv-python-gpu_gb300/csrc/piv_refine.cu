@@ -15,11 +15,10 @@
 // FFT form's up to float32 rounding of the sums, at a cost of 5 ss^2 products
 // per window.
 //
-// Work split: a group of ss threads per window (128-thread blocks: 8, 4 or
-// 2 windows at a time), each thread one column; the window's frame values,
-// less their means (from the engine, or summed here), are staged in shared
-// memory with the zero padding, and the five sums are reduced over the group
-// (warp shuffles, and shared memory across the two warps for ss = 64).
+// Work split: a group of ss threads per window, each thread one column
+// sliding down the rows; the window means come from the engine (or are
+// summed here), the five sums are reduced over the group (warp shuffles, and
+// shared memory across warps for ss = 64).
 #include <math.h>
 
 #include "piv_common.cuh"
@@ -30,7 +29,7 @@ namespace piv {
 
 namespace {
 
-constexpr int kRefineThreads = 128;
+constexpr int kRefineThreads = 256;
 
 // Sum of v over the thread's group of G consecutive threads (G a power of two
 // dividing the block); every thread of the block must call it. part: K floats
@@ -65,27 +64,15 @@ PIV_D float px(const P* p) {
   return (float)__ldg(p);
 }
 
-// Shared-memory tile of one window: A = a - mean a (SS x SS) and B = the b
-// rows di - 1 .. di + SS and columns dj - 1 .. dj + SS of the window, less
-// mean b, zero outside the window ((SS + 2) x (SS + 2)).
-template <int SS>
-struct RefineTile {
-  static constexpr int BS = SS + 2;
-  static constexpr int FLOATS = SS * SS + BS * BS;
-};
-
-// One window by a group of SS threads, thread x taking column x: the group
-// stages A and B into shared memory with coalesced row loads (the means
-// subtracted and the zero padding written once), then thread x runs down
-// column x of A: row y meets B rows y, y + 1, y + 2 at column x + 1 (lags
-// di - 1, di, di + 1) and B row y + 1 at columns x and x + 2 (lags dj - 1,
-// dj + 1). Every thread of the block calls it (block barriers).
+// One window by a group of SS threads, thread x taking column x of frame a:
+// row y of a meets rows y + di - 1, y + di and y + di + 1 of b at column
+// x + dj and row y + di at columns x + dj -+ 1, in chunks of 8 rows whose
+// values are all loaded before they are used (the loads of a chunk are in
+// flight together; consecutive threads read consecutive columns).
 template <int SS, typename P>
 PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int x,
-                         float* part, float* tile) {
-  constexpr int G = SS, HN = SS, N = 2 * SS, BS = RefineTile<SS>::BS;
-  float* A = tile;
-  float* B = tile + SS * SS;
+                         float* part) {
+  constexpr int G = SS, HN = SS, N = 2 * SS;
   int sg = 0;
   long long loc = 0, base = 0;
   bool ok = active;
@@ -132,34 +119,42 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
     pj = q->peak_j[loc];
   }
   const int di = pi_ - HN, dj = pj - HN;
-  // Stage A (rows of SS) and B (rows of BS: column x, and the two extra
-  // columns by threads 0 and 1), eight rows of loads in flight at a time.
-  __syncthreads();  // the previous window's reads of the tile are done
-#pragma unroll 8
-  for (int y = 0; y < SS; ++y) A[y * SS + x] = ok ? px<P>(fa + y * width + x) - ma : 0.f;
-  const int c0 = x + dj - 1, c1 = x + SS + dj - 1;  // b columns of tile columns x and x + SS
-  const bool v0 = ok && (unsigned)c0 < (unsigned)SS, v1 = ok && x < 2 && (unsigned)c1 < (unsigned)SS;
-#pragma unroll 8
-  for (int rho = 0; rho < BS; ++rho) {
-    const int r = rho + di - 1;
-    const bool vr = (unsigned)r < (unsigned)SS;
-    B[rho * BS + x] = (v0 && vr) ? px<P>(fb + r * width + c0) - mb : 0.f;
-    if (x < 2) B[rho * BS + SS + x] = (v1 && vr) ? px<P>(fb + r * width + c1) - mb : 0.f;
-  }
-  __syncthreads();
+  const int xb = x + dj;  // this thread's column of b
+  const bool cm = ok && (unsigned)(xb - 1) < (unsigned)SS, c0 = ok && (unsigned)xb < (unsigned)SS,
+             cp = ok && (unsigned)(xb + 1) < (unsigned)SS;
+  // Column pointers of b (this thread's column and its two neighbours).
+  const P* pb = fb + xb;
+  // Chunks of R rows: every value of a chunk is loaded before any is used,
+  // so that the chunk's loads are in flight together; a row's offset and
+  // validity serve its three loads.
+  constexpr int R = 8;
   float s_c = 0.f, s_d = 0.f, s_u = 0.f, s_l = 0.f, s_r = 0.f;
-  float bm = B[x + 1], b0 = B[BS + x + 1];
-#pragma unroll 8
-  for (int y = 0; y < SS; ++y) {
-    const float av = A[y * SS + x];
-    const float bp = B[(y + 2) * BS + x + 1];
-    s_d = fmaf(av, bm, s_d);
-    s_c = fmaf(av, b0, s_c);
-    s_u = fmaf(av, bp, s_u);
-    s_l = fmaf(av, B[(y + 1) * BS + x], s_l);
-    s_r = fmaf(av, B[(y + 1) * BS + x + 2], s_r);
-    bm = b0;
-    b0 = bp;
+#pragma unroll 1
+  for (int y0 = 0; y0 < SS; y0 += R) {
+    float av[R], bc[R + 2], bl[R], br[R];
+    const P* pa = fa + y0 * width + x;
+#pragma unroll
+    for (int k = 0; k < R; ++k) av[k] = ok ? px<P>(pa + k * width) : 0.f;
+#pragma unroll
+    for (int k = 0; k < R + 2; ++k) {  // rows y0 + di - 1 .. y0 + di + R
+      const int r = y0 + k + di - 1;
+      const bool vr = (unsigned)r < (unsigned)SS;
+      const P* row = pb + r * width;
+      bc[k] = (vr && c0) ? px<P>(row) - mb : 0.f;
+      if (k >= 1 && k <= R) {
+        bl[k - 1] = (vr && cm) ? px<P>(row - 1) - mb : 0.f;
+        br[k - 1] = (vr && cp) ? px<P>(row + 1) - mb : 0.f;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const float ap = ok ? av[k] - ma : 0.f;
+      s_c = fmaf(ap, bc[k + 1], s_c);
+      s_d = fmaf(ap, bc[k], s_d);
+      s_u = fmaf(ap, bc[k + 2], s_u);
+      s_l = fmaf(ap, bl[k], s_l);
+      s_r = fmaf(ap, br[k], s_r);
+    }
   }
   // Stencil sums: c (di, dj), cd (di - 1), cu (di + 1), cl (dj - 1), cr (dj + 1).
   float c5[5] = {s_c, s_d, s_u, s_l, s_r};
@@ -173,19 +168,17 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
 }
 
 template <int SS, typename P>
-__global__ void __launch_bounds__(kRefineThreads) k_refine(CorrArgs a) {
+__global__ void __launch_bounds__(kRefineThreads, 3) k_refine(CorrArgs a) {
   constexpr int G = SS, WPB = kRefineThreads / G;
-  extern __shared__ __align__(16) float refine_smem[];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float part[kRefineThreads / 32 * 5];
   const int n_seg = load_segments(a, seg_s);
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int wl = threadIdx.x / G, x = threadIdx.x % G;
-  float* tile = refine_smem + wl * RefineTile<SS>::FLOATS;
-  // The loop bound is the same for every thread of the block (barriers).
+  // The loop bound is the same for every thread of the block (group sums).
   for (long long g0 = (long long)blockIdx.x * WPB; g0 < total; g0 += (long long)gridDim.x * WPB) {
     const long long g = g0 + wl;
-    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, x, part, tile);
+    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, x, part);
   }
 }
 
@@ -193,29 +186,17 @@ template <int SS>
 int launch_refine_ss(const CorrArgs& a, cudaStream_t stream) {
   constexpr int G = SS, WPB = kRefineThreads / G;
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
-  const size_t smem = (size_t)WPB * RefineTile<SS>::FLOATS * sizeof(float);
   long long blocks = (total + WPB - 1) / WPB;
-  const long long cap = (long long)sm_count() * 16;
+  const long long cap = (long long)sm_count() * 8;
   if (blocks > cap) blocks = cap;
-  auto go = [&](auto kernel) -> int {
-    static thread_local int configured_dev = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (configured_dev != dev) {
-      const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return set_cuda_error(e, "cudaFuncSetAttribute(k_refine)");
-      configured_dev = dev;
-    }
-    kernel<<<(unsigned)blocks, kRefineThreads, smem, stream>>>(a);
-    const cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_refine launch");
-  };
   switch (a.pixel_type) {
-    case PIV_PIXEL_U8: return go(k_refine<SS, uint8_t>);
-    case PIV_PIXEL_U16: return go(k_refine<SS, uint16_t>);
-    case PIV_PIXEL_F32: return go(k_refine<SS, float>);
+    case PIV_PIXEL_U8: k_refine<SS, uint8_t><<<(unsigned)blocks, kRefineThreads, 0, stream>>>(a); break;
+    case PIV_PIXEL_U16: k_refine<SS, uint16_t><<<(unsigned)blocks, kRefineThreads, 0, stream>>>(a); break;
+    case PIV_PIXEL_F32: k_refine<SS, float><<<(unsigned)blocks, kRefineThreads, 0, stream>>>(a); break;
     default: return set_error(PIV_E_UNSUPPORTED, "peak refinement of float64 frames");
   }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PIV_OK : set_cuda_error(e, "k_refine launch");
 }
 
 __global__ void k_compact_ties(const uint8_t* __restrict__ flags, long long windows, int* __restrict__ list,

@@ -43,6 +43,14 @@ def libs():
     return torch, _lib, normal, checked
 
 
+def _chk(lib, rc):
+    """Raises with the message of the library that failed (each library keeps its own)."""
+    if rc != 0:
+        buf = ctypes.create_string_buffer(512)
+        lib.piv_last_error(buf, 512)
+        raise RuntimeError(f"[{rc}] {buf.value.decode(errors='replace')}")
+
+
 def _violations(_lib, checked):
     flag, count = ctypes.c_int(0), ctypes.c_int(0)
     _lib.check(checked.piv_bounds_check(ctypes.byref(flag), ctypes.byref(count)))
@@ -52,14 +60,14 @@ def _violations(_lib, checked):
 def _run_plan(torch, _lib, lib, proc, a, b):
     cfg, keep = proc._config(_lib.PIXEL["u8"], 1)
     plan = ctypes.c_void_p()
-    _lib.check(lib.piv_plan_create(ctypes.byref(cfg), ctypes.byref(plan)))
+    _chk(lib, lib.piv_plan_create(ctypes.byref(cfg), ctypes.byref(plan)))
     try:
         fa = torch.as_tensor(a[None]).cuda()
         fb = torch.as_tensor(b[None]).cuda()
         m, n = proc.piv_fields[-1].field_shape
         u = torch.empty((1, m, n), dtype=torch.float64, device="cuda")
         v = torch.empty_like(u)
-        _lib.check(lib.piv_plan_run(plan, 1, fa.data_ptr(), fb.data_ptr(), 0, u.data_ptr(), v.data_ptr(), None,
+        _chk(lib, lib.piv_plan_run(plan, 1, fa.data_ptr(), fb.data_ptr(), 0, u.data_ptr(), v.data_ptr(), None,
                                     None, 0, torch.cuda.current_stream().cuda_stream))
         torch.cuda.synchronize()
         return u.cpu().numpy(), v.cpu().numpy()
@@ -99,10 +107,10 @@ def test_correlation_in_bounds(libs, ss, pixel, shape, dft):
     out = []
     for lib in (checked, normal):
         g = _lib.PivGeometry()
-        _lib.check(lib.piv_field_geometry(shape[0], shape[1], ss, ss, 0.5, 1, ctypes.byref(g)))
+        _chk(lib, lib.piv_field_geometry(shape[0], shape[1], ss, ss, 0.5, 1, ctypes.byref(g)))
         u = torch.empty((3, g.m, g.n), dtype=torch.float32, device="cuda")
         v = torch.empty_like(u)
-        _lib.check(lib.piv_correlate(ctypes.byref(g), 3, da.data_ptr(), db.data_ptr(), _lib.PIXEL[pixel], 0, 2 * ss,
+        _chk(lib, lib.piv_correlate(ctypes.byref(g), 3, da.data_ptr(), db.data_ptr(), _lib.PIXEL[pixel], 0, 2 * ss,
                                      1, 0, None, u.data_ptr(), v.data_ptr(), None, None, 0, 2, None, _lib.DFT[dft],
                                      torch.cuda.current_stream().cuda_stream))
         torch.cuda.synchronize()
