@@ -15,8 +15,9 @@
 // FFT form's up to float32 rounding of the sums, at a cost of 5 ss^2 products
 // per window.
 //
-// Work split: a group of ss threads per window, each thread one column
-// sliding down the rows; the window means come from the engine (or are
+// Work split: a group of ss threads per window (8 for 16-px windows, two
+// columns each), each thread one column sliding down the rows in chunks of
+// 8 rows loaded together; the window means come from the engine (or are
 // summed here), the five sums are reduced over the group (warp shuffles, and
 // shared memory across warps for ss = 64).
 #include <math.h>
@@ -59,6 +60,15 @@ PIV_D void group_sum(float (&v)[K], float* part) {
   }
 }
 
+// Threads per window G and columns per thread CPT: 16-px windows take two
+// columns per thread (8 threads per window), which halves the per-window
+// overhead (window decode, means, group sums, fit lanes) of the small windows.
+template <int SS>
+struct RefineGroup {
+  static constexpr int CPT = SS == 16 ? 2 : 1;
+  static constexpr int G = SS / CPT;
+};
+
 template <typename P>
 PIV_D float px(const P* p) {
   return (float)__ldg(p);
@@ -72,7 +82,7 @@ PIV_D float px(const P* p) {
 template <int SS, typename P>
 PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int x,
                          float* part) {
-  constexpr int G = SS, HN = SS, N = 2 * SS;
+  constexpr int CPT = RefineGroup<SS>::CPT, G = RefineGroup<SS>::G, HN = SS, N = 2 * SS;
   int sg = 0;
   long long loc = 0, base = 0;
   bool ok = active;
@@ -104,10 +114,11 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
   } else {
     float sums[2] = {0.f, 0.f};
     if (ok)
-      for (int y = 0; y < SS; ++y) {
-        sums[0] += px<P>(fa + y * width + x);
-        sums[1] += px<P>(fb + y * width + x);
-      }
+      for (int c = 0; c < CPT; ++c)
+        for (int y = 0; y < SS; ++y) {
+          sums[0] += px<P>(fa + y * width + x + c * G);
+          sums[1] += px<P>(fb + y * width + x + c * G);
+        }
     group_sum<G, 2>(sums, part);
     ma = sums[0] / (float)(SS * SS);
     mb = sums[1] / (float)(SS * SS);
@@ -119,41 +130,43 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
     pj = q->peak_j[loc];
   }
   const int di = pi_ - HN, dj = pj - HN;
-  const int xb = x + dj;  // this thread's column of b
-  const bool cm = ok && (unsigned)(xb - 1) < (unsigned)SS, c0 = ok && (unsigned)xb < (unsigned)SS,
-             cp = ok && (unsigned)(xb + 1) < (unsigned)SS;
-  // Column pointers of b (this thread's column and its two neighbours).
-  const P* pb = fb + xb;
   // Chunks of R rows: every value of a chunk is loaded before any is used,
   // so that the chunk's loads are in flight together; a row's offset and
   // validity serve its three loads.
   constexpr int R = 8;
   float s_c = 0.f, s_d = 0.f, s_u = 0.f, s_l = 0.f, s_r = 0.f;
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) {
+    const int xa = x + c * G, xb = xa + dj;  // this thread's column of a, and of b
+    const bool cm = ok && (unsigned)(xb - 1) < (unsigned)SS, c0 = ok && (unsigned)xb < (unsigned)SS,
+               cp = ok && (unsigned)(xb + 1) < (unsigned)SS;
+    const P* pb = fb + xb;
 #pragma unroll 1
-  for (int y0 = 0; y0 < SS; y0 += R) {
-    float av[R], bc[R + 2], bl[R], br[R];
-    const P* pa = fa + y0 * width + x;
+    for (int y0 = 0; y0 < SS; y0 += R) {
+      float av[R], bc[R + 2], bl[R], br[R];
+      const P* pa = fa + y0 * width + xa;
 #pragma unroll
-    for (int k = 0; k < R; ++k) av[k] = ok ? px<P>(pa + k * width) : 0.f;
+      for (int k = 0; k < R; ++k) av[k] = ok ? px<P>(pa + k * width) : 0.f;
 #pragma unroll
-    for (int k = 0; k < R + 2; ++k) {  // rows y0 + di - 1 .. y0 + di + R
-      const int r = y0 + k + di - 1;
-      const bool vr = (unsigned)r < (unsigned)SS;
-      const P* row = pb + r * width;
-      bc[k] = (vr && c0) ? px<P>(row) - mb : 0.f;
-      if (k >= 1 && k <= R) {
-        bl[k - 1] = (vr && cm) ? px<P>(row - 1) - mb : 0.f;
-        br[k - 1] = (vr && cp) ? px<P>(row + 1) - mb : 0.f;
+      for (int k = 0; k < R + 2; ++k) {  // rows y0 + di - 1 .. y0 + di + R
+        const int r = y0 + k + di - 1;
+        const bool vr = (unsigned)r < (unsigned)SS;
+        const P* row = pb + r * width;
+        bc[k] = (vr && c0) ? px<P>(row) - mb : 0.f;
+        if (k >= 1 && k <= R) {
+          bl[k - 1] = (vr && cm) ? px<P>(row - 1) - mb : 0.f;
+          br[k - 1] = (vr && cp) ? px<P>(row + 1) - mb : 0.f;
+        }
       }
-    }
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const float ap = ok ? av[k] - ma : 0.f;
-      s_c = fmaf(ap, bc[k + 1], s_c);
-      s_d = fmaf(ap, bc[k], s_d);
-      s_u = fmaf(ap, bc[k + 2], s_u);
-      s_l = fmaf(ap, bl[k], s_l);
-      s_r = fmaf(ap, br[k], s_r);
+      for (int k = 0; k < R; ++k) {
+        const float ap = ok ? av[k] - ma : 0.f;
+        s_c = fmaf(ap, bc[k + 1], s_c);
+        s_d = fmaf(ap, bc[k], s_d);
+        s_u = fmaf(ap, bc[k + 2], s_u);
+        s_l = fmaf(ap, bl[k], s_l);
+        s_r = fmaf(ap, br[k], s_r);
+      }
     }
   }
   // Stencil sums: c (di, dj), cd (di - 1), cu (di + 1), cl (dj - 1), cr (dj + 1).
@@ -169,7 +182,7 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
 
 template <int SS, typename P>
 __global__ void __launch_bounds__(kRefineThreads, 3) k_refine(CorrArgs a) {
-  constexpr int G = SS, WPB = kRefineThreads / G;
+  constexpr int G = RefineGroup<SS>::G, WPB = kRefineThreads / G;
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float part[kRefineThreads / 32 * 5];
   const int n_seg = load_segments(a, seg_s);
@@ -184,7 +197,7 @@ __global__ void __launch_bounds__(kRefineThreads, 3) k_refine(CorrArgs a) {
 
 template <int SS>
 int launch_refine_ss(const CorrArgs& a, cudaStream_t stream) {
-  constexpr int G = SS, WPB = kRefineThreads / G;
+  constexpr int G = RefineGroup<SS>::G, WPB = kRefineThreads / G;
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   long long blocks = (total + WPB - 1) / WPB;
   const long long cap = (long long)sm_count() * 8;
