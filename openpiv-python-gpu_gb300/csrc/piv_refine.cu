@@ -15,11 +15,10 @@
 // FFT form's up to float32 rounding of the sums, at a cost of 5 ss^2 products
 // per window.
 //
-// Work split: a group of ss threads per window (8 for 16-px windows, two
-// columns each), each thread one column sliding down the rows in chunks of
-// 8 rows loaded together; the window means come from the engine (or are
-// summed here), the five sums are reduced over the group (warp shuffles, and
-// shared memory across warps for ss = 64).
+// Work split: a group of ss / 2 threads per window, each thread two columns
+// sliding down the rows in chunks of 8 rows loaded together; the window means
+// come from the engine (or are summed here), the five sums are reduced over
+// the group by warp shuffles.
 #include <math.h>
 
 #include "piv_common.cuh"
@@ -60,12 +59,13 @@ PIV_D void group_sum(float (&v)[K], float* part) {
   }
 }
 
-// Threads per window G and columns per thread CPT: 16-px windows take two
-// columns per thread (8 threads per window), which halves the per-window
-// overhead (window decode, means, group sums, fit lanes) of the small windows.
+// Threads per window G and columns per thread CPT: two columns per thread
+// (8, 16 or 32 threads per window) halve the per-window overhead (window
+// decode, means, group sums, fit lanes), and keep a 64-px window in one warp
+// (its group sum in shuffles alone).
 template <int SS>
 struct RefineGroup {
-  static constexpr int CPT = SS == 16 ? 2 : 1;
+  static constexpr int CPT = 2;
   static constexpr int G = SS / CPT;
 };
 
