@@ -114,7 +114,9 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
   } else {
     float sums[2] = {0.f, 0.f};
     if (ok)
+#pragma unroll 1
       for (int c = 0; c < CPT; ++c)
+#pragma unroll 4
         for (int y = 0; y < SS; ++y) {
           sums[0] += px<P>(fa + y * width + x + c * G);
           sums[1] += px<P>(fb + y * width + x + c * G);
