@@ -647,14 +647,30 @@ def run_serve(args):
     acc_jobs = {tuple(sh): oracle_pool.apply_async(_oracle_case, ((5, 100 + i, sh),)) for i, sh in enumerate(shapes)}
     first_pair = {tuple(sh): pool_by_shape[tuple(sh)][0] for sh in shapes}
     settings = dict(synthetic.CONFIGS[5]["piv"])
-    server = PIVServer(settings, max_batch=8, slots_per_shape=2, dft=args.dft)
-    for shape in shapes:  # lanes, plans and first launches outside the timed run
-        a, b = pool_by_shape[tuple(shape)][0]
-        server.submit(a, b)
-    server.drain()
-    server.done = []
-    done, secs = serve_arrivals(server, frames, arrivals)
-    stats = server.latency_stats()
+
+    def serve_form(form):
+        server = PIVServer(settings, max_batch=8, slots_per_shape=2, dft=form)
+        for shape in shapes:  # lanes, plans and first launches outside the timed run
+            a, b = pool_by_shape[tuple(shape)][0]
+            server.submit(a, b)
+        server.drain()
+        server.done = []
+        done, secs = serve_arrivals(server, frames, arrivals)
+        stats = server.latency_stats()
+        # The first pair of every size through the same server and lanes.
+        acc_reqs = {sh: server.submit(*first_pair[sh]) for sh in first_pair}
+        server.drain()
+        res = {"pairs_per_s": len(done) / secs, "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
+               "mean_ms": stats["mean_ms"], "requests": len(done), "form": form,
+               "device_status": max(l.proc.status() for l in server.lanes.values()),
+               "continuous_batching": {"max_batches_in_flight": server.max_in_flight,
+                                       "overlapping_batch_pairs": server.overlapping_batches(),
+                                       "held_for_memory": server.held_for_memory},
+               "uv": {sh: (r.u, r.v) for sh, r in acc_reqs.items()}}
+        server.close()
+        return res
+
+    served = {form: serve_form(form) for form in dict.fromkeys((args.dft, "tensor_refined"))}
     # Plain per-pair path: each pair alone, in arrival order, on the FP32 FFT form.
     kw = dict(settings)
     mss = kw.pop("min_search_size")
@@ -671,31 +687,31 @@ def run_serve(args):
         lat.append(time.perf_counter() - t0 - t_arr)
     plain_secs = time.perf_counter() - t0
     lat = np.array(lat)
-    # The first pair of every size through the same server and lanes.
-    acc_reqs = {sh: server.submit(*first_pair[sh]) for sh in first_pair}
-    server.drain()
-    accuracy = {}
     for sh, job in acc_jobs.items():
         u64, v64, secs_o = job.get()
-        accuracy[f"{sh[1]}x{sh[0]}"] = _rms(acc_reqs[sh].u, acc_reqs[sh].v, u64, v64)
+        for res in served.values():
+            res.setdefault("rms_px_vs_fp64_oracle", {})[f"{sh[1]}x{sh[0]}"] = _rms(*res["uv"][sh], u64, v64)
+    for res in served.values():
+        res.pop("uv")
+    chosen = served[args.dft]
     oracle_pool.close()
     line = {
         "metric": "serving pairs/s with p50/p99 latency (Poisson arrivals, 5 frame sizes, 64->32->16 px three-pass PIV)",
-        "value": len(done) / secs, "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True,
-        "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"], "mean_ms": stats["mean_ms"], "requests": len(done),
-        "arrival_rate": args.rate, "form": args.dft, "max_batch": 8, "slots_per_shape": 2,
+        "value": chosen["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True,
+        "p50_ms": chosen["p50_ms"], "p99_ms": chosen["p99_ms"], "mean_ms": chosen["mean_ms"],
+        "requests": chosen["requests"], "arrival_rate": args.rate, "form": args.dft, "max_batch": 8,
+        "slots_per_shape": 2,
+        "forms": {form: {k: v for k, v in res.items() if k != "continuous_batching"} for form, res in served.items()},
         "plain_per_pair": {"pairs_per_s": args.requests / plain_secs, "p50_ms": float(np.percentile(lat, 50) * 1e3),
                            "p99_ms": float(np.percentile(lat, 99) * 1e3), "form": "fft"},
         "config": {"workload": "Poisson stream, sizes uniform over " + ", ".join(f"{w}x{h}" for h, w in shapes) +
                    "; particle density U[0.01, 0.04], vortex or shear up to 12 px; 64->32->16 px @50%, median "
                    "validation, 2 revalidated spring replacements, smoothn GCV; float32",
                    "data": "synthetic (2 seeded pairs per size, reused)"},
-        "device_status": max(l.proc.status() for l in server.lanes.values()),
-        "accuracy": {"rms_px_vs_fp64_oracle": accuracy,
+        "device_status": chosen["device_status"],
+        "accuracy": {"rms_px_vs_fp64_oracle": chosen["rms_px_vs_fp64_oracle"],
                      "case": "the first pair of every size, served by the same loop, against the float64 oracle"},
-        "continuous_batching": {"max_batches_in_flight": server.max_in_flight,
-                                "overlapping_batch_pairs": server.overlapping_batches(),
-                                "held_for_memory": server.held_for_memory},
+        "continuous_batching": chosen["continuous_batching"],
     }
     print(json.dumps(line), flush=True)
 
@@ -729,7 +745,7 @@ def run_mixed(args):
     settings = dict(synthetic.CONFIGS[4]["piv"])
     shapes = [a.shape for a, _ in pairs]
     out = {}
-    for form in (args.dft, "fft"):
+    for form in dict.fromkeys((args.dft, "tensor_refined", "fft")):
         batch = PIVMixedBatch(shapes, settings, dft=form)
         batch.load(pairs)
         batch.capture()
@@ -764,6 +780,8 @@ def run_mixed(args):
         "value": out[args.dft]["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "form": args.dft, "chosen": out[args.dft],
         "plain_form": out["fft"], "chosen_over_plain": out[args.dft]["pairs_per_s"] / out["fft"]["pairs_per_s"],
+        "refined_form": out["tensor_refined"],
+        "refined_over_plain": out["tensor_refined"]["pairs_per_s"] / out["fft"]["pairs_per_s"],
         "config": {"workload": "16 pairs each of 512x512, 1280x800, 1024x768, 2048x2048; density U[0.01, 0.05], "
                                "vortex or shear up to 10 px; 64->32->16 px @50%, median validation, 2 revalidated "
                                "spring replacements, smoothn GCV; float32",
@@ -777,8 +795,9 @@ def run_mixed(args):
 def run_precision(args):
     """Precision form (the two-pass 2048x2048 workload at 75% overlap): 16
     resident pairs per step, each form captured as a CUDA graph and replayed
-    K times (CUDA events): hi/lo split tensor form (chosen), fp16 tensor form
-    and plain FP32 FFT form, every one autotuned first. Accuracy: RMS against
+    K times (CUDA events): the hi/lo split and refined tensor forms (the
+    faster one is the chosen precision form), the fp16 tensor form and the
+    plain FP32 FFT form, every one autotuned first. Accuracy: RMS against
     the float64 oracle on 512x512 pairs of the same particle model, flow and
     settings (the oracle takes minutes on a full 2048x2048 pair)."""
     import ctypes as ct
@@ -812,7 +831,7 @@ def run_precision(args):
     shape = tuple(fa.shape[1:])
     stream = torch.cuda.Stream()
     out = {}
-    for form in ("tensor_split", "tensor", "fft"):
+    for form in ("tensor_split", "tensor_refined", "tensor", "fft"):
         proc = PIVGPU(shape, mss, **kw, dft=form, autotune=True)
         with torch.cuda.stream(stream):
             for _ in range(max(1, args.warmup)):
@@ -858,12 +877,16 @@ def run_precision(args):
     for form in out:
         gu, gv = out[form].pop("full_uv")
         out[form]["rms_px_vs_fp64_oracle_full_pair"] = _rms(gu, gv, u64, v64)
-    chosen = out["tensor_split"]
+    # The chosen precision form: the faster of the two float32-accurate tensor forms.
+    chosen_form = max(("tensor_split", "tensor_refined"), key=lambda f: out[f]["pairs_per_s"])
+    chosen = out[chosen_form]
     line = {
         "metric": "frame pairs/s (2048x2048, 32->16 px two-pass PIV at 75% overlap, precision form) on 1 GB300",
         "value": chosen["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "form": "tensor_split", "dtype": DTYPE_OF_FORM["tensor_split"],
-        "data": "synthetic (seeded particle images)", "chosen": chosen, "fp16_tensor_form": out["tensor"],
+        "ms_per_step": chosen["ms_per_step"], "higher_is_better": True, "form": chosen_form,
+        "dtype": DTYPE_OF_FORM[chosen_form], "data": "synthetic (seeded particle images)", "chosen": chosen,
+        "forms": {f: out[f] for f in ("tensor_split", "tensor_refined") if f != chosen_form},
+        "fp16_tensor_form": out["tensor"],
         "plain_form": out["fft"], "chosen_over_plain": chosen["pairs_per_s"] / out["fft"]["pairs_per_s"],
         "config": {"workload": "16 resident 2048x2048 uint8 pairs, 0.05 ppp, 8-mode streamfunction flow up to 8 px; "
                                "32 -> 16 px at 75%, n_fft 2, median validation, 2 revalidated spring replacements; "

@@ -15,10 +15,10 @@
 // FFT form's up to float32 rounding of the sums, at a cost of 5 ss^2 products
 // per window.
 //
-// Work split: a group of ss / 2 threads per window, each thread two columns
-// sliding down the rows in chunks of 8 rows loaded together; the window means
-// come from the engine (or are summed here), the five sums are reduced over
-// the group by warp shuffles.
+// Work split: a group of ss / 4 threads per window, each thread four adjacent
+// columns; frame b is walked once, row by row, against the three latest rows
+// of frame a (refine_window); the window means come from the engine (or are
+// summed here), the five sums are reduced over the group by warp shuffles.
 #include <math.h>
 
 #include "piv_common.cuh"
@@ -31,58 +31,60 @@ namespace {
 
 constexpr int kRefineThreads = 256;
 
-// Sum of v over the thread's group of G consecutive threads (G a power of two
-// dividing the block); every thread of the block must call it. part: K floats
-// per warp of the block.
+// Sum of v over the thread's group of G consecutive lanes (G a power of two,
+// at most 32); every lane of the warp must call it.
 template <int G, int K>
-PIV_D void group_sum(float (&v)[K], float* part) {
-  constexpr int L = G < 32 ? G : 32;
+PIV_D void group_sum(float (&v)[K]) {
+  static_assert(G <= 32 && (G & (G - 1)) == 0, "a group is a power-of-two part of a warp");
 #pragma unroll
   for (int k = 0; k < K; ++k)
 #pragma unroll
-    for (int o = L / 2; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  if constexpr (G > 32) {
-    const int warp = threadIdx.x >> 5;
-    __syncthreads();  // the previous group_sum's reads of part[] are done
-    if ((threadIdx.x & 31) == 0)
-#pragma unroll
-      for (int k = 0; k < K; ++k) part[warp * K + k] = v[k];
-    __syncthreads();
-    const int w0 = (threadIdx.x / G) * (G / 32);
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      float s = 0.f;
-#pragma unroll
-      for (int j = 0; j < G / 32; ++j) s += part[(w0 + j) * K + k];
-      v[k] = s;
-    }
-  }
+    for (int o = G / 2; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
-// Threads per window G and columns per thread CPT: two columns per thread
-// (8, 16 or 32 threads per window) halve the per-window overhead (window
-// decode, means, group sums, fit lanes), and keep a 64-px window in one warp
-// (its group sum in shuffles alone).
-template <int SS>
-struct RefineGroup {
-  static constexpr int CPT = 2;
-  static constexpr int G = SS / CPT;
-};
+// Four adjacent columns per thread: G = ss / 4 threads per window (4, 8 or
+// 16), so a window always lies in one warp.
+constexpr int kCols = 4;
 
 template <typename P>
 PIV_D float px(const P* p) {
   return (float)__ldg(p);
 }
 
-// One window by a group of SS threads, thread x taking column x of frame a:
-// row y of a meets rows y + di - 1, y + di and y + di + 1 of b at column
-// x + dj and row y + di at columns x + dj -+ 1, in chunks of 8 rows whose
-// values are all loaded before they are used (the loads of a chunk are in
-// flight together; consecutive threads read consecutive columns).
+// Four adjacent pixels from p; vec: p is aligned for one vector load.
+template <typename P>
+PIV_D void load4(const P* p, bool vec, float (&v)[4]) {
+  if (vec) {
+    if constexpr (sizeof(P) == 4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+      v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+    } else if constexpr (sizeof(P) == 2) {
+      const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+      v[0] = (float)(q.x & 0xffffu), v[1] = (float)(q.x >> 16), v[2] = (float)(q.y & 0xffffu), v[3] = (float)(q.y >> 16);
+    } else {
+      const unsigned q = __ldg(reinterpret_cast<const unsigned*>(p));
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = (float)((q >> (8 * k)) & 0xffu);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = px<P>(p + k);
+  }
+}
+
+// One window by a group of G threads, thread x taking columns 4x .. 4x + 3 of
+// frame a. Frame b is walked row by row: b row r = t + di - 1 (step t) meets
+// a row t at lag di - 1, a row t - 1 at lags di and dj -+ 1, and a row t - 2
+// at lag di + 1, so each row of either frame is loaded once and the three
+// latest rows of a slide along in registers. A thread's six columns of b
+// (4x + dj - 1 .. 4x + dj + 4) give the centre column of its four a columns
+// and both side columns; columns outside b's window are read at a clamped
+// column and weighted by zero (and no mean is removed there), rows outside it
+// are left out by the step range. Steps run in chunks of R whose loads are
+// issued together.
 template <int SS, typename P>
-PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int x,
-                         float* part) {
-  constexpr int CPT = RefineGroup<SS>::CPT, G = RefineGroup<SS>::G, HN = SS, N = 2 * SS;
+PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, long long g, bool active, int x) {
+  constexpr int G = SS / kCols, HN = SS, N = 2 * SS, R = sizeof(P) == 1 ? 3 : 4;
   int sg = 0;
   long long loc = 0, base = 0;
   bool ok = active;
@@ -101,9 +103,14 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
                                            (long long)q->n_pairs * q->height * q->width))
       ok = false;
   }
+  // Inactive groups walk the first window of the first segment (in bounds)
+  // and write nothing.
   const int width = q->width;
+  const int xa0 = kCols * x;
   const P* fa = reinterpret_cast<const P*>(q->frame_a) + (ok ? base : 0);
   const P* fb = reinterpret_cast<const P*>(q->frame_b) + (ok ? base : 0);
+  constexpr unsigned VB = kCols * sizeof(P);
+  const bool vec = ((reinterpret_cast<uintptr_t>(fa + xa0) | (uintptr_t)width * sizeof(P)) & (VB - 1)) == 0;
   // Window means: written by the engine, or summed here.
   float ma = 0.f, mb = 0.f;
   if (q->win_means) {
@@ -112,16 +119,17 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
       mb = q->win_means[2 * loc + 1];
     }
   } else {
+    const bool vb = ((reinterpret_cast<uintptr_t>(fb + xa0)) & (VB - 1)) == 0 && vec;
     float sums[2] = {0.f, 0.f};
-    if (ok)
-#pragma unroll 1
-      for (int c = 0; c < CPT; ++c)
 #pragma unroll 4
-        for (int y = 0; y < SS; ++y) {
-          sums[0] += px<P>(fa + y * width + x + c * G);
-          sums[1] += px<P>(fb + y * width + x + c * G);
-        }
-    group_sum<G, 2>(sums, part);
+    for (int y = 0; y < SS; ++y) {
+      float va[4], vb4[4];
+      load4<P>(fa + y * width + xa0, vec, va);
+      load4<P>(fb + y * width + xa0, vb, vb4);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sums[0] += va[k], sums[1] += vb4[k];
+    }
+    group_sum<G, 2>(sums);
     ma = sums[0] / (float)(SS * SS);
     mb = sums[1] / (float)(SS * SS);
   }
@@ -132,48 +140,71 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
     pj = q->peak_j[loc];
   }
   const int di = pi_ - HN, dj = pj - HN;
-  // Chunks of R rows: every value of a chunk is loaded before any is used,
-  // so that the chunk's loads are in flight together; a row's offset and
-  // validity serve its three loads.
-  constexpr int R = 8;
+  // The six b columns: clamped read position, weight and removed mean.
+  int cb[6];
+  float mk[6], nmb[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const int c = xa0 + dj - 1 + j;
+    const bool v = (unsigned)c < (unsigned)SS;
+    cb[j] = min(max(c, 0), SS - 1);
+    mk[j] = v ? 1.f : 0.f;
+    nmb[j] = v ? -mb : 0.f;
+  }
+  auto load_b = [&](const P* row, float (&bv)[6]) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) bv[j] = fmaf(px<P>(row + cb[j]), mk[j], nmb[j]);
+  };
+  auto load_a = [&](const P* row, float (&av)[4]) {
+    load4<P>(row + xa0, vec, av);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) av[k] -= ma;
+  };
   float s_c = 0.f, s_d = 0.f, s_u = 0.f, s_l = 0.f, s_r = 0.f;
+  auto step = [&](const float (&a0)[4], const float (&a1)[4], const float (&a2)[4], const float (&bv)[6]) {
 #pragma unroll
-  for (int c = 0; c < CPT; ++c) {
-    const int xa = x + c * G, xb = xa + dj;  // this thread's column of a, and of b
-    const bool cm = ok && (unsigned)(xb - 1) < (unsigned)SS, c0 = ok && (unsigned)xb < (unsigned)SS,
-               cp = ok && (unsigned)(xb + 1) < (unsigned)SS;
-    const P* pb = fb + xb;
-#pragma unroll 1
-    for (int y0 = 0; y0 < SS; y0 += R) {
-      float av[R], bc[R + 2], bl[R], br[R];
-      const P* pa = fa + y0 * width + xa;
-#pragma unroll
-      for (int k = 0; k < R; ++k) av[k] = ok ? px<P>(pa + k * width) : 0.f;
-#pragma unroll
-      for (int k = 0; k < R + 2; ++k) {  // rows y0 + di - 1 .. y0 + di + R
-        const int r = y0 + k + di - 1;
-        const bool vr = (unsigned)r < (unsigned)SS;
-        const P* row = pb + r * width;
-        bc[k] = (vr && c0) ? px<P>(row) - mb : 0.f;
-        if (k >= 1 && k <= R) {
-          bl[k - 1] = (vr && cm) ? px<P>(row - 1) - mb : 0.f;
-          br[k - 1] = (vr && cp) ? px<P>(row + 1) - mb : 0.f;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        const float ap = ok ? av[k] - ma : 0.f;
-        s_c = fmaf(ap, bc[k + 1], s_c);
-        s_d = fmaf(ap, bc[k], s_d);
-        s_u = fmaf(ap, bc[k + 2], s_u);
-        s_l = fmaf(ap, bl[k], s_l);
-        s_r = fmaf(ap, br[k], s_r);
-      }
+    for (int k = 0; k < 4; ++k) {
+      s_d = fmaf(a0[k], bv[k + 1], s_d);
+      s_c = fmaf(a1[k], bv[k + 1], s_c);
+      s_l = fmaf(a1[k], bv[k], s_l);
+      s_r = fmaf(a1[k], bv[k + 2], s_r);
+      s_u = fmaf(a2[k], bv[k + 1], s_u);
     }
+  };
+  // Steps t with b row t + di - 1 inside b's window; a rows t - 1 and t - 2
+  // enter as zeros where they are above the window, a row t below it.
+  const int t0 = max(0, 1 - di), t1 = min(SS + 2, SS + 1 - di), tm = min(t1, SS);
+  float a1[4] = {0.f, 0.f, 0.f, 0.f}, a2[4] = {0.f, 0.f, 0.f, 0.f};
+  if (t0 >= 1 && t0 - 1 < SS) load_a(fa + (t0 - 1) * width, a1);
+  if (t0 >= 2 && t0 - 2 < SS) load_a(fa + (t0 - 2) * width, a2);
+  int t = t0;
+  const P* ra = fa + t0 * width;
+  const P* rb = fb + (t0 + di - 1) * width;
+  for (; t + R <= tm; t += R, ra += R * width, rb += R * width) {
+    float av[R][4], bv[R][6];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      load_a(ra + k * width, av[k]);
+      load_b(rb + k * width, bv[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      step(av[k], a1, a2, bv[k]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) a2[e] = a1[e], a1[e] = av[k][e];
+    }
+  }
+  for (; t < t1; ++t, ra += width, rb += width) {
+    float a0[4] = {0.f, 0.f, 0.f, 0.f}, bv[6];
+    if (t < SS) load_a(ra, a0);
+    load_b(rb, bv);
+    step(a0, a1, a2, bv);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) a2[e] = a1[e], a1[e] = a0[e];
   }
   // Stencil sums: c (di, dj), cd (di - 1), cu (di + 1), cl (dj - 1), cr (dj + 1).
   float c5[5] = {s_c, s_d, s_u, s_l, s_r};
-  group_sum<G, 5>(c5, part);
+  group_sum<G, 5>(c5);
   if (!ok || x != 0 || !in_bounds(loc >= 0 && loc < (long long)q->n_pairs * q->m * q->n)) return;
   float isp = (float)pi_, jsp = (float)pj;
   if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1)
@@ -184,22 +215,21 @@ PIV_D void refine_window(const CorrArgs& a, const CorrSeg* seg_s, int n_seg, lon
 
 template <int SS, typename P>
 __global__ void __launch_bounds__(kRefineThreads, 3) k_refine(CorrArgs a) {
-  constexpr int G = RefineGroup<SS>::G, WPB = kRefineThreads / G;
+  constexpr int G = SS / kCols, WPB = kRefineThreads / G;
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
-  __shared__ float part[kRefineThreads / 32 * 5];
   const int n_seg = load_segments(a, seg_s);
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int wl = threadIdx.x / G, x = threadIdx.x % G;
   // The loop bound is the same for every thread of the block (group sums).
   for (long long g0 = (long long)blockIdx.x * WPB; g0 < total; g0 += (long long)gridDim.x * WPB) {
     const long long g = g0 + wl;
-    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, x, part);
+    refine_window<SS, P>(a, seg_s, n_seg, g, g < total, x);
   }
 }
 
 template <int SS>
 int launch_refine_ss(const CorrArgs& a, cudaStream_t stream) {
-  constexpr int G = RefineGroup<SS>::G, WPB = kRefineThreads / G;
+  constexpr int G = SS / kCols, WPB = kRefineThreads / G;
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   long long blocks = (total + WPB - 1) / WPB;
   const long long cap = (long long)sm_count() * 8;

@@ -153,6 +153,14 @@ class PIVServer:
                     time.sleep(poll_interval)
         return self.done
 
+    def close(self):
+        """Finishes every submitted request, then releases every lane's plans
+        and device workspaces."""
+        self.drain()
+        for lane in self.lanes.values():
+            lane.release()
+        self.lanes.clear()
+
     # -- internals ---------------------------------------------------------
     def _collect(self):
         count = 0

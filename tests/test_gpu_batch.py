@@ -103,7 +103,9 @@ MANY_SHAPES = [(96 + 16 * (k % 5), 96 + 32 * (k // 5)) for k in range(10)] + [(9
 
 @pytest.mark.parametrize("dft,shapes,schedule", [
     ("tensor", MIXED_SHAPES, "joint"), ("tensor", MIXED_SHAPES, "streams"), ("tensor_split", MIXED_SHAPES, "joint"),
-    ("fft", MIXED_SHAPES, "joint"), ("tensor", MANY_SHAPES, "joint"), ("tensor", MIXED_SHAPES, "auto")])
+    ("fft", MIXED_SHAPES, "joint"), ("tensor", MANY_SHAPES, "joint"), ("tensor", MIXED_SHAPES, "auto"),
+    ("tensor_refined", MIXED_SHAPES, "joint"), ("tensor_refined", MANY_SHAPES, "joint"),
+    ("tensor_refined", MIXED_SHAPES, "streams")])
 def test_mixed_size_submission_equals_single_runs(dft, shapes, schedule):
     """PIVMixedBatch: pairs of several frame sizes in one submission (one
     correlation launch per pass over every size on the tensor engines),

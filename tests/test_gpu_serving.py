@@ -11,7 +11,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_results_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("dft", ["tensor", "tensor_refined"])
+def test_results_same_alone_and_in_the_mix(dft):
     import torch
 
     from openpiv_gpu import _build, synthetic
@@ -23,7 +24,7 @@ def test_results_same_alone_and_in_the_mix():
     settings = dict(synthetic.CONFIGS[5]["piv"])
     shapes = [(96, 128), (128, 160), (160, 96)]
     pairs = [synthetic.config_case(5, k, shape=shapes[k % 3])[:2] for k in range(11)]
-    server = PIVServer(settings, max_batch=3, slots_per_shape=2, hbm_reserve=0)
+    server = PIVServer(settings, max_batch=3, slots_per_shape=2, hbm_reserve=0, dft=dft)
     reqs = []
     for k, (a, b) in enumerate(pairs):
         reqs.append(server.submit(a, b))
@@ -38,10 +39,12 @@ def test_results_same_alone_and_in_the_mix():
     kw = dict(settings)
     mss = kw.pop("min_search_size")
     for req, (a, b) in zip(reqs, pairs):
-        alone = PIVGPU(a.shape, mss, dft="tensor", **kw)
+        alone = PIVGPU(a.shape, mss, dft=dft, **kw)
         u, v = alone.run_batch(a[None], b[None], host_out=True)
         np.testing.assert_array_equal(req.u, u[0])
         np.testing.assert_array_equal(req.v, v[0])
+    server.close()
+    assert not server.lanes
 
 
 def test_admission_waits_for_device_memory():
