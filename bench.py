@@ -59,8 +59,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--pairs", type=int, default=128, help="pairs per step per GPU")
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--dft", choices=["fft", "tensor", "tensor_split", "tensor_refined"], default="tensor",
-                    help="correlation engine of the chosen form")
+    ap.add_argument("--dft", choices=["fft", "tensor", "tensor_split", "tensor_refined"], default="tensor_refined",
+                    help="correlation engine of the chosen form (default: the refined tensor form, float32 FFT "
+                         "parity)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
@@ -69,15 +70,16 @@ def parse_args():
     ap.add_argument("--no-others", action="store_true",
                     help="skip timing the other tensor forms (fp16, hi/lo split, refined) beside the chosen one")
     ap.add_argument("--no-split", action="store_true",
-                    help="skip timing the hi/lo split tensor form beside the fp16 tensor form")
+                    help="skip timing the hi/lo split tensor form beside the chosen one")
     ap.add_argument("--serve", action="store_true",
                     help="serving form instead: Poisson arrivals of mixed-size pairs through the continuous-batching "
                          "loop, p50/p99 latency and pairs/s beside the plain per-pair path")
     ap.add_argument("--mixed", action="store_true",
                     help="batched form instead: one submission of 64 pairs of four frame sizes, replayed as one graph")
     ap.add_argument("--precision", action="store_true",
-                    help="precision form instead: 16 pairs of 2048x2048, 32->16 px at 75%% overlap, hi/lo split "
-                         "tensor form beside the fp16 tensor and plain FP32 FFT forms, RMS vs the float64 oracle")
+                    help="precision form instead: 16 pairs of 2048x2048, 32->16 px at 75%% overlap, the faster of "
+                         "the hi/lo split and refined tensor forms beside the other tensor forms and the plain FP32 "
+                         "FFT form, RMS vs the float64 oracle")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--requests", type=int, default=400, help="serving: number of requests")
     return ap.parse_args()
@@ -518,7 +520,8 @@ def run_gpu(args):
     roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
                 "traffic": per_window_traffic * n_win if per_window_traffic else None,
                 "kernel": f"correlate pass {kdom + 1} (ss={f.search_size}, N={N}, {n_win} windows/launch, "
-                          f"{'tcgen05' if on_tensor else 'fft'})",
+                          f"{'tcgen05' if on_tensor else 'fft'}"
+                          f"{'; the stage: fp16 engine, peak refinement and near-tie FFT reruns' if args.dft == 'tensor_refined' else ''})",
                 "peak_source": src, "launch_ms": corr[dom],
                 "algorithmic_flops_per_window": corr_flops(f.search_size, N)}
     if on_tensor:
@@ -614,9 +617,10 @@ def run_gpu(args):
 
 def run_serve(args):
     """Serving form: Poisson arrivals (rate args.rate) of pairs whose size is
-    drawn uniformly from the five serving sizes, through PIVServer (tensor
-    form, continuous batching, lanes per size) and, beside it, through the
-    plain per-pair path (each pair alone, in arrival order, FP32 FFT form)."""
+    drawn uniformly from the five serving sizes, through PIVServer (the chosen
+    form, then the other two tensor forms on the same arrivals; continuous
+    batching, lanes per size) and, beside it, through the plain per-pair path
+    (each pair alone, in arrival order, FP32 FFT form)."""
     import multiprocessing as mp
 
     import numpy as np
@@ -670,7 +674,7 @@ def run_serve(args):
         server.close()
         return res
 
-    served = {form: serve_form(form) for form in dict.fromkeys((args.dft, "tensor_refined"))}
+    served = {form: serve_form(form) for form in dict.fromkeys((args.dft, "tensor", "tensor_refined"))}
     # Plain per-pair path: each pair alone, in arrival order, on the FP32 FFT form.
     kw = dict(settings)
     mss = kw.pop("min_search_size")
@@ -720,7 +724,7 @@ def run_mixed(args):
     """Batched form: 64 pairs, 16 each of 512x512, 1280x800, 1024x768 and
     2048x2048 (each with its own seeded vortex or shear field), in one
     submission: per-size plans on their own streams for the per-field stages,
-    one correlation launch per pass over every size (tensor form), captured as
+    one correlation launch per pass over every size (tensor forms), captured as
     one CUDA graph, replayed K times (CUDA events). The plain FP32 FFT form of the same
     submission is timed beside it."""
     import multiprocessing as mp
@@ -745,7 +749,7 @@ def run_mixed(args):
     settings = dict(synthetic.CONFIGS[4]["piv"])
     shapes = [a.shape for a, _ in pairs]
     out = {}
-    for form in dict.fromkeys((args.dft, "tensor_refined", "fft")):
+    for form in dict.fromkeys((args.dft, "tensor", "tensor_refined", "fft")):
         batch = PIVMixedBatch(shapes, settings, dft=form)
         batch.load(pairs)
         batch.capture()
@@ -780,13 +784,13 @@ def run_mixed(args):
         "value": out[args.dft]["pairs_per_s"], "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "form": args.dft, "chosen": out[args.dft],
         "plain_form": out["fft"], "chosen_over_plain": out[args.dft]["pairs_per_s"] / out["fft"]["pairs_per_s"],
-        "refined_form": out["tensor_refined"],
-        "refined_over_plain": out["tensor_refined"]["pairs_per_s"] / out["fft"]["pairs_per_s"],
+        "other_forms": {f: dict(r, over_plain=r["pairs_per_s"] / out["fft"]["pairs_per_s"])
+                        for f, r in out.items() if f not in (args.dft, "fft")},
         "config": {"workload": "16 pairs each of 512x512, 1280x800, 1024x768, 2048x2048; density U[0.01, 0.05], "
                                "vortex or shear up to 10 px; 64->32->16 px @50%, median validation, 2 revalidated "
                                "spring replacements, smoothn GCV; float32",
                    "graph": "one CUDA graph per submission: per-size plans on their own streams for the "
-                            "per-field stages; one correlation launch per pass over all four sizes (tensor form)",
+                            "per-field stages; one correlation launch per pass over all four sizes (tensor forms)",
                    "data": "synthetic (seeded particle images)"},
     }
     print(json.dumps(line), flush=True)
