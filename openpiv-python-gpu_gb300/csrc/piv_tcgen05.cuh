@@ -36,6 +36,11 @@ PIV_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// One arrival (release semantics, CTA scope) on `bar`.
+PIV_D void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Polls until the phase with `parity` completes; gives up after max_polls and
 // returns false (each try_wait itself suspends for a hardware-defined time).
 PIV_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_polls) {

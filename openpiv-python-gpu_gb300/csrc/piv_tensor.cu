@@ -16,7 +16,11 @@
 //            each thread finds both halves of its complex column in its own lane.
 //   product  Q(f_r, c) = conj(A) B for c = 1 .. N/2-1 and all f_r; row c = 0
 //            packs the two real-input columns: Q = conj(A0) B0 + i conj(AN) BN.
-//   stage 3  U = Q E / N rows (w, c),              K = (Re|Im, f_r), cols (Re|Im, r)
+//            Each frequency pair (g, N - g) is folded into P = Q(g) + Q(N-g)
+//            and M = Q(g) - Q(N-g), so that the inverse along f_r needs only
+//            cosines and sines of g = 0 .. N/2-1:
+//   stage 3  U = Q E / N rows (w, c), two products:  Re U = [Re P | Im M] [C; -S],
+//            Im U = [Im P | Re M] [C; S], K = N each, cols r
 //   stage 4  c = U E' / N rows (w, r),             K = (Re|Im, c),   cols s
 // where E is the inverse DFT along f_r and E' the real inverse along f_c
 // (U(r, N-c) = conj U(r, c)). Each frame's window is scaled by a power of two
@@ -50,11 +54,11 @@ struct TcLayout {
   static constexpr int W = 128 / SS;         // window pairs per tile
   static constexpr int TCOLS = 4 * N;        // TMEM columns (stage 2: two frames x two row tiles)
   static constexpr int P = SPLIT ? 2 : 1;    // copies of every operand
-  static constexpr int NB1 = N * SS * 2, NB3 = 2 * N * 2 * N * 2, NB4 = N * N * 2, NOP = 1024 * SS;
+  static constexpr int NB1 = N * SS * 2, NB3 = N * HN * 2, NB4 = N * N * 2, NOP = 1024 * SS;
   // Byte offsets in dynamic shared memory (16-byte aligned).
   static constexpr int B1 = 0;                          // F [N][SS] K-major (stages 1 and 2)
-  static constexpr int B3 = B1 + P * NB1;               // [2N][2N] K-major
-  static constexpr int B4 = B3 + P * NB3;               // [N][N] K-major
+  static constexpr int B3 = B1 + P * NB1;               // stage 3: blocks C, -S, S [N][HN] K-major
+  static constexpr int B4 = B3 + 3 * P * NB3;           // [N][N] K-major
   // Operand region, rewritten by each phase once the product that read it has
   // completed: A1 2 x [128][SS] K-major; A2 2 x 2 x [128][SS] MN-major; A3
   // [128][2N] K-major; A4 2 x [128][N] MN-major; then the peak-neighbour rows.
@@ -324,6 +328,38 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
   return q;
 }
 
+// The folded pair: P = Q(g) + Q(N - g) and M = Q(g) - Q(N - g) of
+// pair_product's outputs. Row c = 0 in closed form (no cancellation of the
+// packed halves): Re P = 2 Re conj(E_a) E_b, Im P = 2 Re conj(O_a) O_b,
+// Re M = -2 Im conj(O_a) O_b, Im M = 2 Im conj(E_a) E_b. Every part is at
+// most |A| |B| + |A'| |B'|, twice the bound of one spectrum product.
+struct PairPM {
+  float pr, pi, mr, mi;
+};
+PIV_D PairPM pair_fold(float ar, float ai, float orr, float oi, float br, float bi, float pr, float pi,
+                       bool special) {
+  const PairQ q = pair_product(ar, ai, orr, oi, br, bi, pr, pi, special);
+  const float re1 = fmaf(ar, br, ai * bi), im1 = fmaf(ar, bi, -ai * br);     // conj(E_a) E_b
+  const float re2 = fmaf(orr, pr, oi * pi), im2 = fmaf(orr, pi, -oi * pr);   // conj(O_a) O_b
+  PairPM o;
+  o.pr = special ? 2.f * re1 : q.r0 + q.r1;
+  o.pi = special ? 2.f * re2 : q.i0 + q.i1;
+  o.mr = special ? -2.f * im2 : q.r0 - q.r1;
+  o.mi = special ? 2.f * im1 : q.i0 - q.i1;
+  return o;
+}
+
+// Stage-3 operand columns (K = 2N) of one row: [Re P | Im M | Im P | Re M],
+// N/2 columns each; at g = 0 the slots hold Re Q(0), Re Q(N/2), Im Q(0) and
+// Im Q(N/2) (the unpaired frequencies), whose inverse weights are 1 and
+// (-1)^r. Value of block k (0: C, 1: -S, 2: S) at output r, column g, for
+// cos / sin of 2 pi g r / N scaled by s.
+PIV_D float stage3_weight(int blk, int r, int g, float cs, float sn, float s) {
+  if (blk == 0) return cs;
+  if (g == 0) return (r & 1) ? -s : s;
+  return blk == 1 ? -sn : sn;
+}
+
 // Whether any segment asks for near-tie flags or counts.
 PIV_D bool any_tie_output(const CorrSeg* seg_s, int n_seg) {
   bool any = false;
@@ -389,14 +425,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   // The split form keeps the inverse DFTs' 1/N out of B3 and B4 (their lo
   // parts would fall below the fp16 normal range) and scales Q and U instead.
   const float bscale = SPLIT ? 1.0f : inv_n;
-  for (int e = tid; e < 4 * N * N; e += NT) {  // B3[n][kappa], kappa = (part, b, g)
-    const int n = e / (2 * N), kap = e % (2 * N);
-    const int part = kap / N, b = (kap % N) / HN, g = kap % HN;
-    const int fr = b == 0 ? g : (g == 0 ? HN : N - g), r = n % N;
-    const int q = (fr * r) % N;
-    const float cs = tw_re[q] * bscale, sn = -tw_im[q] * bscale;
-    const float v = n < N ? (part == 0 ? cs : -sn) : (part == 0 ? sn : cs);
-    sths<SPLIT>(sm + L::B3, L::NB3, off_k(n, kap, 2 * N), v);
+  for (int e = tid; e < 3 * N * HN; e += NT) {  // B3 blocks C, -S, S: [r][g]
+    const int blk = e / (N * HN), r = (e / HN) % N, g = e % HN;
+    const int q = (g * r) % N;
+    const float v = stage3_weight(blk, r, g, tw_re[q] * bscale, -tw_im[q] * bscale, bscale);
+    sths<SPLIT>(sm + L::B3 + blk * L::P * L::NB3, L::NB3, off_k(r, g, HN), v);
   }
   for (int e = tid; e < N * N; e += NT) {  // B4[s][kappa], kappa = (part, c)
     const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
@@ -643,8 +676,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     }
     wait_mma();
 
-    // ---- Product: thread (w, c) forms row c of Q, K = (Re|Im, b, g) with
-    // f_r = g (b = 0) or N - g (b = 1; g = 0 pairs with f_r = N/2).
+    // ---- Product: thread (w, c) forms row c of the stage-3 operand,
+    // [Re P | Im M | Im P | Re M] of the folded pairs (g, N - g); at g = 0
+    // Re Q(0), Re Q(N/2), Im Q(0), Im Q(N/2).
     {
       const bool special = (t % HN) == 0;
       unsigned char* dst = sm + L::OP;
@@ -658,34 +692,40 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         tld(tmem + lane_sel + 3 * N + 2 * g0, ob);
         tc::tmem_ld_wait();
         tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
-        float qr0[8], qi0[8], qr1[8], qi1[8];
+        float rp[8], im[8], ip[8], rm[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          PairQ q;
+          PairPM o;
           if (g0 + i == 0) {
-            // f_r = 0 and f_r = N/2: real spectra R[0] and R[1].
+            // f_r = 0 and f_r = N/2: real spectra R[0] and R[1], not folded.
             const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
             const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
-            q.r0 = q0.r0; q.i0 = q0.i0; q.r1 = q1.r0; q.i1 = q1.i0;
+            o.pr = q0.r0; o.mi = q1.r0; o.pi = q0.i0; o.mr = q1.i0;
           } else {
-            q = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
-                             ob[2 * i], ob[2 * i + 1], special);
+            o = pair_fold(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                          ob[2 * i], ob[2 * i + 1], special);
           }
-          qr0[i] = q.r0 * oscale; qi0[i] = q.i0 * oscale; qr1[i] = q.r1 * oscale; qi1[i] = q.i1 * oscale;
+          rp[i] = o.pr * oscale; im[i] = o.mi * oscale; ip[i] = o.pi * oscale; rm[i] = o.mr * oscale;
         }
-        st8s<SPLIT>(dst, L::NOP, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
-        st8s<SPLIT>(dst, L::NOP, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
-        st8s<SPLIT>(dst, L::NOP, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
-        st8s<SPLIT>(dst, L::NOP, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 0 * HN + g0, 2 * N), rp);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 1 * HN + g0, 2 * N), im);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 2 * HN + g0, 2 * N), ip);
+        st8s<SPLIT>(dst, L::NOP, off_k(t, 3 * HN + g0, 2 * N), rm);
       }
     }
     if (!sync_for_mma()) break;
 
-    // ---- Stage 3: U = Q E / N -> TMEM cols [0, 2N).
+    // ---- Stage 3: Re U = [Re P | Im M] [C; -S] -> TMEM cols [0, N),
+    // Im U = [Im P | Re M] [C; S] -> cols [N, 2N).
     if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
-      const uint32_t id = tc::idesc_f16(128, 2 * N, 0, 0);
-      mma_chain<SPLIT>(tmem, sbase + L::OP, L::NOP, 256, 128, 2 * N * 16, sbase + L::B3, L::NB3, 256, 128,
-                       2 * N * 16, 2 * N / 16, id, false);
+      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+#pragma unroll
+      for (int part = 0; part < 2; ++part)
+#pragma unroll
+        for (int kb = 0; kb < 2; ++kb)
+          mma_chain<SPLIT>(tmem + part * N, sbase + L::OP + (part * N + kb * HN) * 16, L::NOP, 256, 128, 2 * N * 16,
+                           sbase + L::B3 + (kb == 0 ? 0 : 1 + part) * L::P * L::NB3, L::NB3, 256, 128, HN * 16,
+                           HN / 16, id, kb > 0);
       tc::mma_commit<SPLIT>(&bar);
     }
     wait_mma();
@@ -903,28 +943,41 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 }
 
 // ---------------------------------------------------------------------------
-// 64-pixel windows (N = 128). The operands and constants need 208 KB of shared
-// memory and the stage-2 spectra all 512 TMEM columns, so one CTA runs per SM
-// with 512 threads, four per TMEM lane (warp w reads lanes 32 (w % 4)); each
-// phase splits its columns (or frames) between the four. The four operand
-// tiles live one after the other in a single 64 KB region: each phase writes
-// its operand only after the previous product has completed. Stage 3 uses
-// E = [[C, -S], [S, C]] / N from three 128 x 128 blocks instead of the full
-// 256 x 256 matrix.
+// 64-pixel windows (N = 128), warp-specialised and pipelined over tiles. One
+// CTA per SM with 16 compute warps (512 threads, four per TMEM lane; warp w
+// reads lanes 32 (w % 4); each phase splits its columns or frames between the
+// four) and one MMA warp. The MMA warp issues each product as soon as the
+// compute warps have written its operand (one arrival per compute warp on
+// that operand's "ready" mbarrier) and commits it to the product's own
+// mbarrier, so the tensor core and the compute warps work on different
+// phases at the same time: tile i + 1 is staged while stage 4 of tile i runs,
+// the map of tile i is searched while stage 1 of tile i + 1 runs, and the
+// product of the first half of stage 2 (f_r columns 0-63) is formed while
+// the second half is computed.
+//   TMEM: stage 1 -> columns [256, 512); stage 2 half 0 -> [0, 256), half 1
+//   -> [256, 512); stages 3 and 4 -> [0, 256).
+//   Shared memory (208 KB): constants F (16 KB), C / -S / S (48 KB) and E'
+//   (32 KB); the stage-1 operands (32 KB, then the first half of the stage-3
+//   operand); a 64 KB region for the stage-2 operands, then the second half
+//   of the stage-3 operand, the stage-4 operands and the peak-neighbour rows;
+//   the next tile's 8-bit rows (16 KB).
 // ---------------------------------------------------------------------------
 struct Tc64 {
-  static constexpr int SS = 64, N = 128, HN = 64, W = 2, NT = 512, TCOLS = 512;
-  static constexpr int B1 = 0;                  // F [N][SS] K-major
-  static constexpr int BC = B1 + N * SS * 2;    // cos / N   [N][N] K-major, K = (b, g)
-  static constexpr int BS = BC + N * N * 2;     // sin / N
-  static constexpr int BNS = BS + N * N * 2;    // -sin / N
-  static constexpr int B4 = BNS + N * N * 2;    // [N][N] K-major, K = (part, c)
-  static constexpr int OP = B4 + N * N * 2;     // operand region (then the peak-neighbour rows)
-  static constexpr int STG = OP + 65536;        // next tile's 8-bit rows [frame][w][y][64 B], chunks swizzled
+  static constexpr int SS = 64, N = 128, HN = 64, W = 2, TCOLS = 512;
+  static constexpr int NCW = 16, NC = 32 * NCW, NT = NC + 32;  // compute warps, their threads, all threads
+  static constexpr int NB3 = N * HN * 2;
+  static constexpr int B1 = 0;                      // F [N][SS] K-major
+  static constexpr int B3 = B1 + N * SS * 2;        // stage 3: blocks C, -S, S (/ N) [N][HN] K-major
+  static constexpr int B4 = B3 + 3 * NB3;           // [N][N] K-major, K = (part, c)
+  static constexpr int A1 = B4 + N * N * 2;         // 2 x [128][SS] K-major; then stage-3 operand half 0
+  static constexpr int OP = A1 + 2 * 128 * SS * 2;  // 64 KB operand region (then the neighbour rows)
+  static constexpr int STG = OP + 65536;            // next tile's 8-bit rows [frame][w][y][64 B], chunks swizzled
   static constexpr int END = STG + 2 * W * SS * SS;
-  static constexpr int A1_BYTES = 128 * SS * 2; // per frame, K-major [128][SS]
-  static constexpr int A2_BYTES = 128 * SS * 2; // per (frame, tile), MN-major [128][SS]
-  static constexpr int A4_BYTES = 128 * N * 2;  // per tile, MN-major [128][N]
+  static constexpr int A1_BYTES = 128 * SS * 2;     // per frame, K-major [128][SS]
+  static constexpr int A2_BYTES = 128 * SS * 2;     // per (frame, tile), MN-major [128][SS]
+  static constexpr int A4_BYTES = 128 * N * 2;      // per tile, MN-major [128][N]
+  static constexpr int QH = 128;                    // columns of one half of the stage-3 operand (K-major)
+  static constexpr uint32_t T_S1 = 256;             // TMEM column of the stage-1 outputs
   static constexpr size_t SMEM = END;
 };
 
@@ -933,20 +986,28 @@ PIV_D int stg64_chunk(int t, int k) { return k ^ ((t >> 1) & 3); }
 
 // ASYNC: 8-bit frames whose window rows start on 16-byte boundaries; the next
 // tile's rows are copied with cp.async while the current tile runs.
+// Registers: the 17 warps are spread over the SM's four sub-partitions (16K
+// registers each), five on the first, so a thread may hold at most 96.
 template <bool ASYNC>
-__global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
+__global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   using L = Tc64;
   constexpr int SS = L::SS, N = L::N, HN = L::HN, W = L::W;
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ uint64_t bar;
+  // Completion of each product (committed by the MMA warp) and readiness of
+  // each operand (one arrival per compute warp). Each completes once per tile.
+  enum { kS1, kS2a, kS2b, kS3, kS4, kNDone };
+  enum { kRA1, kRA2, kRQ, kRA4, kNReady };
+  __shared__ uint64_t done_bar[kNDone], ready_bar[kNReady];
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
   __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
-  __shared__ int sc_e[2][W];
-  __shared__ long long win_base[2][W];
-  __shared__ int win_valid[2][W];
-  __shared__ long long win_loc[2][W];  // window index within its segment
-  __shared__ int win_seg[2][W];
+  // Per tile slot (three: the tile being correlated, the next one, whose rows
+  // are in flight, and the one after, whose corners are being computed).
+  __shared__ int sc_e[3][2][W];
+  __shared__ long long win_base[3][W];
+  __shared__ int win_valid[3][W];
+  __shared__ long long win_loc[3][W];  // window index within its segment
+  __shared__ int win_seg[3][W];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ unsigned long long pk_key[W];  // per window: the running first maximum (peak_key)
   __shared__ unsigned sec_key[W];           // per window: key of the largest half-row maximum outside the peak row
@@ -965,7 +1026,8 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     tw_im[k] = -sn;
   }
   if (tid == 0) {
-    tc::mbar_init(&bar, 1);
+    for (int k = 0; k < kNDone; ++k) tc::mbar_init(&done_bar[k], 1);
+    for (int k = 0; k < kNReady; ++k) tc::mbar_init(&ready_bar[k], L::NCW);
     abort_s = 0;
   }
   __syncthreads();
@@ -979,14 +1041,11 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
     else v = (k & 1) ? tw_im[qq] : tw_re[qq];
     sth(sm + L::B1, off_k(k, x, SS), v);
   }
-  for (int e = tid; e < N * N; e += L::NT) {  // C, S, -S [r][kappa = (b, g)]
-    const int r = e / N, kap = e % N, b = kap / HN, g = kap % HN;
-    const int fr = b == 0 ? g : (g == 0 ? HN : N - g);
-    const int qq = (fr * r) % N;
-    const float cs = tw_re[qq] * inv_n, sn = -tw_im[qq] * inv_n;
-    sth(sm + L::BC, off_k(r, kap, N), cs);
-    sth(sm + L::BS, off_k(r, kap, N), sn);
-    sth(sm + L::BNS, off_k(r, kap, N), -sn);
+  for (int e = tid; e < 3 * N * HN; e += L::NT) {  // B3 blocks C, -S, S: [r][g]
+    const int blk = e / (N * HN), r = (e / HN) % N, g = e % HN;
+    const int qq = (g * r) % N;
+    sth(sm + L::B3 + blk * L::NB3, off_k(r, g, HN),
+        stage3_weight(blk, r, g, tw_re[qq] * inv_n, -tw_im[qq] * inv_n, inv_n));
   }
   for (int e = tid; e < N * N; e += L::NT) {  // B4[s][kappa = (part, c)]
     const int s_ = e / N, kap = e % N, part = kap / HN, c = kap % HN;
@@ -1002,114 +1061,176 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base_s;
-  // TMEM loads of the CTA's allocation (checked build: columns inside it).
-  auto tld = [&](uint32_t addr, float (&v)[16]) {
-    if (in_bounds(((addr - tmem) & 0xffffu) + 16 <= (uint32_t)L::TCOLS)) tc::tmem_ld16(addr, v);
-  };
   const uint32_t sbase = tc::smem_u32(sm);
-  uint32_t phase = 0;
 
   const int n_seg = load_segments(a, seg_s);
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + W - 1) / W);
+  const int first = blockIdx.x, stride = gridDim.x;
 
-  // Every thread waits for the last commit itself; a wait that gives up sets
-  // abort_s, which all threads read after the next barrier and leave the tile
-  // loop together.
-  auto wait_mma = [&]() {
-    const bool ok = tc::mbar_wait_bounded(&bar, phase, kMaxPolls);
-    phase ^= 1u;
-    if (!ok) {
-      abort_s = 1;
-      atomicExch(status, PIV_E_TIMEOUT);
-    }
-    tc::fence_after_sync();
-  };
-  auto sync_for_mma = [&]() -> bool {
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    return abort_s == 0;
-  };
-  auto window_setup = [&](int tl, int sl) {
-    const long long g = (long long)tl * W + tid;
-    int ok = tl < n_tiles && g < total;
-    long long base = 0, loc = 0;
-    int sg = 0;
-    if (ok) {
-      while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
-      const CorrSeg& q = seg_s[sg];
-      loc = g - q.win0;
-      // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
-      const int li = (int)loc, nw = q.m * q.n;
-      const int pair = li / nw, k = li - pair * nw;
-      const int wr = k / q.n, wc = k - wr * q.n;
-      if (q.win_mask) ok = q.win_mask[k] == 0;
-      base = pair * (long long)q.height * q.width + (long long)(wr * q.spacing + q.y_offset) * q.width +
-             wc * q.spacing + q.x_offset;
-      if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * q.width + SS <=
-                                             (long long)q.n_pairs * q.height * q.width))
-        ok = 0;
-    }
-    win_valid[sl][tid] = ok;
-    win_base[sl][tid] = base;
-    win_loc[sl][tid] = loc;
-    win_seg[sl][tid] = sg;
-  };
-  // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it
-  // stages itself; rows of invalid windows are zero-filled (no global read).
-  auto stage_async = [&](int sl) {
-    const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
-    const bool ok = win_valid[sl][w] != 0;
-    const CorrSeg& sq = seg_s[win_seg[sl][w]];
-    const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? sq.frame_a : sq.frame_b) +
-                         (ok ? win_base[sl][w] + (long long)y * sq.width + 16 * 2 * h : 0);
-    const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS);
+  if (warp == L::NCW) {
+    // ---- MMA warp: lane 0 waits for each operand, issues the product and
+    // commits it; a wait that gives up stops the warp (the compute warps'
+    // own waits then give up as well).
+    uint32_t ph[kNReady] = {0u, 0u, 0u, 0u};
+    auto ready = [&](int k) -> bool {
+      bool ok = true;
+      if (lane == 0) {
+        ok = tc::mbar_wait_bounded(&ready_bar[k], ph[k], kMaxPolls);
+        if (!ok) {
+          abort_s = 1;
+          atomicExch(status, PIV_E_TIMEOUT);
+        }
+      }
+      ph[k] ^= 1u;
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      tc::fence_after_sync();
+      return ok;
+    };
+    // Stage 1: T = a F^T per frame -> TMEM cols [T_S1 + f N, + N).
+    auto stage1 = [&]() {
+      if (lane == 0) {
+        const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
-    for (int c = 0; c < 2; ++c) cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
-  };
-
-  if (tid < W) {
-    pk_key[tid] = 0ull;
-    sec_key[tid] = kKeyNegInf;
-    window_setup(blockIdx.x, 0);
-  }
-  __syncthreads();
-  if (ASYNC) {
-    stage_async(0);
-    cp_async_commit();
-  }
-  const bool ties = any_tie_output(seg_s, n_seg);
-  // Near-tie flag of window `lane` of the current tile (lanes < W of the
-  // calling warp; tile_near_ties's result) to the window's outputs.
-  int cur_sl = 0;
-  long long cur_g0 = 0;
-  auto write_near_ties = [&](bool tie) {
-    if (lane >= W || cur_g0 + lane >= total) return;
-    const CorrSeg& sq = seg_s[win_seg[cur_sl][lane]];
-    const long long gl = win_loc[cur_sl][lane];
-    tie = tie && win_valid[cur_sl][lane];
-    if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
-    if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
-    if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
-  };
-
-  int sl = 0;
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
-    const long long g0 = (long long)tile * W;
-    if (ASYNC) cp_async_wait_all();
-    __syncthreads();
-    // The previous tile's epilogue has finished with the peak and near-tie keys.
-    if (tid < W) {
-      pk_key[tid] = 0ull;
-      sec_key[tid] = kKeyNegInf;
+        for (int f = 0; f < 2; ++f)
+#pragma unroll
+          for (int ks = 0; ks < SS / 16; ++ks)
+            tc::mma_f16(tmem + L::T_S1 + f * N, tc::sdesc(sbase + L::A1 + f * L::A1_BYTES + ks * 256, 128, SS * 16),
+                        tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16), id, ks > 0);
+        tc::mma_commit(&done_bar[kS1]);
+      }
+      __syncwarp();
+    };
+    if (first < n_tiles && ready(kRA1)) {
+      stage1();
+      for (int tile = first; tile < n_tiles; tile += stride) {
+        // Stage 2 in two halves of f_r: X = T^T F^T, packed columns [64 h, 64 h + 64)
+        // of spectrum (rt, f) -> TMEM cols [256 h + (2 rt + f) 64, + 64).
+        if (!ready(kRA2)) break;
+        if (lane == 0) {
+          const uint32_t id = tc::idesc_f16(128, HN, 1, 0);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int rt = 0; rt < 2; ++rt)
+#pragma unroll
+              for (int f = 0; f < 2; ++f)
+#pragma unroll
+                for (int ks = 0; ks < SS / 16; ++ks)
+                  tc::mma_f16(tmem + 256 * h + (rt * 2 + f) * HN,
+                              tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128),
+                              tc::sdesc(sbase + L::B1 + h * 8 * SS * 16 + ks * 256, 128, SS * 16), id, ks > 0);
+            tc::mma_commit(&done_bar[h == 0 ? kS2a : kS2b]);
+          }
+        }
+        __syncwarp();
+        // Stage 3: Re U = [Re P | Im M] [C; -S] -> cols [0, N); Im U = [Im P | Re M] [C; S]
+        // -> cols [N, 2N). Block b4 of the operand (Re P, Im M, Im P, Re M), g in
+        // [16 s, 16 s + 16), sits in half s / 2 at column 32 b4 + 16 (s % 2).
+        if (!ready(kRQ)) break;
+        if (lane == 0) {
+          const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+#pragma unroll
+          for (int part = 0; part < 2; ++part)
+#pragma unroll
+            for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+              for (int s = 0; s < HN / 16; ++s) {
+                const int b4 = 2 * part + kb;
+                const uint32_t ab = (s >> 1) == 0 ? L::A1 : L::OP;
+                tc::mma_f16(tmem + part * N, tc::sdesc(sbase + ab + (32 * b4 + 16 * (s & 1)) * 16, 128, L::QH * 16),
+                            tc::sdesc(sbase + L::B3 + (kb == 0 ? 0 : 1 + part) * L::NB3 + s * 256, 128, HN * 16), id,
+                            (kb | s) != 0);
+              }
+          tc::mma_commit(&done_bar[kS3]);
+        }
+        __syncwarp();
+        // Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
+        if (!ready(kRA4)) break;
+        if (lane == 0) {
+          const uint32_t id = tc::idesc_f16(128, N, 1, 0);
+#pragma unroll
+          for (int rt = 0; rt < 2; ++rt)
+#pragma unroll
+            for (int ks = 0; ks < N / 16; ++ks)
+              tc::mma_f16(tmem + rt * N, tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128),
+                          tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16), id, ks > 0);
+          tc::mma_commit(&done_bar[kS4]);
+        }
+        __syncwarp();
+        if (tile + stride < n_tiles) {
+          if (!ready(kRA1)) break;
+          stage1();
+        }
+      }
     }
-    cur_sl = sl;
-    cur_g0 = g0;
-
-    // ---- Staging: thread (q, t) takes half h = q >> 1 of row y of window w of frame f = q & 1.
-    {
+  } else {
+    // ---- Compute warps (512 threads).
+    // TMEM loads of the CTA's allocation (checked build: columns inside it).
+    auto tld = [&](uint32_t addr, float (&v)[16]) {
+      if (in_bounds(((addr - tmem) & 0xffffu) + 16 <= (uint32_t)L::TCOLS)) tc::tmem_ld16(addr, v);
+    };
+    auto cw_sync = []() { asm volatile("bar.sync 1, %0;" ::"n"(L::NC) : "memory"); };
+    uint32_t ph[kNDone] = {0u, 0u, 0u, 0u, 0u};
+    // Every thread waits for the product itself; a wait that gives up sets
+    // abort_s, which all threads read after the tile's last barrier.
+    auto done = [&](int k) {
+      const bool ok = tc::mbar_wait_bounded(&done_bar[k], ph[k], kMaxPolls);
+      ph[k] ^= 1u;
+      if (!ok) {
+        abort_s = 1;
+        atomicExch(status, PIV_E_TIMEOUT);
+      }
+      tc::fence_after_sync();
+    };
+    // This warp's operand writes (and its TMEM loads) are complete.
+    auto signal = [&](int k) {
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&ready_bar[k]);
+    };
+    auto window_setup = [&](int tl, int sl) {
+      const long long g = (long long)tl * W + tid;
+      int ok = tl < n_tiles && g < total;
+      long long base = 0, loc = 0;
+      int sg = 0;
+      if (ok) {
+        while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
+        const CorrSeg& sq = seg_s[sg];
+        loc = g - sq.win0;
+        // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
+        const int li = (int)loc, nw = sq.m * sq.n;
+        const int pair = li / nw, k = li - pair * nw;
+        const int wr = k / sq.n, wc = k - wr * sq.n;
+        if (sq.win_mask) ok = sq.win_mask[k] == 0;
+        base = pair * (long long)sq.height * sq.width + (long long)(wr * sq.spacing + sq.y_offset) * sq.width +
+               wc * sq.spacing + sq.x_offset;
+        if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * sq.width + SS <=
+                                              (long long)sq.n_pairs * sq.height * sq.width))
+          ok = 0;
+      }
+      win_valid[sl][tid] = ok;
+      win_base[sl][tid] = base;
+      win_loc[sl][tid] = loc;
+      win_seg[sl][tid] = sg;
+    };
+    // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it
+    // stages itself; rows of invalid windows are zero-filled (no global read).
+    auto stage_async = [&](int sl) {
+      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
+      const bool ok = win_valid[sl][w] != 0;
+      const CorrSeg& sq = seg_s[win_seg[sl][w]];
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(f == 0 ? sq.frame_a : sq.frame_b) +
+                           (ok ? win_base[sl][w] + (long long)y * sq.width + 16 * 2 * h : 0);
+      const uint32_t row = sbase + L::STG + (uint32_t)((f * 128 + t) * SS);
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
+    };
+    // Staging of the tile in slot sl -> stage-1 operands: thread (q, t) takes
+    // half h = q >> 1 of row y of window w of frame f = q & 1.
+    auto stage_tile = [&](int sl) {
       const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63, grp = h * 2 + ((t >> 5) & 1);
       const bool ok = win_valid[sl][w] != 0;
       float r[32];
@@ -1133,7 +1254,7 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
       if (lane == 0) red[f][w][grp] = sum;
-      __syncthreads();
+      cw_sync();
       const float mean = (red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3]) / (float)(SS * SS);
       float l = 0.f;
 #pragma unroll
@@ -1143,9 +1264,9 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-      __syncthreads();
+      cw_sync();
       if (lane == 0) red[f][w][grp] = l;
-      __syncthreads();
+      cw_sync();
       const float l1 = red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3];
       int e = 0;
       if (l1 > 0.f) e = min(120, max(-120, 6 - exp2_floor(l1)));
@@ -1153,260 +1274,252 @@ __global__ void __launch_bounds__(512, 1) k_corr_tc64(CorrArgs a, int* status) {
 #pragma unroll
       for (int x = 0; x < 32; ++x) r[x] *= s;
       if (h == 0 && y == 0) {
-        sc_e[f][w] = e;
+        sc_e[sl][f][w] = e;
         const CorrSeg& sq = seg_s[win_seg[sl][w]];
         if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
       }
 #pragma unroll
-      for (int x = 0; x < 32; x += 8) st8(sm + L::OP + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
-    }
-    if (!sync_for_mma()) break;
+      for (int x = 0; x < 32; x += 8) st8(sm + L::A1 + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
+    };
 
-    // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
-    if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
-#pragma unroll
-      for (int f = 0; f < 2; ++f)
-#pragma unroll
-        for (int ks = 0; ks < SS / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::OP + f * L::A1_BYTES + ks * 256, 128, SS * 16);
-          const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
-          tc::mma_f16(tmem + f * N, ad, bd, id, ks > 0);
-        }
-      tc::mma_commit(&bar);
-    }
-    // The next tile's window corners, while the products run (slot sl ^ 1 was
-    // last read by the previous tile's fits, before its final barrier).
-    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
-    wait_mma();
+    const bool ties = any_tie_output(seg_s, n_seg);
+    // Near-tie flag of window `lane` of the current tile (lanes < W of the
+    // calling warp; tile_near_ties's result) to the window's outputs.
+    int cur_sl = 0;
+    long long cur_g0 = 0;
+    auto write_near_ties = [&](bool tie) {
+      if (lane >= W || cur_g0 + lane >= total) return;
+      const CorrSeg& sq = seg_s[win_seg[cur_sl][lane]];
+      const long long gl = win_loc[cur_sl][lane];
+      tie = tie && win_valid[cur_sl][lane];
+      if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
+      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
+    };
 
-    // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
-    {
-      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
-      float v[64];
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16)
-        tld(tmem + lane_sel + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
-      tc::reg_fence(v);
-#pragma unroll
-      for (int rt = 0; rt < 2; ++rt) {
-        unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
-#pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += 8) {
-          float v8[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
-          st8(dst, off_mn(w * HN + 32 * h + c0, y, 128), v8);
-        }
+    if (tid < W) {
+      window_setup(first, 0);
+      window_setup(first + stride, 1);
+    }
+    cw_sync();
+    if (first < n_tiles) {
+      if (ASYNC) {
+        stage_async(0);
+        cp_async_commit();
+        cp_async_wait_all();
+        cw_sync();
       }
-    }
-    if (!sync_for_mma()) break;
-    if (ASYNC) {
-      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
-      cp_async_commit();
+      stage_tile(0);
+      signal(kRA1);
     }
 
-    // ---- Stage 2: X = T^T F^T -> TMEM cols [(rt 2 + f) N, +N).
-    if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, N, 1, 0);
-#pragma unroll
-      for (int rt = 0; rt < 2; ++rt)
-#pragma unroll
-        for (int f = 0; f < 2; ++f)
-#pragma unroll
-          for (int ks = 0; ks < SS / 16; ++ks) {
-            const uint64_t ad =
-                tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128);
-            const uint64_t bd = tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16);
-            tc::mma_f16(tmem + (rt * 2 + f) * N, ad, bd, id, ks > 0);
-          }
-      tc::mma_commit(&bar);
-    }
-    wait_mma();
+    int sl = 0;
+    for (int tile = first; tile < n_tiles; tile += stride) {
+      const long long g0 = (long long)tile * W;
+      const int sl1 = sl == 2 ? 0 : sl + 1, sl2 = sl1 == 2 ? 0 : sl1 + 1;
+      const bool has_next = tile + stride < n_tiles;
+      // The previous tile's epilogue has finished with the peak and near-tie
+      // keys and with slot sl2 (its own slot).
+      if (tid < W) {
+        pk_key[tid] = 0ull;
+        sec_key[tid] = kKeyNegInf;
+        window_setup(tile + 2 * stride, sl2);
+      }
+      cur_sl = sl;
+      cur_g0 = g0;
 
-    // ---- Product: thread (q, t) forms g in [16 q, 16 q + 16) of row c = t % HN of window t / HN.
-    {
-      const bool special = (t % HN) == 0;
-      unsigned char* dst = sm + L::OP;
+      // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
+      done(kS1);
+      {
+        const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
+        float v[64];
 #pragma unroll
-      for (int gc = 0; gc < 16; gc += 8) {
-        const int g0 = 16 * q + gc;
-        float ea[16], eb[16], oa[16], ob[16];
-        tld(tmem + lane_sel + 0 * N + 2 * g0, ea);
-        tld(tmem + lane_sel + 1 * N + 2 * g0, eb);
-        tld(tmem + lane_sel + 2 * N + 2 * g0, oa);
-        tld(tmem + lane_sel + 3 * N + 2 * g0, ob);
+        for (int c0 = 0; c0 < 64; c0 += 16)
+          tld(tmem + lane_sel + L::T_S1 + f * N + 64 * h + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
-        tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
-        float qr0[8], qi0[8], qr1[8], qi1[8];
+        tc::reg_fence(v);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          PairQ pq;
-          if (i == 0 && g0 == 0) {
-            const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
-            const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
-            pq.r0 = q0.r0; pq.i0 = q0.i0; pq.r1 = q1.r0; pq.i1 = q1.i0;
-          } else {
-            pq = pair_product(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
-                              ob[2 * i], ob[2 * i + 1], special);
+        for (int rt = 0; rt < 2; ++rt) {
+          unsigned char* dst = sm + L::OP + (f * 2 + rt) * L::A2_BYTES;
+#pragma unroll
+          for (int c0 = 0; c0 < 32; c0 += 8) {
+            float v8[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v8[j] = v[2 * (c0 + j) + rt];
+            st8(dst, off_mn(w * HN + 32 * h + c0, y, 128), v8);
           }
-          qr0[i] = pq.r0; qi0[i] = pq.i0; qr1[i] = pq.r1; qi1[i] = pq.i1;
         }
-        st8(dst, off_k(t, 0 * N + 0 * HN + g0, 2 * N), qr0);
-        st8(dst, off_k(t, 0 * N + 1 * HN + g0, 2 * N), qr1);
-        st8(dst, off_k(t, 1 * N + 0 * HN + g0, 2 * N), qi0);
-        st8(dst, off_k(t, 1 * N + 1 * HN + g0, 2 * N), qi1);
       }
-    }
-    if (!sync_for_mma()) break;
+      signal(kRA2);
+      if (ASYNC && has_next) {
+        stage_async(sl1);  // the next tile's rows land while this tile runs
+        cp_async_commit();
+      }
 
-    // ---- Stage 3: Re U = Qr C - Qi S -> cols [0, N); Im U = Qr S + Qi C -> cols [N, 2N).
-    if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+      // ---- Product, per half hh of f_r: thread (q, t) folds g in [32 hh + 8 q, + 8)
+      // of row c = t % HN of window t / HN into half hh of the stage-3 operand
+      // (K-major [128][128], block b4 at column 32 b4).
+      {
+        const bool special = (t % HN) == 0;
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        const int bre = part == 0 ? L::BC : L::BS;   // multiplies Qr
-        const int bim = part == 0 ? L::BNS : L::BC;  // multiplies Qi
+        for (int hh = 0; hh < 2; ++hh) {
+          done(hh == 0 ? kS2a : kS2b);
+          const int g0 = 32 * hh + 8 * q;
+          const uint32_t src = tmem + lane_sel + 256 * hh + 16 * q;
+          float ea[16], eb[16], oa[16], ob[16];
+          tld(src + 0 * HN, ea);
+          tld(src + 1 * HN, eb);
+          tld(src + 2 * HN, oa);
+          tld(src + 3 * HN, ob);
+          tc::tmem_ld_wait();
+          tc::reg_fence(ea); tc::reg_fence(eb); tc::reg_fence(oa); tc::reg_fence(ob);
+          float rp[8], im[8], ip[8], rm[8];
 #pragma unroll
-        for (int src = 0; src < 2; ++src)
-#pragma unroll
-          for (int ks = 0; ks < N / 16; ++ks) {
-            const uint64_t ad = tc::sdesc(sbase + L::OP + src * 2048 + ks * 256, 128, 2 * N * 16);
-            const uint64_t bd = tc::sdesc(sbase + (src == 0 ? bre : bim) + ks * 256, 128, N * 16);
-            tc::mma_f16(tmem + part * N, ad, bd, id, (src | ks) != 0);
+          for (int i = 0; i < 8; ++i) {
+            PairPM o;
+            if (i == 0 && g0 == 0) {  // f_r = 0 and N/2, not folded
+              const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
+              const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
+              o.pr = q0.r0; o.mi = q1.r0; o.pi = q0.i0; o.mr = q1.i0;
+            } else {
+              o = pair_fold(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                            ob[2 * i], ob[2 * i + 1], special);
+            }
+            rp[i] = o.pr; im[i] = o.mi; ip[i] = o.pi; rm[i] = o.mr;
           }
-      }
-      tc::mma_commit(&bar);
-    }
-    wait_mma();
-
-    // ---- Stage 3 -> 4: thread (q, t) moves r in [64 rh, 64 rh + 64) of part q & 1 of row (w, c).
-    {
-      const int part = q & 1, rh = q >> 1, w = t / HN, c = t % HN;
-      float v[64];
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16)
-        tld(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
-      tc::reg_fence(v);
-#pragma unroll
-      for (int r0 = 0; r0 < 64; r0 += 8) {
-        const int m = w * N + 64 * rh + r0;
-        st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
-      }
-    }
-    if (!sync_for_mma()) break;
-
-    // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
-    if (tid == 0) {
-      const uint32_t id = tc::idesc_f16(128, N, 1, 0);
-#pragma unroll
-      for (int rt = 0; rt < 2; ++rt)
-#pragma unroll
-        for (int ks = 0; ks < N / 16; ++ks) {
-          const uint64_t ad = tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128);
-          const uint64_t bd = tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16);
-          tc::mma_f16(tmem + rt * N, ad, bd, id, ks > 0);
+          unsigned char* dst = sm + (hh == 0 ? L::A1 : L::OP);
+          st8(dst, off_k(t, 0 * 32 + 8 * q, L::QH), rp);
+          st8(dst, off_k(t, 1 * 32 + 8 * q, L::QH), im);
+          st8(dst, off_k(t, 2 * 32 + 8 * q, L::QH), ip);
+          st8(dst, off_k(t, 3 * 32 + 8 * q, L::QH), rm);
         }
-      tc::mma_commit(&bar);
-    }
-    wait_mma();
+      }
+      signal(kRQ);
 
-    // ---- Epilogue: thread (q, t) holds shifted columns [64 ch, 64 ch + 64) of
-    // map row t of window w = q & 1 (row index i = t ^ N/2).
-    const int w = q & 1, ch = q >> 1, i = t ^ HN;
-    const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
-    float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
-    float hbest;  // maximum of this thread's half row
-    {
-      float v[64];
+      // ---- Stage 3 -> 4: thread (q, t) moves r in [64 rh, 64 rh + 64) of part q & 1 of row (w, c).
+      done(kS3);
+      {
+        const int part = q & 1, rh = q >> 1, w = t / HN, c = t % HN;
+        float v[64];
 #pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16)
-        tld(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
-      tc::tmem_ld_wait();
-      tc::reg_fence(v);
-      if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
-      float best;
-      int bk;
-      first_max<64>(v, best, bk);
-      int idx = i * N + 64 * ch + bk;
-      if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
-      hbest = best;
-      warp_first_max(best, idx);
-      if (lane == 0) atomicMax(&pk_key[w], peak_key(best, idx));
-      if (a.maps && g0 + w < total) {
-        const int ue = -sc_e[0][w] - sc_e[1][w];
-        float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
+        for (int c0 = 0; c0 < 64; c0 += 16)
+          tld(tmem + lane_sel + part * N + 64 * rh + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+        tc::tmem_ld_wait();
+        tc::reg_fence(v);
 #pragma unroll
-        for (int k = 0; k < 64; ++k) mo[k] = i == 0 ? 0.f : ldexpf(v[k], ue);
+        for (int r0 = 0; r0 < 64; r0 += 8) {
+          const int m = w * N + 64 * rh + r0;
+          st8(sm + L::OP + (m >> 7) * L::A4_BYTES, off_mn(m & 127, part * HN + c, 128), v + r0);
+        }
       }
-    }
-    __syncthreads();
-    {
-      const int pidx = peak_index(pk_key[w]), pi_ = pidx / N, pj = pidx % N;
-      if (ties) {  // the warp's largest half-row maximum outside the peak row (a warp's rows share a window)
-        const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(hbest));
-        if (lane == 0) atomicMax(&sec_key[w], k);
+      signal(kRA4);
+
+      // ---- The next tile's staging while stage 4 runs.
+      if (has_next) {
+        if (ASYNC) cp_async_wait_all();
+        cw_sync();
+        stage_tile(sl1);
+        signal(kRA1);
       }
-      const bool mine = (ties && i == pi_) ||
-                        (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
-      if (__any_sync(0xffffffffu, mine)) {
+
+      // ---- Epilogue: thread (q, t) holds shifted columns [64 ch, 64 ch + 64) of
+      // map row t of window w = q & 1 (row index i = t ^ N/2).
+      done(kS4);
+      const int w = q & 1, ch = q >> 1, i = t ^ HN;
+      const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
+      float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
+      float hbest;  // maximum of this thread's half row
+      {
         float v[64];
 #pragma unroll
         for (int c0 = 0; c0 < 64; c0 += 16)
           tld(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
         tc::tmem_ld_wait();
         tc::reg_fence(v);
-        if (mine) {
-          float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N + s0);
-          if (in_dyn_smem(dst, 64 * 4))
+        if (ch == 0) v[0] = 0.f;  // shifted column 0: no window overlap
+        float best;
+        int bk;
+        first_max<64>(v, best, bk);
+        int idx = i * N + 64 * ch + bk;
+        if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
+        hbest = best;
+        warp_first_max(best, idx);
+        if (lane == 0) atomicMax(&pk_key[w], peak_key(best, idx));
+        if (a.maps && g0 + w < total) {
+          const int ue = -sc_e[sl][0][w] - sc_e[sl][1][w];
+          float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
 #pragma unroll
-            for (int c4 = 0; c4 < 16; ++c4)
-              dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+          for (int k = 0; k < 64; ++k) mo[k] = i == 0 ? 0.f : ldexpf(v[k], ue);
         }
       }
+      cw_sync();
+      {
+        const int pidx = peak_index(pk_key[w]), pi_ = pidx / N, pj = pidx % N;
+        if (ties) {  // the warp's largest half-row maximum outside the peak row (a warp's rows share a window)
+          const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(hbest));
+          if (lane == 0) atomicMax(&sec_key[w], k);
+        }
+        const bool mine = (ties && i == pi_) ||
+                          (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
+        if (__any_sync(0xffffffffu, mine)) {
+          float v[64];
+#pragma unroll
+          for (int c0 = 0; c0 < 64; c0 += 16)
+            tld(tmem + lane_sel + w * N + s0 + c0, *reinterpret_cast<float(*)[16]>(v + c0));
+          tc::tmem_ld_wait();
+          tc::reg_fence(v);
+          if (mine) {
+            float4* dst = reinterpret_cast<float4*>(nbrow + (w * 3 + (i - pi_ + 1)) * N + s0);
+            if (in_dyn_smem(dst, 64 * 4))
+#pragma unroll
+              for (int c4 = 0; c4 < 16; ++c4)
+                dst[c4] = make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]);
+          }
+        }
+      }
+      // The map's TMEM columns are read: the next tile's stage 2 may overwrite them.
+      tc::fence_before_sync();
+      cw_sync();
+      // The near-tie flags in warp 1 while warp 0 fits.
+      if (ties && warp == 1)
+        write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol,
+                                             [&](int ww) { return peak_index(pk_key[ww]); },
+                                             [&](int ww) { return nbrow + (ww * 3 + 1) * N; }));
+      if (tid < W && g0 + tid < total) {
+        const int ww = tid;
+        const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
+        float isp = (float)pi_, jsp = (float)pj;
+        if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
+          const int ue = -sc_e[sl][0][ww] - sc_e[sl][1][ww];
+          const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
+          auto at = [&](int ii, int j) -> float {
+            return (ii == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
+          };
+          subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
+                       at(pi_, pj + 1), isp, jsp);
+        }
+        const CorrSeg& sq = seg_s[win_seg[sl][ww]];
+        const long long gl = win_loc[sl][ww];
+        float* uo = reinterpret_cast<float*>(sq.u);
+        float* vo = reinterpret_cast<float*>(sq.v);
+        if (in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) {
+          if (win_valid[sl][ww]) {
+            uo[gl] = sub_rn(jsp, (float)HN);
+            vo[gl] = sub_rn(isp, (float)HN);
+          } else {
+            uo[gl] = NAN;
+            vo[gl] = NAN;
+          }
+          if (sq.peak_i) sq.peak_i[gl] = pi_;
+          if (sq.peak_j) sq.peak_j[gl] = pj;
+        }
+      }
+      cw_sync();
+      sl = sl1;
+      if (abort_s) break;
     }
-    __syncthreads();
-    // The near-tie flags in warp 1 while warp 0 fits.
-    if (ties && warp == 1)
-      write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return peak_index(pk_key[ww]); },
-                                           [&](int ww) { return nbrow + (ww * 3 + 1) * N; }));
-    if (tid < W && g0 + tid < total) {
-      const int ww = tid;
-      const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
-      float isp = (float)pi_, jsp = (float)pj;
-      if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-        const int ue = -sc_e[0][ww] - sc_e[1][ww];
-        const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
-        auto at = [&](int ii, int j) -> float {
-          return (ii == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
-        };
-        subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
-                     at(pi_, pj + 1), isp, jsp);
-      }
-      const CorrSeg& sq = seg_s[win_seg[sl][ww]];
-      const long long gl = win_loc[sl][ww];
-      float* uo = reinterpret_cast<float*>(sq.u);
-      float* vo = reinterpret_cast<float*>(sq.v);
-      if (in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) {
-      if (win_valid[sl][ww]) {
-        uo[gl] = sub_rn(jsp, (float)HN);
-        vo[gl] = sub_rn(isp, (float)HN);
-      } else {
-        uo[gl] = NAN;
-        vo[gl] = NAN;
-      }
-      if (sq.peak_i) sq.peak_i[gl] = pi_;
-      if (sq.peak_j) sq.peak_j[gl] = pj;
-      }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (abort_s) break;
+    if (ASYNC) cp_async_wait_all();
   }
-  if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_free(tmem, L::TCOLS);
