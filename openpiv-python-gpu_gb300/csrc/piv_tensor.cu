@@ -953,26 +953,32 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 // phases at the same time: tile i + 1 is staged while stage 4 of tile i runs,
 // the map of tile i is searched while stage 1 of tile i + 1 runs, and the
 // product of the first half of stage 2 (f_r columns 0-63) is formed while
-// the second half is computed.
+// the second half is computed. A fit warp runs the near-tie test and the
+// subpixel fits of tile i (from the peak keys and the three map rows around
+// each peak, which the compute warps leave in a buffer of their own) while
+// tile i + 1 is correlated, so the compute warps go from the peak search
+// straight on to the next tile.
 //   TMEM: stage 1 -> columns [256, 512); stage 2 half 0 -> [0, 256), half 1
 //   -> [256, 512); stages 3 and 4 -> [0, 256).
-//   Shared memory (208 KB): constants F (16 KB), C / -S / S (48 KB) and E'
+//   Shared memory (211 KB): constants F (16 KB), C / -S / S (48 KB) and E'
 //   (32 KB); the stage-1 operands (32 KB, then the first half of the stage-3
 //   operand); a 64 KB region for the stage-2 operands, then the second half
-//   of the stage-3 operand, the stage-4 operands and the peak-neighbour rows;
-//   the next tile's 8-bit rows (16 KB).
+//   of the stage-3 operand and the stage-4 operands; the next tile's 8-bit
+//   rows (16 KB); the peak-neighbour rows (3 KB).
 // ---------------------------------------------------------------------------
 struct Tc64 {
   static constexpr int SS = 64, N = 128, HN = 64, W = 2, TCOLS = 512;
-  static constexpr int NCW = 16, NC = 32 * NCW, NT = NC + 32;  // compute warps, their threads, all threads
+  // Compute warps, their threads, all threads (with the MMA warp and the fit warp).
+  static constexpr int NCW = 16, NC = 32 * NCW, NT = NC + 64;
   static constexpr int NB3 = N * HN * 2;
   static constexpr int B1 = 0;                      // F [N][SS] K-major
   static constexpr int B3 = B1 + N * SS * 2;        // stage 3: blocks C, -S, S (/ N) [N][HN] K-major
   static constexpr int B4 = B3 + 3 * NB3;           // [N][N] K-major, K = (part, c)
   static constexpr int A1 = B4 + N * N * 2;         // 2 x [128][SS] K-major; then stage-3 operand half 0
-  static constexpr int OP = A1 + 2 * 128 * SS * 2;  // 64 KB operand region (then the neighbour rows)
+  static constexpr int OP = A1 + 2 * 128 * SS * 2;  // 64 KB operand region
   static constexpr int STG = OP + 65536;            // next tile's 8-bit rows [frame][w][y][64 B], chunks swizzled
-  static constexpr int END = STG + 2 * W * SS * SS;
+  static constexpr int NBR = STG + 2 * W * SS * SS; // [W][3][N] floats: map rows pi-1, pi, pi+1 (natural columns)
+  static constexpr int END = NBR + W * 3 * N * 4;
   static constexpr int A1_BYTES = 128 * SS * 2;     // per frame, K-major [128][SS]
   static constexpr int A2_BYTES = 128 * SS * 2;     // per (frame, tile), MN-major [128][SS]
   static constexpr int A4_BYTES = 128 * N * 2;      // per tile, MN-major [128][N]
@@ -986,8 +992,9 @@ PIV_D int stg64_chunk(int t, int k) { return k ^ ((t >> 1) & 3); }
 
 // ASYNC: 8-bit frames whose window rows start on 16-byte boundaries; the next
 // tile's rows are copied with cp.async while the current tile runs.
-// Registers: the 17 warps are spread over the SM's four sub-partitions (16K
-// registers each), five on the first, so a thread may hold at most 96.
+// Registers: the 18 warps are spread over the SM's four sub-partitions (16K
+// registers each), five on each of the first two, so a thread may hold at
+// most 96.
 template <bool ASYNC>
 __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   using L = Tc64;
@@ -996,21 +1003,28 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   // Completion of each product (committed by the MMA warp) and readiness of
   // each operand (one arrival per compute warp). Each completes once per tile.
   enum { kS1, kS2a, kS2b, kS3, kS4, kNDone };
-  enum { kRA1, kRA2, kRQ, kRA4, kNReady };
+  enum { kRA1, kRA2, kRQa, kRQ, kRA4, kNReady };
   __shared__ uint64_t done_bar[kNDone], ready_bar[kNReady];
+  // The neighbour rows of a tile are written (compute warps) / have been
+  // read by its fits (MMA warp). Each completes once per tile.
+  __shared__ uint64_t nbr_full, nbr_empty;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
   __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
-  // Per tile slot (three: the tile being correlated, the next one, whose rows
-  // are in flight, and the one after, whose corners are being computed).
-  __shared__ int sc_e[3][2][W];
-  __shared__ long long win_base[3][W];
-  __shared__ int win_valid[3][W];
-  __shared__ long long win_loc[3][W];  // window index within its segment
-  __shared__ int win_seg[3][W];
+  // Per tile slot (four: the tile whose fits are pending, the tile being
+  // correlated, the next one, whose rows are in flight, and the one after,
+  // whose corners are being computed); slot = local tile count % 4.
+  __shared__ int sc_e[4][2][W];
+  __shared__ long long win_base[4][W];
+  __shared__ int win_valid[4][W];
+  __shared__ long long win_loc[4][W];  // window index within its segment
+  __shared__ int win_seg[4][W];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
-  __shared__ unsigned long long pk_key[W];  // per window: the running first maximum (peak_key)
-  __shared__ unsigned sec_key[W];           // per window: key of the largest half-row maximum outside the peak row
+  // Per window, for the current tile and the one whose fits are pending
+  // (local tile count % 2): the running first maximum (peak_key) and the key
+  // of the largest half-row maximum outside the peak row.
+  __shared__ unsigned long long pk_key[2][W];
+  __shared__ unsigned sec_key[2][W];
 
   const int tid = threadIdx.x;
   const int q = tid >> 7, t = tid & 127;
@@ -1028,6 +1042,8 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   if (tid == 0) {
     for (int k = 0; k < kNDone; ++k) tc::mbar_init(&done_bar[k], 1);
     for (int k = 0; k < kNReady; ++k) tc::mbar_init(&ready_bar[k], L::NCW);
+    tc::mbar_init(&nbr_full, 1);
+    tc::mbar_init(&nbr_empty, 1);
     abort_s = 0;
   }
   __syncthreads();
@@ -1067,12 +1083,107 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   const long long total = a.n_segs > 0 ? a.seg_windows : (long long)a.n_pairs * a.m * a.n;
   const int n_tiles = (int)((total + W - 1) / W);
   const int first = blockIdx.x, stride = gridDim.x;
+  const bool ties = any_tie_output(seg_s, n_seg);
+  float* nbrow = reinterpret_cast<float*>(sm + L::NBR);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
 
+  // Corners, validity and segment of window wi of tile tl, into slot sl.
+  auto window_setup = [&](int tl, int sl, int wi) {
+    const long long g = (long long)tl * W + wi;
+    int ok = tl < n_tiles && g < total;
+    long long base = 0, loc = 0;
+    int sg = 0;
+    if (ok) {
+      while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
+      const CorrSeg& sq = seg_s[sg];
+      loc = g - sq.win0;
+      // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
+      const int li = (int)loc, nw = sq.m * sq.n;
+      const int pair = li / nw, k = li - pair * nw;
+      const int wr = k / sq.n, wc = k - wr * sq.n;
+      if (sq.win_mask) ok = sq.win_mask[k] == 0;
+      base = pair * (long long)sq.height * sq.width + (long long)(wr * sq.spacing + sq.y_offset) * sq.width +
+             wc * sq.spacing + sq.x_offset;
+      if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * sq.width + SS <=
+                                            (long long)sq.n_pairs * sq.height * sq.width))
+        ok = 0;
+    }
+    win_valid[sl][wi] = ok;
+    win_base[sl][wi] = base;
+    win_loc[sl][wi] = loc;
+    win_seg[sl][wi] = sg;
+  };
+  uint32_t ph_full = 0u;
+  // Near-tie flags and subpixel fits of tile `tl` (local tile count `it`), run
+  // by the fit warp: every lane waits for the tile's neighbour rows, the warp
+  // runs the near-tie test, lanes < W fit one window each and set up the
+  // windows of tile tl + 3 strides, then lane 0 hands the rows back. False
+  // when the wait gave up.
+  auto fit_tile = [&](int tl, int it) -> bool {
+    const bool got = __all_sync(0xffffffffu, tc::mbar_wait_bounded(&nbr_full, ph_full, kMaxPolls));
+    ph_full ^= 1u;
+    if (!got) {
+      if (lane == 0) {
+        abort_s = 1;
+        atomicExch(status, PIV_E_TIMEOUT);
+      }
+      return false;
+    }
+    const int sl = it & 3, kb = it & 1;
+    const long long g0 = (long long)tl * W;
+    const bool mine = lane < W && g0 + lane < total;
+    const CorrSeg& sq = seg_s[win_seg[sl][mine ? lane : 0]];
+    const long long gl = win_loc[sl][mine ? lane : 0];
+    const bool gl_ok = mine && in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n);
+    if (ties) {
+      const bool tie = tile_near_ties<N, W>(lane, sec_key[kb], a.tie_tol,
+                                            [&](int ww) { return peak_index(pk_key[kb][ww]); },
+                                            [&](int ww) { return nbrow + (ww * 3 + 1) * N; }) &&
+                       mine && win_valid[sl][lane];
+      if (gl_ok) {
+        if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
+        if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
+      }
+    }
+    if (gl_ok) {
+      const int ww = lane;
+      const int pidx = peak_index(pk_key[kb][ww]), pi_ = pidx / N, pj = pidx % N;
+      float isp = (float)pi_, jsp = (float)pj;
+      if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
+        const int ue = -sc_e[sl][0][ww] - sc_e[sl][1][ww];
+        const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
+        auto at = [&](int ii, int j) -> float {
+          return (ii == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
+        };
+        subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
+                     at(pi_, pj + 1), isp, jsp);
+      }
+      float* uo = reinterpret_cast<float*>(sq.u);
+      float* vo = reinterpret_cast<float*>(sq.v);
+      if (win_valid[sl][ww]) {
+        uo[gl] = sub_rn(jsp, (float)HN);
+        vo[gl] = sub_rn(isp, (float)HN);
+      } else {
+        uo[gl] = NAN;
+        vo[gl] = NAN;
+      }
+      if (sq.peak_i) sq.peak_i[gl] = pi_;
+      if (sq.peak_j) sq.peak_j[gl] = pj;
+    }
+    // The corners of the tile three strides on, into this tile's slot's
+    // predecessor (tile it - 1, whose fits are done): the compute warps use
+    // them from tile it + 2 on, after waiting for these fits in the epilogue
+    // of tile it + 1.
+    if (lane < W) window_setup(tl + 3 * stride, (it + 3) & 3, lane);
+    __syncwarp();
+    if (lane == 0) tc::mbar_arrive(&nbr_empty);
+    return true;
+  };
   if (warp == L::NCW) {
-    // ---- MMA warp: lane 0 waits for each operand, issues the product and
-    // commits it; a wait that gives up stops the warp (the compute warps'
-    // own waits then give up as well).
-    uint32_t ph[kNReady] = {0u, 0u, 0u, 0u};
+    // ---- MMA warp: lane 0 waits for each operand, then the converged warp
+    // issues the product (one elected lane; the descriptor arithmetic stays
+    // on the uniform datapath) and commits it; a wait that gives up stops
+    // the warp (the compute warps' own waits then give up as well).
+    uint32_t ph[kNReady] = {0u, 0u, 0u, 0u, 0u};
     auto ready = [&](int k) -> bool {
       bool ok = true;
       if (lane == 0) {
@@ -1089,16 +1200,15 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
     };
     // Stage 1: T = a F^T per frame -> TMEM cols [T_S1 + f N, + N).
     auto stage1 = [&]() {
-      if (lane == 0) {
-        const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+      const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
-        for (int f = 0; f < 2; ++f)
+      for (int f = 0; f < 2; ++f)
 #pragma unroll
-          for (int ks = 0; ks < SS / 16; ++ks)
-            tc::mma_f16(tmem + L::T_S1 + f * N, tc::sdesc(sbase + L::A1 + f * L::A1_BYTES + ks * 256, 128, SS * 16),
-                        tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16), id, ks > 0);
-        tc::mma_commit(&done_bar[kS1]);
-      }
+        for (int ks = 0; ks < SS / 16; ++ks)
+          tc::mma_f16<true>(tmem + L::T_S1 + f * N,
+                            tc::sdesc(sbase + L::A1 + f * L::A1_BYTES + ks * 256, 128, SS * 16),
+                            tc::sdesc(sbase + L::B1 + ks * 256, 128, SS * 16), id, ks > 0);
+      tc::mma_commit<true>(&done_bar[kS1]);
       __syncwarp();
     };
     if (first < n_tiles && ready(kRA1)) {
@@ -1107,7 +1217,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
         // Stage 2 in two halves of f_r: X = T^T F^T, packed columns [64 h, 64 h + 64)
         // of spectrum (rt, f) -> TMEM cols [256 h + (2 rt + f) 64, + 64).
         if (!ready(kRA2)) break;
-        if (lane == 0) {
+        {
           const uint32_t id = tc::idesc_f16(128, HN, 1, 0);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -1117,45 +1227,56 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
               for (int f = 0; f < 2; ++f)
 #pragma unroll
                 for (int ks = 0; ks < SS / 16; ++ks)
-                  tc::mma_f16(tmem + 256 * h + (rt * 2 + f) * HN,
-                              tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128),
-                              tc::sdesc(sbase + L::B1 + h * 8 * SS * 16 + ks * 256, 128, SS * 16), id, ks > 0);
-            tc::mma_commit(&done_bar[h == 0 ? kS2a : kS2b]);
+                  tc::mma_f16<true>(
+                      tmem + 256 * h + (rt * 2 + f) * HN,
+                      tc::sdesc(sbase + L::OP + (f * 2 + rt) * L::A2_BYTES + ks * 32 * 128, 128 * 16, 128),
+                      tc::sdesc(sbase + L::B1 + h * 8 * SS * 16 + ks * 256, 128, SS * 16), id, ks > 0);
+            tc::mma_commit<true>(&done_bar[h == 0 ? kS2a : kS2b]);
           }
         }
         __syncwarp();
         // Stage 3: Re U = [Re P | Im M] [C; -S] -> cols [0, N); Im U = [Im P | Re M] [C; S]
         // -> cols [N, 2N). Block b4 of the operand (Re P, Im M, Im P, Re M), g in
-        // [16 s, 16 s + 16), sits in half s / 2 at column 32 b4 + 16 (s % 2).
-        if (!ready(kRQ)) break;
-        if (lane == 0) {
+        // [16 s, 16 s + 16), sits in half s / 2 at column 32 b4 + 16 (s % 2). The
+        // K steps of operand half hh (g in [32 hh, 32 hh + 32)) go as soon as the
+        // compute warps have written that half.
+        {
           const uint32_t id = tc::idesc_f16(128, N, 0, 0);
+          bool ok = true;
 #pragma unroll
-          for (int part = 0; part < 2; ++part)
+          for (int hh = 0; hh < 2 && ok; ++hh) {
+            ok = ready(hh == 0 ? kRQa : kRQ);
+            if (!ok) break;
 #pragma unroll
-            for (int kb = 0; kb < 2; ++kb)
+            for (int part = 0; part < 2; ++part)
 #pragma unroll
-              for (int s = 0; s < HN / 16; ++s) {
-                const int b4 = 2 * part + kb;
-                const uint32_t ab = (s >> 1) == 0 ? L::A1 : L::OP;
-                tc::mma_f16(tmem + part * N, tc::sdesc(sbase + ab + (32 * b4 + 16 * (s & 1)) * 16, 128, L::QH * 16),
-                            tc::sdesc(sbase + L::B3 + (kb == 0 ? 0 : 1 + part) * L::NB3 + s * 256, 128, HN * 16), id,
-                            (kb | s) != 0);
-              }
-          tc::mma_commit(&done_bar[kS3]);
+              for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+                for (int s = 2 * hh; s < 2 * hh + 2; ++s) {
+                  const int b4 = 2 * part + kb;
+                  tc::mma_f16<true>(
+                      tmem + part * N,
+                      tc::sdesc(sbase + (hh == 0 ? L::A1 : L::OP) + (32 * b4 + 16 * (s & 1)) * 16, 128, L::QH * 16),
+                      tc::sdesc(sbase + L::B3 + (kb == 0 ? 0 : 1 + part) * L::NB3 + s * 256, 128, HN * 16), id,
+                      (kb | s) != 0);
+                }
+          }
+          if (!ok) break;
+          tc::mma_commit<true>(&done_bar[kS3]);
         }
         __syncwarp();
         // Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
         if (!ready(kRA4)) break;
-        if (lane == 0) {
+        {
           const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
           for (int rt = 0; rt < 2; ++rt)
 #pragma unroll
             for (int ks = 0; ks < N / 16; ++ks)
-              tc::mma_f16(tmem + rt * N, tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128),
-                          tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16), id, ks > 0);
-          tc::mma_commit(&done_bar[kS4]);
+              tc::mma_f16<true>(tmem + rt * N,
+                                tc::sdesc(sbase + L::OP + rt * L::A4_BYTES + ks * 32 * 128, 128 * 16, 128),
+                                tc::sdesc(sbase + L::B4 + ks * 256, 128, N * 16), id, ks > 0);
+          tc::mma_commit<true>(&done_bar[kS4]);
         }
         __syncwarp();
         if (tile + stride < n_tiles) {
@@ -1164,6 +1285,11 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
         }
       }
     }
+  } else if (warp == L::NCW + 1) {
+    // ---- Fit warp: the near-tie test and the subpixel fits of each tile,
+    // once the compute warps have left its neighbour rows and peak keys.
+    for (int tile = first, it = 0; tile < n_tiles; tile += stride, ++it)
+      if (!fit_tile(tile, it)) break;
   } else {
     // ---- Compute warps (512 threads).
     // TMEM loads of the CTA's allocation (checked build: columns inside it).
@@ -1171,7 +1297,25 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       if (in_bounds(((addr - tmem) & 0xffffu) + 16 <= (uint32_t)L::TCOLS)) tc::tmem_ld16(addr, v);
     };
     auto cw_sync = []() { asm volatile("bar.sync 1, %0;" ::"n"(L::NC) : "memory"); };
+    // Barrier of the compute warps that also ORs `p` over them: every thread
+    // gets the same answer (a flag read by each thread separately could
+    // change between the reads when the MMA warp sets it).
+    auto cw_sync_or = [](bool p) -> bool {
+      int r;
+      asm volatile(
+          "{\n"
+          ".reg .pred a, b;\n"
+          "setp.ne.s32 a, %1, 0;\n"
+          "bar.red.or.pred b, 1, %2, a;\n"
+          "selp.s32 %0, 1, 0, b;\n"
+          "}\n"
+          : "=r"(r)
+          : "r"((int)p), "n"(L::NC)
+          : "memory");
+      return r != 0;
+    };
     uint32_t ph[kNDone] = {0u, 0u, 0u, 0u, 0u};
+    uint32_t ph_empty = 0u;
     // Every thread waits for the product itself; a wait that gives up sets
     // abort_s, which all threads read after the tile's last barrier.
     auto done = [&](int k) {
@@ -1189,31 +1333,6 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&ready_bar[k]);
-    };
-    auto window_setup = [&](int tl, int sl) {
-      const long long g = (long long)tl * W + tid;
-      int ok = tl < n_tiles && g < total;
-      long long base = 0, loc = 0;
-      int sg = 0;
-      if (ok) {
-        while (sg + 1 < n_seg && g >= seg_s[sg + 1].win0) ++sg;
-        const CorrSeg& sq = seg_s[sg];
-        loc = g - sq.win0;
-        // 32-bit quotients: a segment holds fewer than 2^31 windows (checked at launch).
-        const int li = (int)loc, nw = sq.m * sq.n;
-        const int pair = li / nw, k = li - pair * nw;
-        const int wr = k / sq.n, wc = k - wr * sq.n;
-        if (sq.win_mask) ok = sq.win_mask[k] == 0;
-        base = pair * (long long)sq.height * sq.width + (long long)(wr * sq.spacing + sq.y_offset) * sq.width +
-               wc * sq.spacing + sq.x_offset;
-        if (ok && !in_bounds(base >= 0 && base + (long long)(SS - 1) * sq.width + SS <=
-                                              (long long)sq.n_pairs * sq.height * sq.width))
-          ok = 0;
-      }
-      win_valid[sl][tid] = ok;
-      win_base[sl][tid] = base;
-      win_loc[sl][tid] = loc;
-      win_seg[sl][tid] = sg;
     };
     // Thread (q, t) copies chunks 2h, 2h + 1 of row t of frame f: the bytes it
     // stages itself; rows of invalid windows are zero-filled (no global read).
@@ -1282,24 +1401,10 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       for (int x = 0; x < 32; x += 8) st8(sm + L::A1 + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     };
 
-    const bool ties = any_tie_output(seg_s, n_seg);
-    // Near-tie flag of window `lane` of the current tile (lanes < W of the
-    // calling warp; tile_near_ties's result) to the window's outputs.
-    int cur_sl = 0;
-    long long cur_g0 = 0;
-    auto write_near_ties = [&](bool tie) {
-      if (lane >= W || cur_g0 + lane >= total) return;
-      const CorrSeg& sq = seg_s[win_seg[cur_sl][lane]];
-      const long long gl = win_loc[cur_sl][lane];
-      tie = tie && win_valid[cur_sl][lane];
-      if (!in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) return;
-      if (sq.near_tie) sq.near_tie[gl] = tie ? 1 : 0;
-      if (tie && sq.tie_count) atomicAdd(sq.tie_count, 1);
-    };
-
     if (tid < W) {
-      window_setup(first, 0);
-      window_setup(first + stride, 1);
+      window_setup(first, 0, tid);
+      window_setup(first + stride, 1, tid);
+      window_setup(first + 2 * stride, 2, tid);
     }
     cw_sync();
     if (first < n_tiles) {
@@ -1313,20 +1418,17 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       signal(kRA1);
     }
 
-    int sl = 0;
-    for (int tile = first; tile < n_tiles; tile += stride) {
+    int it = 0;  // local tile count
+    for (int tile = first; tile < n_tiles; tile += stride, ++it) {
       const long long g0 = (long long)tile * W;
-      const int sl1 = sl == 2 ? 0 : sl + 1, sl2 = sl1 == 2 ? 0 : sl1 + 1;
+      const int sl = it & 3, sl1 = (it + 1) & 3, kb = it & 1;
       const bool has_next = tile + stride < n_tiles;
-      // The previous tile's epilogue has finished with the peak and near-tie
-      // keys and with slot sl2 (its own slot).
+      // The fits of tile it - 2 (same keys) have finished: this thread waited
+      // for them before writing the neighbour rows of tile it - 1.
       if (tid < W) {
-        pk_key[tid] = 0ull;
-        sec_key[tid] = kKeyNegInf;
-        window_setup(tile + 2 * stride, sl2);
+        pk_key[kb][tid] = 0ull;
+        sec_key[kb][tid] = kKeyNegInf;
       }
-      cur_sl = sl;
-      cur_g0 = g0;
 
       // ---- Stage 1 -> 2: thread (q, t) moves packed columns [64 h, 64 h + 64) of frame f.
       done(kS1);
@@ -1392,9 +1494,9 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
           st8(dst, off_k(t, 1 * 32 + 8 * q, L::QH), im);
           st8(dst, off_k(t, 2 * 32 + 8 * q, L::QH), ip);
           st8(dst, off_k(t, 3 * 32 + 8 * q, L::QH), rm);
+          signal(hh == 0 ? kRQa : kRQ);
         }
       }
-      signal(kRQ);
 
       // ---- Stage 3 -> 4: thread (q, t) moves r in [64 rh, 64 rh + 64) of part q & 1 of row (w, c).
       done(kS3);
@@ -1427,7 +1529,6 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       done(kS4);
       const int w = q & 1, ch = q >> 1, i = t ^ HN;
       const int s0 = ch == 0 ? HN : 0;  // natural column of shifted column 64 ch
-      float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
       float hbest;  // maximum of this thread's half row
       {
         float v[64];
@@ -1444,7 +1545,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
         if (i == 0) { best = 0.f; idx = 64 * ch; }  // shifted row 0: no window overlap
         hbest = best;
         warp_first_max(best, idx);
-        if (lane == 0) atomicMax(&pk_key[w], peak_key(best, idx));
+        if (lane == 0) atomicMax(&pk_key[kb][w], peak_key(best, idx));
         if (a.maps && g0 + w < total) {
           const int ue = -sc_e[sl][0][w] - sc_e[sl][1][w];
           float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N + 64 * ch;
@@ -1454,13 +1555,22 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       }
       cw_sync();
       {
-        const int pidx = peak_index(pk_key[w]), pi_ = pidx / N, pj = pidx % N;
+        const int pidx = peak_index(pk_key[kb][w]), pi_ = pidx / N, pj = pidx % N;
         if (ties) {  // the warp's largest half-row maximum outside the peak row (a warp's rows share a window)
           const unsigned k = __reduce_max_sync(0xffffffffu, i == pi_ ? kKeyNegInf : fkey(hbest));
-          if (lane == 0) atomicMax(&sec_key[w], k);
+          if (lane == 0) atomicMax(&sec_key[kb][w], k);
         }
         const bool mine = (ties && i == pi_) ||
                           (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
+        // The MMA warp has run the fits of the previous tile (it read the rows).
+        if (it > 0) {
+          const bool ok = tc::mbar_wait_bounded(&nbr_empty, ph_empty, kMaxPolls);
+          ph_empty ^= 1u;
+          if (!ok) {
+            abort_s = 1;
+            atomicExch(status, PIV_E_TIMEOUT);
+          }
+        }
         if (__any_sync(0xffffffffu, mine)) {
           float v[64];
 #pragma unroll
@@ -1477,46 +1587,13 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
           }
         }
       }
-      // The map's TMEM columns are read: the next tile's stage 2 may overwrite them.
+      // The map's TMEM columns are read (the next tile's stage 2 may overwrite
+      // them) and the neighbour rows written: they go to the MMA warp, which
+      // runs the fits while this tile's successor is correlated.
       tc::fence_before_sync();
-      cw_sync();
-      // The near-tie flags in warp 1 while warp 0 fits.
-      if (ties && warp == 1)
-        write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol,
-                                             [&](int ww) { return peak_index(pk_key[ww]); },
-                                             [&](int ww) { return nbrow + (ww * 3 + 1) * N; }));
-      if (tid < W && g0 + tid < total) {
-        const int ww = tid;
-        const int pidx = peak_index(pk_key[ww]), pi_ = pidx / N, pj = pidx % N;
-        float isp = (float)pi_, jsp = (float)pj;
-        if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-          const int ue = -sc_e[sl][0][ww] - sc_e[sl][1][ww];
-          const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
-          auto at = [&](int ii, int j) -> float {
-            return (ii == 0 || j == 0) ? 0.f : nbrow[(ww * 3 + (ii - pi_ + 1)) * N + (j ^ HN)] * s1 * s2;
-          };
-          subpixel_fit(a.subpixel, pi_, pj, at(pi_, pj), at(pi_ - 1, pj), at(pi_ + 1, pj), at(pi_, pj - 1),
-                       at(pi_, pj + 1), isp, jsp);
-        }
-        const CorrSeg& sq = seg_s[win_seg[sl][ww]];
-        const long long gl = win_loc[sl][ww];
-        float* uo = reinterpret_cast<float*>(sq.u);
-        float* vo = reinterpret_cast<float*>(sq.v);
-        if (in_bounds(gl >= 0 && gl < (long long)sq.n_pairs * sq.m * sq.n)) {
-          if (win_valid[sl][ww]) {
-            uo[gl] = sub_rn(jsp, (float)HN);
-            vo[gl] = sub_rn(isp, (float)HN);
-          } else {
-            uo[gl] = NAN;
-            vo[gl] = NAN;
-          }
-          if (sq.peak_i) sq.peak_i[gl] = pi_;
-          if (sq.peak_j) sq.peak_j[gl] = pj;
-        }
-      }
-      cw_sync();
-      sl = sl1;
-      if (abort_s) break;
+      const bool stop = cw_sync_or(abort_s != 0);
+      if (tid == 0) tc::mbar_arrive(&nbr_full);
+      if (stop) break;
     }
     if (ASYNC) cp_async_wait_all();
   }
