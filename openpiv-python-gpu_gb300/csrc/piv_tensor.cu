@@ -17,8 +17,9 @@
 //   product  Q(f_r, c) = conj(A) B for c = 1 .. N/2-1 and all f_r; row c = 0
 //            packs the two real-input columns: Q = conj(A0) B0 + i conj(AN) BN.
 //            Each frequency pair (g, N - g) is folded into P = Q(g) + Q(N-g)
-//            and M = Q(g) - Q(N-g), so that the inverse along f_r needs only
-//            cosines and sines of g = 0 .. N/2-1:
+//            and M = Q(g) - Q(N-g) (stored halved, the 2 in the constants),
+//            so that the inverse along f_r needs only cosines and sines of
+//            g = 0 .. N/2-1:
 //   stage 3  U = Q E / N rows (w, c), two products:  Re U = [Re P | Im M] [C; -S],
 //            Im U = [Im P | Re M] [C; S], K = N each, cols r
 //   stage 4  c = U E' / N rows (w, r),             K = (Re|Im, c),   cols s
@@ -272,6 +273,13 @@ PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uin
   }
 }
 
+// Byte k of w as a float, exactly, without an integer-to-float conversion
+// (a quarter-rate instruction): the byte becomes the low mantissa bits of
+// 2^23 (0x4B0000bb = 2^23 + b), and 2^23 is subtracted.
+PIV_D float u8_to_float(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
+}
+
 // 2^e for |e| <= 126.
 PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
 
@@ -328,36 +336,42 @@ PIV_D PairQ pair_product(float ar, float ai, float orr, float oi, float br, floa
   return q;
 }
 
-// The folded pair: P = Q(g) + Q(N - g) and M = Q(g) - Q(N - g) of
-// pair_product's outputs. Row c = 0 in closed form (no cancellation of the
-// packed halves): Re P = 2 Re conj(E_a) E_b, Im P = 2 Re conj(O_a) O_b,
-// Re M = -2 Im conj(O_a) O_b, Im M = 2 Im conj(E_a) E_b. Every part is at
-// most |A| |B| + |A'| |B'|, twice the bound of one spectrum product.
+// Half the folded pair: P / 2 and M / 2 with P = Q(g) + Q(N - g) and
+// M = Q(g) - Q(N - g) of pair_product's outputs. With u = conj(E_a) E_b +
+// conj(O_a) O_b and v = conj(E_a) O_b - conj(O_a) E_b, Q(g) = u + i v and
+// Q(N - g) = conj(u) + i conj(v), so P / 2 = Re u + i Re v and
+// M / 2 = -Im v + i Im u: eight two-term products, no cancellation of the
+// sums A = E_a + i O_a that pair_product forms. Row c = 0 (`special`, the two
+// packed real-input columns): P / 2 = Re conj(E_a) E_b + i Re conj(O_a) O_b,
+// M / 2 = -Im conj(O_a) O_b + i Im conj(E_a) E_b. Every part is at most
+// (|A| |B| + |A'| |B'|) / 2, the bound of one spectrum product.
 struct PairPM {
   float pr, pi, mr, mi;
 };
-PIV_D PairPM pair_fold(float ar, float ai, float orr, float oi, float br, float bi, float pr, float pi,
-                       bool special) {
-  const PairQ q = pair_product(ar, ai, orr, oi, br, bi, pr, pi, special);
-  const float re1 = fmaf(ar, br, ai * bi), im1 = fmaf(ar, bi, -ai * br);     // conj(E_a) E_b
-  const float re2 = fmaf(orr, pr, oi * pi), im2 = fmaf(orr, pi, -oi * pr);   // conj(O_a) O_b
+PIV_D PairPM pair_fold_half(float ar, float ai, float orr, float oi, float br, float bi, float pr, float pi,
+                            bool special) {
+  const float t1 = fmaf(ar, br, ai * bi), t3 = fmaf(ar, bi, -ai * br);     // conj(E_a) E_b
+  const float t2 = fmaf(orr, pr, oi * pi), t4 = fmaf(orr, pi, -oi * pr);   // conj(O_a) O_b
+  const float t5 = fmaf(ar, pr, ai * pi), t7 = fmaf(ar, pi, -ai * pr);     // conj(E_a) O_b
+  const float t6 = fmaf(orr, br, oi * bi), t8 = fmaf(orr, bi, -oi * br);   // conj(O_a) E_b
   PairPM o;
-  o.pr = special ? 2.f * re1 : q.r0 + q.r1;
-  o.pi = special ? 2.f * re2 : q.i0 + q.i1;
-  o.mr = special ? -2.f * im2 : q.r0 - q.r1;
-  o.mi = special ? 2.f * im1 : q.i0 - q.i1;
+  o.pr = special ? t1 : t1 + t2;
+  o.pi = special ? t2 : t5 - t6;
+  o.mr = special ? -t4 : t8 - t7;
+  o.mi = special ? t3 : t3 + t4;
   return o;
 }
 
-// Stage-3 operand columns (K = 2N) of one row: [Re P | Im M | Im P | Re M],
+// Stage-3 operand columns (K = 2N) of one row: [Re P | Im M | Im P | Re M] / 2,
 // N/2 columns each; at g = 0 the slots hold Re Q(0), Re Q(N/2), Im Q(0) and
-// Im Q(N/2) (the unpaired frequencies), whose inverse weights are 1 and
-// (-1)^r. Value of block k (0: C, 1: -S, 2: S) at output r, column g, for
-// cos / sin of 2 pi g r / N scaled by s.
+// Im Q(N/2) (the unpaired frequencies), also halved, whose inverse weights
+// are 1 and (-1)^r. Value of block k (0: C, 1: -S, 2: S) at output r, column
+// g, for cos / sin of 2 pi g r / N scaled by s; the factor 2 restores the
+// halved operand (exact: powers of two).
 PIV_D float stage3_weight(int blk, int r, int g, float cs, float sn, float s) {
-  if (blk == 0) return cs;
-  if (g == 0) return (r & 1) ? -s : s;
-  return blk == 1 ? -sn : sn;
+  if (blk == 0) return 2.f * cs;
+  if (g == 0) return (r & 1) ? -2.f * s : 2.f * s;
+  return blk == 1 ? -2.f * sn : 2.f * sn;
 }
 
 // Whether any segment asks for near-tie flags or counts.
@@ -677,8 +691,8 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     wait_mma();
 
     // ---- Product: thread (w, c) forms row c of the stage-3 operand,
-    // [Re P | Im M | Im P | Re M] of the folded pairs (g, N - g); at g = 0
-    // Re Q(0), Re Q(N/2), Im Q(0), Im Q(N/2).
+    // [Re P | Im M | Im P | Re M] / 2 of the folded pairs (g, N - g); at g = 0
+    // Re Q(0), Re Q(N/2), Im Q(0), Im Q(N/2), halved.
     {
       const bool special = (t % HN) == 0;
       unsigned char* dst = sm + L::OP;
@@ -697,13 +711,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         for (int i = 0; i < 8; ++i) {
           PairPM o;
           if (g0 + i == 0) {
-            // f_r = 0 and f_r = N/2: real spectra R[0] and R[1], not folded.
+            // f_r = 0 and f_r = N/2: real spectra R[0] and R[1], not folded (halved).
             const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
             const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
-            o.pr = q0.r0; o.mi = q1.r0; o.pi = q0.i0; o.mr = q1.i0;
+            o.pr = 0.5f * q0.r0; o.mi = 0.5f * q1.r0; o.pi = 0.5f * q0.i0; o.mr = 0.5f * q1.i0;
           } else {
-            o = pair_fold(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
-                          ob[2 * i], ob[2 * i + 1], special);
+            o = pair_fold_half(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                               ob[2 * i], ob[2 * i + 1], special);
           }
           rp[i] = o.pr * oscale; im[i] = o.mi * oscale; ip[i] = o.pi * oscale; rm[i] = o.mr * oscale;
         }
@@ -1360,7 +1374,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
           const uint4 q4 = *reinterpret_cast<const uint4*>(row + 16 * stg64_chunk(t, 2 * h + c));
           const uint32_t wds[4] = {q4.x, q4.y, q4.z, q4.w};
 #pragma unroll
-          for (int k = 0; k < 16; ++k) r[16 * c + k] = (float)((wds[k >> 2] >> (8 * (k & 3))) & 0xffu);
+          for (int k = 0; k < 16; ++k) r[16 * c + k] = u8_to_float(wds[k >> 2], k & 3);
         }
       } else {
         const CorrSeg& sq = seg_s[win_seg[sl][w]];
@@ -1479,13 +1493,13 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             PairPM o;
-            if (i == 0 && g0 == 0) {  // f_r = 0 and N/2, not folded
+            if (i == 0 && g0 == 0) {  // f_r = 0 and N/2, not folded (halved)
               const PairQ q0 = pair_product(ea[0], 0.f, oa[0], 0.f, eb[0], 0.f, ob[0], 0.f, special);
               const PairQ q1 = pair_product(ea[1], 0.f, oa[1], 0.f, eb[1], 0.f, ob[1], 0.f, special);
-              o.pr = q0.r0; o.mi = q1.r0; o.pi = q0.i0; o.mr = q1.i0;
+              o.pr = 0.5f * q0.r0; o.mi = 0.5f * q1.r0; o.pi = 0.5f * q0.i0; o.mr = 0.5f * q1.i0;
             } else {
-              o = pair_fold(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
-                            ob[2 * i], ob[2 * i + 1], special);
+              o = pair_fold_half(ea[2 * i], ea[2 * i + 1], oa[2 * i], oa[2 * i + 1], eb[2 * i], eb[2 * i + 1],
+                                 ob[2 * i], ob[2 * i + 1], special);
             }
             rp[i] = o.pr; im[i] = o.mi; ip[i] = o.pi; rm[i] = o.mr;
           }
