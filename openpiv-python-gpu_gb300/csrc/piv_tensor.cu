@@ -1024,11 +1024,12 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   __shared__ uint64_t nbr_full, nbr_empty;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
-  __shared__ float red[2][W][4];     // per frame and window: partial sums of the four row groups
+  __shared__ float red[2][2][W][4];  // sums, then absolute deviations: per frame and window, the four row groups' partials
   // Per tile slot (four: the tile whose fits are pending, the tile being
   // correlated, the next one, whose rows are in flight, and the one after,
   // whose corners are being computed); slot = local tile count % 4.
-  __shared__ int sc_e[4][2][W];
+  __shared__ int sc_e[4][2][W];      // per frame and window: log2 of the operand scale
+  __shared__ float mean_s[4][2][W];  // per frame and window: the window mean
   __shared__ long long win_base[4][W];
   __shared__ int win_valid[4][W];
   __shared__ long long win_loc[4][W];  // window index within its segment
@@ -1130,7 +1131,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   // Near-tie flags and subpixel fits of tile `tl` (local tile count `it`), run
   // by the fit warp: every lane waits for the tile's neighbour rows, the warp
   // runs the near-tie test, lanes < W fit one window each and set up the
-  // windows of tile tl + 3 strides, then lane 0 hands the rows back. False
+  // windows of tile tl + 4 strides, then lane 0 hands the rows back. False
   // when the wait gave up.
   auto fit_tile = [&](int tl, int it) -> bool {
     const bool got = __all_sync(0xffffffffu, tc::mbar_wait_bounded(&nbr_full, ph_full, kMaxPolls));
@@ -1183,11 +1184,11 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       if (sq.peak_i) sq.peak_i[gl] = pi_;
       if (sq.peak_j) sq.peak_j[gl] = pj;
     }
-    // The corners of the tile three strides on, into this tile's slot's
-    // predecessor (tile it - 1, whose fits are done): the compute warps use
-    // them from tile it + 2 on, after waiting for these fits in the epilogue
-    // of tile it + 1.
-    if (lane < W) window_setup(tl + 3 * stride, (it + 3) & 3, lane);
+    // The corners of the tile four strides on, into this tile's slot (its
+    // fits are done): the compute warps use them from tile it + 3 on (the
+    // copy of its rows), after waiting for these fits in the epilogue of
+    // tile it + 1.
+    if (lane < W) window_setup(tl + 4 * stride, it & 3, lane);
     __syncwarp();
     if (lane == 0) tc::mbar_arrive(&nbr_empty);
     return true;
@@ -1361,12 +1362,10 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       for (int c = 0; c < 2; ++c)
         cp_async16_zfill(row + 16 * stg64_chunk(t, 2 * h + c), src + (ok ? 16 * c : 0), ok);
     };
-    // Staging of the tile in slot sl -> stage-1 operands: thread (q, t) takes
-    // half h = q >> 1 of row y of window w of frame f = q & 1.
-    auto stage_tile = [&](int sl) {
-      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63, grp = h * 2 + ((t >> 5) & 1);
-      const bool ok = win_valid[sl][w] != 0;
-      float r[32];
+    // Half h = q >> 1 of row y of window w of frame f = q & 1 of the tile in
+    // slot sl, as floats (thread (q, t), w = t >> 6, y = t & 63).
+    auto load_half_row = [&](int sl, float (&r)[32]) {
+      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63;
       if (ASYNC) {
         const unsigned char* row = sm + L::STG + (f * 128 + t) * SS;
 #pragma unroll
@@ -1379,57 +1378,72 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       } else {
         const CorrSeg& sq = seg_s[win_seg[sl][w]];
         load_row(f == 0 ? sq.frame_a : sq.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * sq.width + 32 * h,
-                 ok, r);
+                 win_valid[sl][w] != 0, r);
       }
+    };
+    // Window statistics of the tile in slot sl: mean and operand scale
+    // exponent per frame and window (sum |2^e (a - mean)| <= 2^7), formed
+    // while the previous tile's stage 2 is on the tensor cores.
+    auto stage_stats = [&](int sl) {
+      const int f = q & 1, h = q >> 1, w = t >> 6, y = t & 63, grp = h * 2 + ((t >> 5) & 1);
+      float r[32];
+      load_half_row(sl, r);
       float sum = 0.f;
 #pragma unroll
       for (int x = 0; x < 32; ++x) sum += r[x];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0) red[f][w][grp] = sum;
+      if (lane == 0) red[0][f][w][grp] = sum;
       cw_sync();
-      const float mean = (red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3]) / (float)(SS * SS);
+      const float mean = (red[0][f][w][0] + red[0][f][w][1] + red[0][f][w][2] + red[0][f][w][3]) / (float)(SS * SS);
       float l = 0.f;
 #pragma unroll
-      for (int x = 0; x < 32; ++x) {
-        r[x] -= mean;
-        l += fabsf(r[x]);
-      }
+      for (int x = 0; x < 32; ++x) l += fabsf(r[x] - mean);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+      if (lane == 0) red[1][f][w][grp] = l;
       cw_sync();
-      if (lane == 0) red[f][w][grp] = l;
-      cw_sync();
-      const float l1 = red[f][w][0] + red[f][w][1] + red[f][w][2] + red[f][w][3];
-      int e = 0;
-      if (l1 > 0.f) e = min(120, max(-120, 6 - exp2_floor(l1)));
-      const float s = pow2i(e);
-#pragma unroll
-      for (int x = 0; x < 32; ++x) r[x] *= s;
       if (h == 0 && y == 0) {
+        const float l1 = red[1][f][w][0] + red[1][f][w][1] + red[1][f][w][2] + red[1][f][w][3];
+        int e = 0;
+        if (l1 > 0.f) e = min(120, max(-120, 6 - exp2_floor(l1)));
         sc_e[sl][f][w] = e;
+        mean_s[sl][f][w] = mean;
         const CorrSeg& sq = seg_s[win_seg[sl][w]];
-        if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
+        if (sq.win_means && win_valid[sl][w]) sq.win_means[2 * win_loc[sl][w] + f] = mean;
       }
+      // Every thread's stage_tile reads them (nothing else orders the two).
+      cw_sync();
+    };
+    // Staging of the tile in slot sl (statistics known) -> stage-1 operands:
+    // (a - mean) 2^e as fp16, no reductions or barriers on this path.
+    auto stage_tile = [&](int sl) {
+      const int f = q & 1, h = q >> 1, w = t >> 6;
+      float r[32];
+      load_half_row(sl, r);
+      const float mean = mean_s[sl][f][w], s = pow2i(sc_e[sl][f][w]);
+#pragma unroll
+      for (int x = 0; x < 32; ++x) r[x] = (r[x] - mean) * s;
 #pragma unroll
       for (int x = 0; x < 32; x += 8) st8(sm + L::A1 + f * L::A1_BYTES, off_k(t, 32 * h + x, SS), r + x);
     };
 
-    if (tid < W) {
-      window_setup(first, 0, tid);
-      window_setup(first + stride, 1, tid);
-      window_setup(first + 2 * stride, 2, tid);
-    }
+    if (tid < W)
+      for (int k = 0; k < 4; ++k) window_setup(first + k * stride, k, tid);
     cw_sync();
     if (first < n_tiles) {
       if (ASYNC) {
         stage_async(0);
         cp_async_commit();
         cp_async_wait_all();
-        cw_sync();
       }
+      stage_stats(0);
       stage_tile(0);
       signal(kRA1);
+      if (ASYNC && first + stride < n_tiles) {
+        stage_async(1);  // the next tile's rows land while this tile runs
+        cp_async_commit();
+      }
     }
 
     int it = 0;  // local tile count
@@ -1467,9 +1481,11 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
         }
       }
       signal(kRA2);
-      if (ASYNC && has_next) {
-        stage_async(sl1);  // the next tile's rows land while this tile runs
-        cp_async_commit();
+      // The next tile's window statistics while stage 2 runs (its rows were
+      // copied during the previous tile).
+      if (has_next) {
+        if (ASYNC) cp_async_wait_all();
+        stage_stats(sl1);
       }
 
       // ---- Product, per half hh of f_r: thread (q, t) folds g in [32 hh + 8 q, + 8)
@@ -1530,12 +1546,15 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
       }
       signal(kRA4);
 
-      // ---- The next tile's staging while stage 4 runs.
+      // ---- The next tile's staging while stage 4 runs; then the copy of the
+      // rows of the tile after it (each thread copies the bytes it reads).
       if (has_next) {
-        if (ASYNC) cp_async_wait_all();
-        cw_sync();
         stage_tile(sl1);
         signal(kRA1);
+        if (ASYNC && tile + 2 * stride < n_tiles) {
+          stage_async((it + 2) & 3);
+          cp_async_commit();
+        }
       }
 
       // ---- Epilogue: thread (q, t) holds shifted columns [64 ch, 64 ch + 64) of
