@@ -672,10 +672,6 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       }
     }
     if (!sync_for_mma()) break;
-    if (ASYNC) {
-      stage_async(sl ^ 1);  // the next tile's rows land while this tile runs
-      cp_async_commit();
-    }
 
     // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
     if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
@@ -687,6 +683,12 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           mma_chain<SPLIT>(tmem + rt * 2 * N + f * N, sbase + L::OP + (f * 2 + rt) * L::A2_BYTES, L::NOP, 32 * 128,
                            128 * 16, 128, sbase + L::B1, L::NB1, 256, 128, SS * 16, SS / 16, id, false);
       tc::mma_commit<SPLIT>(&bar);
+    }
+    // The next tile's rows land while this tile runs (issued after the MMAs,
+    // so that the issuing thread's copies do not hold up the product).
+    if (ASYNC) {
+      stage_async(sl ^ 1);
+      cp_async_commit();
     }
     wait_mma();
 
