@@ -62,10 +62,11 @@ struct TcLayout {
   static constexpr int B4 = B3 + 3 * P * NB3;           // [N][N] K-major
   // Operand region, rewritten by each phase once the product that read it has
   // completed: A1 2 x [128][SS] K-major; A2 2 x 2 x [128][SS] MN-major; A3
-  // [128][2N] K-major; A4 2 x [128][N] MN-major; then the peak-neighbour rows.
+  // [128][2N] K-major; A4 2 x [128][N] MN-major.
   static constexpr int OP = B4 + P * NB4;
   static constexpr int STG = OP + P * NOP;              // next tile's float rows [frame][128][SS], 16-byte chunks swizzled
-  static constexpr int END = STG + 2 * 128 * SS * 4;
+  static constexpr int NBR = STG + 2 * 128 * SS * 4;    // [W][3][N] floats: map rows pi-1, pi, pi+1 (natural columns)
+  static constexpr int END = NBR + W * 3 * N * 4;
   static constexpr int A1_BYTES = 128 * SS * 2;
   static constexpr int A2_BYTES = 128 * SS * 2;
   static constexpr int A4_BYTES = 128 * N * 2;
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
-  __shared__ int sc_e[2][W];         // per frame and window: log2 of the operand scale
+  __shared__ int sc_e[2][2][W];      // per slot, frame and window: log2 of the operand scale
   __shared__ long long win_base[2][W];
   __shared__ int win_valid[2][W];
   __shared__ long long win_loc[2][W];  // window index within its segment
@@ -483,12 +484,14 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     }
     tc::fence_after_sync();
   };
+  // Barrier before an MMA issue; false (for every thread alike) once a wait
+  // has given up.
   auto sync_for_mma = [&]() -> bool {
     tc::fence_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    const bool stop = __syncthreads_or(abort_s != 0);
     tc::fence_after_sync();
-    return abort_s == 0;
+    return !stop;
   };
   // Window corners of tile `tl` into slot `sl` (threads tid < W).
   auto window_setup = [&](int tl, int sl) {
@@ -561,10 +564,11 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   int sl = 0;
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
     const long long g0 = (long long)tile * W;
+    // No barrier here: warps 0 and 1 may still be finishing the previous
+    // tile's near-tie test and fits while the others stage this tile (its
+    // rows are the ones each thread copied itself). The stage-1 barrier
+    // below waits for all of them.
     if (ASYNC) cp_async_wait_all();
-    __syncthreads();
-    // The previous tile's epilogue has finished with the near-tie keys.
-    if (tid < W) sec_key[tid] = kKeyNegInf;
     cur_sl = sl;
     cur_g0 = g0;
 
@@ -611,7 +615,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 #pragma unroll
         for (int x = 0; x < SS; ++x) r[x] *= s;
         if (y == 0) {
-          sc_e[f][w] = e;
+          sc_e[sl][f][w] = e;
           const CorrSeg& sq = seg_s[win_seg[sl][w]];
           if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
         }
@@ -631,8 +635,12 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       tc::mma_commit<SPLIT>(&bar);
     }
     // The next tile's window corners, while the products run (slot sl ^ 1 was
-    // last read by the previous tile's fits, before its final barrier).
-    if (tid < W) window_setup(tile + gridDim.x, sl ^ 1);
+    // last read by the previous tile's fits, before the stage-1 barrier), and
+    // the near-tie keys of this tile (the previous tile's test is done).
+    if (tid < W) {
+      window_setup(tile + gridDim.x, sl ^ 1);
+      sec_key[tid] = kKeyNegInf;
+    }
     wait_mma();
 
     // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
@@ -785,14 +793,14 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     // ---- Epilogue. Row rt*128 + tid of the tile is map row r of window w
     // (scaled by 2^(e_a + e_b)); shifted row index i = r ^ N/2, shifted
     // column j = s ^ N/2. Lags without window overlap (i = 0 or j = 0) are 0.
-    float* nbrow = reinterpret_cast<float*>(sm + L::OP);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
+    float* nbrow = reinterpret_cast<float*>(sm + L::NBR);  // [W][3][N]: rows pi-1, pi, pi+1 (natural columns)
     // Subpixel fit and outputs of window ww with flat peak index pidx (its
     // neighbour rows in nbrow).
     auto finish = [&](int ww, int pidx) {
       const int pi_ = pidx / N, pj = pidx % N;
       float isp = (float)pi_, jsp = (float)pj;
       if (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1) {
-        const int ue = -sc_e[0][ww] - sc_e[1][ww];
+        const int ue = -sc_e[sl][0][ww] - sc_e[sl][1][ww];
         // Shifted (i, j) -> stored row slot i - pi + 1, natural column j ^ N/2.
         // x 2^ue as two exact power-of-two products (|ue| <= 240; each factor is a normal float).
         const float s1 = pow2i(ue >> 1), s2 = pow2i(ue - (ue >> 1));
@@ -818,6 +826,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       if (sq.peak_j) sq.peak_j[gl] = pj;
     };
     auto peak_row = [&](int ww) { return nbrow + (ww * 3 + 1) * N; };
+    bool stop = false;
     if constexpr (N == 32 && TPL == 1) {
       // One window per warp and row tile (N = 32 rows): the warp finds its
       // window's peak by shuffles and the lanes of the rows next to it store
@@ -842,7 +851,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         const float rbest = best;
         warp_first_max(best, idx);
         if (a.maps && g0 + w < total) {
-          const int ue = -sc_e[0][w] - sc_e[1][w];
+          const int ue = -sc_e[sl][0][w] - sc_e[sl][1][w];
           float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
 #pragma unroll
           for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
@@ -861,7 +870,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         }
         if (lane == 0) pk_idx[w][0] = idx;
       }
-      __syncthreads();
+      // The peaks and neighbour rows are in shared memory (the map's TMEM
+      // columns are read); the abort decision is the same for every thread.
+      tc::fence_before_sync();
+      stop = __syncthreads_or(abort_s != 0);
       // The near-tie flags in warp 1 while warp 0 fits.
       if (ties && warp == 1)
         write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return pk_idx[ww][0]; },
@@ -894,7 +906,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           pk_idx[w][r / 32] = idx;
         }
         if (a.maps && g0 + w < total) {
-          const int ue = -sc_e[0][w] - sc_e[1][w];
+          const int ue = -sc_e[sl][0][w] - sc_e[sl][1][w];
           float* mo = reinterpret_cast<float*>(a.maps) + (g0 + w) * N * N + (long long)i * N;
 #pragma unroll
           for (int j = 0; j < N; ++j) mo[j] = i == 0 ? 0.f : ldexpf(rowc[j], ue);
@@ -942,15 +954,17 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           }
         }
       }
-      __syncthreads();
+      // The peaks and neighbour rows are in shared memory (the map's TMEM
+      // columns are read); the abort decision is the same for every thread.
+      tc::fence_before_sync();
+      stop = __syncthreads_or(abort_s != 0);
       // The near-tie flags in warp 1 while warp 0 fits.
       if (ties && warp == 1) write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, window_peak, peak_row));
       if (tid < W && g0 + tid < total) finish(tid, window_peak(tid));
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (abort_s) break;
+    // No barrier: the other warps go on to stage the next tile while warps 0
+    // and 1 finish this one (the next tile's stage-1 barrier waits for them).
+    if (stop) break;
   }
   if (ASYNC) cp_async_wait_all();
   tc::fence_before_sync();
