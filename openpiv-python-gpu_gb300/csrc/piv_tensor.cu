@@ -255,21 +255,22 @@ PIV_D void sths(unsigned char* base, int lo, uint32_t off, float v) {
   if (SPLIT) *reinterpret_cast<__half*>(base + lo + off) = __float2half_rn(v - __half2float(h));
 }
 
-// D (+)= A B over `ks_n` k-steps, issued by one thread; with SPLIT also
-// A_hi B_lo and A_lo B_hi (a_lo / b_lo: byte distance to the lo copies).
+// D (+)= A B over `ks_n` k-steps, issued by one elected lane of the calling
+// converged warp; with SPLIT also A_hi B_lo and A_lo B_hi (a_lo / b_lo: byte
+// distance to the lo copies).
 template <bool SPLIT>
 PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uint32_t a_lbo, uint32_t a_sbo,
                      uint32_t b, uint32_t b_lo, uint32_t b_step, uint32_t b_lbo, uint32_t b_sbo, int ks_n,
                      uint32_t id, bool acc_first) {
   for (int ks = 0; ks < ks_n; ++ks)
-    tc::mma_f16<SPLIT>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo), id,
+    tc::mma_f16<true>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo), id,
                 acc_first || ks > 0);
   if (SPLIT) {
     for (int ks = 0; ks < ks_n; ++ks)
-      tc::mma_f16<SPLIT>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + b_lo + ks * b_step, b_lbo, b_sbo),
+      tc::mma_f16<true>(d, tc::sdesc(a + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + b_lo + ks * b_step, b_lbo, b_sbo),
                   id, 1);
     for (int ks = 0; ks < ks_n; ++ks)
-      tc::mma_f16<SPLIT>(d, tc::sdesc(a + a_lo + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo),
+      tc::mma_f16<true>(d, tc::sdesc(a + a_lo + ks * a_step, a_lbo, a_sbo), tc::sdesc(b + ks * b_step, b_lbo, b_sbo),
                   id, 1);
   }
 }
@@ -626,13 +627,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 1: T = a F^T per frame -> TMEM cols [f N, f N + N).
-    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
+    if (warp == 0) {  // MMA issue: a converged warp, one elected lane issues
       const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
       for (int f = 0; f < 2; ++f)
         mma_chain<SPLIT>(tmem + f * N, sbase + L::OP + f * L::A1_BYTES, L::NOP, 256, 128, SS * 16, sbase + L::B1,
                          L::NB1, 256, 128, SS * 16, SS / 16, id, false);
-      tc::mma_commit<SPLIT>(&bar);
+      tc::mma_commit<true>(&bar);
     }
     // The next tile's window corners, while the products run (slot sl ^ 1 was
     // last read by the previous tile's fits, before the stage-1 barrier), and
@@ -682,7 +683,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 2: X = T^T F^T for tiles e, o and frames a, b -> TMEM cols [rt 2N + f N, +N).
-    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
+    if (warp == 0) {  // MMA issue: a converged warp, one elected lane issues
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt)
@@ -690,7 +691,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         for (int f = 0; f < 2; ++f)
           mma_chain<SPLIT>(tmem + rt * 2 * N + f * N, sbase + L::OP + (f * 2 + rt) * L::A2_BYTES, L::NOP, 32 * 128,
                            128 * 16, 128, sbase + L::B1, L::NB1, 256, 128, SS * 16, SS / 16, id, false);
-      tc::mma_commit<SPLIT>(&bar);
+      tc::mma_commit<true>(&bar);
     }
     // The next tile's rows land while this tile runs (issued after the MMAs,
     // so that the issuing thread's copies do not hold up the product).
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 
     // ---- Stage 3: Re U = [Re P | Im M] [C; -S] -> TMEM cols [0, N),
     // Im U = [Im P | Re M] [C; S] -> cols [N, 2N).
-    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
+    if (warp == 0) {  // MMA issue: a converged warp, one elected lane issues
       const uint32_t id = tc::idesc_f16(128, N, 0, 0);
 #pragma unroll
       for (int part = 0; part < 2; ++part)
@@ -750,7 +751,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
           mma_chain<SPLIT>(tmem + part * N, sbase + L::OP + (part * N + kb * HN) * 16, L::NOP, 256, 128, 2 * N * 16,
                            sbase + L::B3 + (kb == 0 ? 0 : 1 + part) * L::P * L::NB3, L::NB3, 256, 128, HN * 16,
                            HN / 16, id, kb > 0);
-      tc::mma_commit<SPLIT>(&bar);
+      tc::mma_commit<true>(&bar);
     }
     wait_mma();
 
@@ -780,13 +781,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     if (!sync_for_mma()) break;
 
     // ---- Stage 4: c = U E' / N -> TMEM cols [rt N, rt N + N).
-    if (SPLIT ? warp == 0 : tid == 0) {  // MMA issue (split form: a warp, one elected lane issues)
+    if (warp == 0) {  // MMA issue: a converged warp, one elected lane issues
       const uint32_t id = tc::idesc_f16(128, N, 1, 0);
 #pragma unroll
       for (int rt = 0; rt < 2; ++rt)
         mma_chain<SPLIT>(tmem + rt * N, sbase + L::OP + rt * L::A4_BYTES, L::NOP, 32 * 128, 128 * 16, 128,
                          sbase + L::B4, L::NB4, 256, 128, N * 16, N / 16, id, false);
-      tc::mma_commit<SPLIT>(&bar);
+      tc::mma_commit<true>(&bar);
     }
     wait_mma();
 
