@@ -397,11 +397,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
-  __shared__ int sc_e[2][2][W];      // per slot, frame and window: log2 of the operand scale
-  __shared__ long long win_base[2][W];
-  __shared__ int win_valid[2][W];
-  __shared__ long long win_loc[2][W];  // window index within its segment
-  __shared__ int win_seg[2][W];
+  // Per tile slot (three: the tile being correlated, the next one, whose rows
+  // are in flight, and the one after, whose corners are being computed).
+  __shared__ int sc_e[3][2][W];      // per slot, frame and window: log2 of the operand scale
+  __shared__ long long win_base[3][W];
+  __shared__ int win_valid[3][W];
+  __shared__ long long win_loc[3][W];  // window index within its segment
+  __shared__ int win_seg[3][W];
   __shared__ CorrSeg seg_s[kMaxCorrSegs];
   __shared__ float pk_val[W][NPART];
   __shared__ int pk_idx[W][NPART];
@@ -494,9 +496,9 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     tc::fence_after_sync();
     return !stop;
   };
-  // Window corners of tile `tl` into slot `sl` (threads tid < W).
-  auto window_setup = [&](int tl, int sl) {
-    const long long g = (long long)tl * W + tid;
+  // Corners of window wi of tile `tl` into slot `sl`.
+  auto window_setup = [&](int tl, int sl, int wi) {
+    const long long g = (long long)tl * W + wi;
     int ok = tl < n_tiles && g < total;
     long long base = 0, loc = 0;
     int sg = 0;
@@ -515,10 +517,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
                                              (long long)q.n_pairs * q.height * q.width))
         ok = 0;
     }
-    win_valid[sl][tid] = ok;
-    win_base[sl][tid] = base;
-    win_loc[sl][tid] = loc;
-    win_seg[sl][tid] = sg;
+    win_valid[sl][wi] = ok;
+    win_base[sl][wi] = base;
+    win_loc[sl][wi] = loc;
+    win_seg[sl][wi] = sg;
   };
   // Thread (half, t) starts the copies of row t of its frames of the tile in
   // slot `sl`; rows of invalid windows are zero-filled (no global read), so
@@ -539,7 +541,8 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   };
 
   if (tid < W) {
-    window_setup(blockIdx.x, 0);
+    window_setup(blockIdx.x, 0, tid);
+    window_setup(blockIdx.x + gridDim.x, 1, tid);
     sec_key[tid] = kKeyNegInf;
   }
   __syncthreads();
@@ -563,7 +566,8 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
   };
 
   int sl = 0;
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl ^= 1) {
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, sl = sl == 2 ? 0 : sl + 1) {
+    const int sl1 = sl == 2 ? 0 : sl + 1, sl2 = sl1 == 2 ? 0 : sl1 + 1;
     const long long g0 = (long long)tile * W;
     // No barrier here: warps 0 and 1 may still be finishing the previous
     // tile's near-tie test and fits while the others stage this tile (its
@@ -635,13 +639,8 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
                          L::NB1, 256, 128, SS * 16, SS / 16, id, false);
       tc::mma_commit<true>(&bar);
     }
-    // The next tile's window corners, while the products run (slot sl ^ 1 was
-    // last read by the previous tile's fits, before the stage-1 barrier), and
-    // the near-tie keys of this tile (the previous tile's test is done).
-    if (tid < W) {
-      window_setup(tile + gridDim.x, sl ^ 1);
-      sec_key[tid] = kKeyNegInf;
-    }
+    // The near-tie keys of this tile (the previous tile's test is done).
+    if (tid < W) sec_key[tid] = kKeyNegInf;
     wait_mma();
 
     // ---- Stage 1 -> 2: row (w, y) of T becomes column y of the MN-major rows
@@ -696,7 +695,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     // The next tile's rows land while this tile runs (issued after the MMAs,
     // so that the issuing thread's copies do not hold up the product).
     if (ASYNC) {
-      stage_async(sl ^ 1);
+      stage_async(sl1);
       cp_async_commit();
     }
     wait_mma();
@@ -880,6 +879,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
         write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, [&](int ww) { return pk_idx[ww][0]; },
                                              peak_row));
       if (tid < W && g0 + tid < total) finish(tid, pk_idx[tid][0]);
+      if (warp == 2 && lane < W) window_setup(tile + 2 * gridDim.x, sl2, lane);
     } else {
       float rbest[2 / TPL];  // this thread's row maxima
 #pragma unroll
@@ -962,9 +962,13 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       // The near-tie flags in warp 1 while warp 0 fits.
       if (ties && warp == 1) write_near_ties(tile_near_ties<N, W>(lane, sec_key, a.tie_tol, window_peak, peak_row));
       if (tid < W && g0 + tid < total) finish(tid, window_peak(tid));
+      if (warp == 2 && lane < W) window_setup(tile + 2 * gridDim.x, sl2, lane);
     }
     // No barrier: the other warps go on to stage the next tile while warps 0
-    // and 1 finish this one (the next tile's stage-1 barrier waits for them).
+    // and 1 finish this one and warp 2 sets up the corners of the tile after
+    // the next (slot sl2, last read by the previous tile) with its integer
+    // divisions off the path of the MMAs; the next tile's stage-1 barrier
+    // waits for all of them.
     if (stop) break;
   }
   if (ASYNC) cp_async_wait_all();
