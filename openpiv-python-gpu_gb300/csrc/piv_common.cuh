@@ -29,6 +29,29 @@ template <typename T> PIV_D Cplx<T> cconj(Cplx<T> a) { return cmake<T>(a.x, -a.y
 
 // Round-to-nearest arithmetic without FMA contraction, used where the host
 // oracle evaluates an expression as separate IEEE operations.
+// Small unsigned integers as floats, exactly and without an integer-to-float
+// conversion (a reduced-rate instruction): the integer (below 2^16) becomes
+// the low mantissa bits of 2^23 (0x4B00xxxx = 2^23 + x), and 2^23 is
+// subtracted.
+PIV_D float u16_to_float(uint32_t x) { return __uint_as_float(0x4B000000u | x) - 8388608.0f; }
+// Byte k (0..3) of w, placed by a byte permute.
+PIV_D float u8_to_float(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
+}
+// A pixel of any supported type as a float.
+template <typename P>
+PIV_D float pixel_to_float(P v) {
+  return (float)v;
+}
+template <>
+PIV_D float pixel_to_float<uint8_t>(uint8_t v) {
+  return u16_to_float(v);
+}
+template <>
+PIV_D float pixel_to_float<uint16_t>(uint16_t v) {
+  return u16_to_float(v);
+}
+
 PIV_D float add_rn(float a, float b) { return __fadd_rn(a, b); }
 PIV_D float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 PIV_D float mul_rn(float a, float b) { return __fmul_rn(a, b); }

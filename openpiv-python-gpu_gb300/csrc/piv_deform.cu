@@ -611,8 +611,8 @@ __global__ void __launch_bounds__(kPfNT) k_prefilter(int H, int W, const P* __re
       for (int k = 0; k < kIters; ++k)
         if (r0 + kGroups * k < kPfR) {
           const uint32_t w = wv[k];
-          *reinterpret_cast<float4*>(dst + k * kGroups * kPfS) = make_float4(
-              (float)(w & 0xffu), (float)((w >> 8) & 0xffu), (float)((w >> 16) & 0xffu), (float)(w >> 24));
+          *reinterpret_cast<float4*>(dst + k * kGroups * kPfS) =
+              make_float4(u8_to_float(w, 0), u8_to_float(w, 1), u8_to_float(w, 2), u8_to_float(w, 3));
         }
     }
   } else if (t < 2 * kPfR) {
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kPfNT) k_prefilter(int H, int W, const P* __re
     for (int r = r0; r < r0 + kPfR / 2; ++r) {
       int gy = y0 - kPfK + r;
       if (gy < 0 || gy >= H) gy = mirror_any(gy, H);
-      reg[r * kPfS + rc] = (float)__ldg(col + (long long)gy * W);
+      reg[r * kPfS + rc] = pixel_to_float<P>(__ldg(col + (long long)gy * W));
     }
   }
   __syncthreads();

@@ -60,11 +60,12 @@ PIV_D void load4(const P* p, bool vec, float (&v)[4]) {
       v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
     } else if constexpr (sizeof(P) == 2) {
       const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
-      v[0] = (float)(q.x & 0xffffu), v[1] = (float)(q.x >> 16), v[2] = (float)(q.y & 0xffffu), v[3] = (float)(q.y >> 16);
+      v[0] = u16_to_float(q.x & 0xffffu), v[1] = u16_to_float(q.x >> 16), v[2] = u16_to_float(q.y & 0xffffu),
+      v[3] = u16_to_float(q.y >> 16);
     } else {
       const unsigned q = __ldg(reinterpret_cast<const unsigned*>(p));
 #pragma unroll
-      for (int k = 0; k < 4; ++k) v[k] = (float)((q >> (8 * k)) & 0xffu);
+      for (int k = 0; k < 4; ++k) v[k] = u16_to_float((q >> (8 * k)) & 0xffu);
     }
   } else {
 #pragma unroll

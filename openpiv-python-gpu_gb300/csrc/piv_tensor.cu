@@ -275,13 +275,6 @@ PIV_D void mma_chain(uint32_t d, uint32_t a, uint32_t a_lo, uint32_t a_step, uin
   }
 }
 
-// Byte k of w as a float, exactly, without an integer-to-float conversion
-// (a quarter-rate instruction): the byte becomes the low mantissa bits of
-// 2^23 (0x4B0000bb = 2^23 + b), and 2^23 is subtracted.
-PIV_D float u8_to_float(uint32_t w, int k) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
-}
-
 // 2^e for |e| <= 126.
 PIV_D float pow2i(int e) { return __int_as_float((127 + e) << 23); }
 
