@@ -1033,8 +1033,9 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   enum { kS1, kS2a, kS2b, kS3, kS4, kNDone };
   enum { kRA1, kRA2, kRQa, kRQ, kRA4, kNReady };
   __shared__ uint64_t done_bar[kNDone], ready_bar[kNReady];
-  // The neighbour rows of a tile are written (compute warps) / have been
-  // read by its fits (MMA warp). Each completes once per tile.
+  // The neighbour rows and peak keys of a tile are written (one arrival per
+  // compute warp) / have been read by its fits (fit warp). Each completes
+  // once per tile.
   __shared__ uint64_t nbr_full, nbr_empty;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
@@ -1071,7 +1072,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
   if (tid == 0) {
     for (int k = 0; k < kNDone; ++k) tc::mbar_init(&done_bar[k], 1);
     for (int k = 0; k < kNReady; ++k) tc::mbar_init(&ready_bar[k], L::NCW);
-    tc::mbar_init(&nbr_full, 1);
+    tc::mbar_init(&nbr_full, L::NCW);
     tc::mbar_init(&nbr_empty, 1);
     abort_s = 0;
   }
@@ -1600,7 +1601,10 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
           for (int k = 0; k < 64; ++k) mo[k] = i == 0 ? 0.f : ldexpf(v[k], ue);
         }
       }
-      cw_sync();
+      // Every warp's candidate is in the peak keys; the abort decision is the
+      // same for every compute thread (the fit warp's wait for this tile's
+      // rows then gives up by itself).
+      if (cw_sync_or(abort_s != 0)) break;
       {
         const int pidx = peak_index(pk_key[kb][w]), pi_ = pidx / N, pj = pidx % N;
         if (ties) {  // the warp's largest half-row maximum outside the peak row (a warp's rows share a window)
@@ -1634,13 +1638,14 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
           }
         }
       }
-      // The map's TMEM columns are read (the next tile's stage 2 may overwrite
-      // them) and the neighbour rows written: they go to the MMA warp, which
-      // runs the fits while this tile's successor is correlated.
+      // This warp's neighbour rows and near-tie key are written: the fit warp
+      // runs the fits once all sixteen warps have arrived, while this tile's
+      // successor is correlated. (The map's TMEM columns are read before
+      // this warp's stage-2 arrival of the next tile, which the stage-2
+      // product waits for.)
       tc::fence_before_sync();
-      const bool stop = cw_sync_or(abort_s != 0);
-      if (tid == 0) tc::mbar_arrive(&nbr_full);
-      if (stop) break;
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&nbr_full);
     }
     if (ASYNC) cp_async_wait_all();
   }
