@@ -686,7 +686,10 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
       tc::mma_commit<true>(&bar);
     }
     // The next tile's rows land while this tile runs (issued after the MMAs,
-    // so that the issuing thread's copies do not hold up the product).
+    // so that the issuing thread's copies do not hold up the product). Not
+    // before this tile's stage-1 barrier: warp 2 writes slot sl1's corners
+    // during the previous tile's fits, and that barrier is what orders them
+    // before these reads.
     if (ASYNC) {
       stage_async(sl1);
       cp_async_commit();
