@@ -8,8 +8,8 @@ during the next one); the 16/32-px engines keep three tile slots and overlap
 a tile's fits with the next tile's staging. A pair correlated alone (about
 one tile per CTA on 512 x 512 frames) must match the same pair inside
 batches of 5 and 12 pairs (up to about ten tiles per CTA, partial last
-tiles, tiles that straddle two pairs) bit for bit: fields, integer peaks and
-near-tie flags, for the fp16, hi/lo split and refined forms."""
+tiles, tiles that straddle two pairs) bit for bit: fields and integer
+peaks, for the fp16, hi/lo split and refined forms."""
 
 import ctypes
 
