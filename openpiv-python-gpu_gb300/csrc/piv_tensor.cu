@@ -977,7 +977,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 // 64-pixel windows (N = 128), warp-specialised and pipelined over tiles. One
 // CTA per SM with 16 compute warps (512 threads, four per TMEM lane; warp w
 // reads lanes 32 (w % 4); each phase splits its columns or frames between the
-// four) and one MMA warp. The MMA warp issues each product as soon as the
+// four), one MMA warp and one fit warp. The MMA warp issues each product as soon as the
 // compute warps have written its operand (one arrival per compute warp on
 // that operand's "ready" mbarrier) and commits it to the product's own
 // mbarrier, so the tensor core and the compute warps work on different
