@@ -976,19 +976,21 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 // ---------------------------------------------------------------------------
 // 64-pixel windows (N = 128), warp-specialised and pipelined over tiles. One
 // CTA per SM with 16 compute warps (512 threads, four per TMEM lane; warp w
-// reads lanes 32 (w % 4); each phase splits its columns or frames between the
-// four), one MMA warp and one fit warp. The MMA warp issues each product as soon as the
-// compute warps have written its operand (one arrival per compute warp on
-// that operand's "ready" mbarrier) and commits it to the product's own
-// mbarrier, so the tensor core and the compute warps work on different
-// phases at the same time: tile i + 1 is staged while stage 4 of tile i runs,
-// the map of tile i is searched while stage 1 of tile i + 1 runs, and the
-// product of the first half of stage 2 (f_r columns 0-63) is formed while
-// the second half is computed. A fit warp runs the near-tie test and the
-// subpixel fits of tile i (from the peak keys and the three map rows around
-// each peak, which the compute warps leave in a buffer of their own) while
-// tile i + 1 is correlated, so the compute warps go from the peak search
-// straight on to the next tile.
+// reads lanes 32 (w % 4); each phase splits its columns or frames between
+// the four), one MMA warp and one fit warp. The MMA warp issues each product
+// as soon as the compute warps have written its operand (one arrival per
+// compute warp on that operand's "ready" mbarrier) and commits it to the
+// product's own mbarrier, so the tensor core and the compute warps work on
+// different phases at the same time: the window statistics of tile i + 1
+// are formed while stage 2 of tile i runs, the product of the first half of
+// stage 2 (f_r columns 0-63) while the second half is computed, and the
+// first half of stage 3 while the second half of the product is formed;
+// tile i + 1 is staged while stage 4 of tile i runs, and the map of tile i
+// is searched while stage 1 of tile i + 1 runs. The fit warp runs the
+// near-tie test and the subpixel fits of tile i (from the peak keys and the
+// three map rows around each peak, which the compute warps leave in a
+// buffer of their own) while tile i + 1 is correlated, so the compute warps
+// go from the peak search straight on to the next tile.
 //   TMEM: stage 1 -> columns [256, 512); stage 2 half 0 -> [0, 256), half 1
 //   -> [256, 512); stages 3 and 4 -> [0, 256).
 //   Shared memory (211 KB): constants F (16 KB), C / -S / S (48 KB) and E'
