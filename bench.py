@@ -270,10 +270,10 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 def tc_executed_flops(ss, N, split=False):
     """FLOPs the tensor engine executes per window pair: packed real DFT along x
-    (both frames), along y (both frames), complex inverse along f_r over N/2
-    packed columns, real inverse along f_c (three products per stage with
-    hi/lo split operands)."""
-    macs = 2 * ss * ss * N + 2 * N * ss * N + (N // 2) * (2 * N) * (2 * N) + N * N * N
+    (both frames), along y (both frames), the inverse along f_r over N/2 packed
+    columns as two products of K = N on the folded frequency pairs, real
+    inverse along f_c (three products per stage with hi/lo split operands)."""
+    macs = 2 * ss * ss * N + 2 * N * ss * N + (N // 2) * (2 * N) * N + N * N * N
     return 2 * macs * (3 if split else 1)
 
 
@@ -557,6 +557,60 @@ def run_gpu(args):
         hbm = peaks.get("hbm_gbs")
         roofline["dram_gbs"] = roofline["traffic"] / (corr[dom] * 1e-3) / 1e9
         roofline["dram_frac"] = roofline["dram_gbs"] / hbm if hbm else None
+    if on_tensor and args.dft != "tensor":
+        # The refined and split forms' correlation stages hold more than one
+        # kernel; the dominant kernel is a pass's tensor-core engine alone,
+        # timed here with CUDA events on its stream over the step's pairs and
+        # that pass's geometry (passes 2 and 3 correlate deformed float32
+        # frames: the step's frames in float32 stand in for them).
+        engine = {}
+        frames_f32 = (fa.float(), fb.float())
+        for k, fk in enumerate(proc.piv_fields):
+            Nk = proc._iterations[k].fft_size
+            if not (Nk == 2 * fk.search_size and fk.search_size in (16, 32, 64)):
+                continue
+            mode = "tensor_split" if args.dft == "tensor_split" and fk.search_size in (16, 32) else "tensor"
+            da, db, pt = (fa, fb, "u8") if k == 0 else (frames_f32[0], frames_f32[1], "f32")
+            ue = torch.empty((B, *fk.field_shape), dtype=torch.float32, device="cuda")
+            ve = torch.empty_like(ue)
+
+            def run_engine():
+                _lib.check(lib.piv_correlate(ctypes.byref(fk.geometry), B, da.data_ptr(), db.data_ptr(),
+                                             _lib.PIXEL[pt], 0, Nk, 1, _lib.SUBPIXEL["gaussian"], None, ue.data_ptr(),
+                                             ve.data_ptr(), None, None, 0, 2, None, _lib.DFT[mode], stream.cuda_stream))
+
+            for _ in range(3):
+                run_engine()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(5):
+                run_engine()
+            e1.record(stream)
+            stream.synchronize()
+            engine[k] = (e0.elapsed_time(e1) / 5, mode, Nk)
+        if engine:
+            ke = max(engine, key=lambda k: engine[k][0])
+            ms_e, mode, Ne = engine[ke]
+            fe = proc.piv_fields[ke]
+            n_win_e = B * fe.n_wins
+            achieved_e = n_win_e * corr_flops(fe.search_size, Ne) / (ms_e * 1e-3) / 1e12
+            tw = traffic_w.get(f"correlate_tc{'s' if mode == 'tensor_split' else ''}_N{Ne}")
+            stage = dict(roofline)
+            roofline = {"bound": "tensor", "achieved": achieved_e, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved_e / peak, "traffic": tw * n_win_e if tw else None,
+                        "kernel": f"{'k_corr_tc64' if fe.search_size == 64 else f'k_corr_tc<{fe.search_size}>'} "
+                                  f"({mode} engine) alone, pass {ke + 1} (ss={fe.search_size}, N={Ne}, "
+                                  f"{n_win_e} windows/launch); the slowest engine launch of the step",
+                        "peak_source": src, "launch_ms": ms_e,
+                        "algorithmic_flops_per_window": corr_flops(fe.search_size, Ne),
+                        "engine_ms_per_pass": {f"pass {k + 1}": round(v[0], 4) for k, v in engine.items()}}
+            roofline["executed_tflops"] = (n_win_e * tc_executed_flops(fe.search_size, Ne, mode == "tensor_split")
+                                           / (ms_e * 1e-3) / 1e12)
+            roofline["executed_frac"] = roofline["executed_tflops"] / peak
+            if roofline["traffic"] and peaks.get("hbm_gbs"):
+                roofline["dram_gbs"] = roofline["traffic"] / (ms_e * 1e-3) / 1e9
+                roofline["dram_frac"] = roofline["dram_gbs"] / peaks["hbm_gbs"]
+            roofline["stage"] = stage
 
     device_status = proc.status()  # PIV_OK unless a bounded device-side wait gave up
 
