@@ -64,6 +64,8 @@ def parse_args():
                          "parity)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-modes", action="store_true",
+                    help="skip the mixed-size, serving and precision runs the default line summarises")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 FFT form beside the tensor form")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default correlation launch variants instead of autotuning them per pass")
@@ -668,9 +670,41 @@ def run_gpu(args):
             "device_status": device_status,
             "stage_ms": stage_ms,
         }
+        if world == 1 and not args.no_modes:
+            line["modes"] = other_modes()
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def other_modes(timeout_s=900):
+    """The mixed-size submission, serving and precision workloads, each run
+    once by this script in a process of its own (after the timed steps
+    above), summarised for the default line; a mode that fails or runs out
+    of time reports why instead."""
+    runs = {"mixed": ["--mixed", "--steps", "5", "--warmup", "3"], "serve": ["--serve"],
+            "precision": ["--precision", "--steps", "5", "--warmup", "3"]}
+    keep = {"mixed": ("metric", "value", "unit", "form", "chosen", "plain_form", "chosen_over_plain", "config"),
+            "serve": ("metric", "value", "unit", "p50_ms", "p99_ms", "mean_ms", "requests", "arrival_rate", "form",
+                      "plain_per_pair", "accuracy", "continuous_batching", "device_status", "config"),
+            "precision": ("metric", "value", "unit", "form", "ms_per_step", "chosen", "fp16_tensor_form", "plain_form",
+                          "chosen_over_plain", "config")}
+    out = {}
+    for name, extra in runs.items():
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True,
+                               timeout=timeout_s, cwd=ROOT)
+            lines = [ln for ln in r.stdout.strip().splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": f"exit {r.returncode}: {r.stderr.strip().splitlines()[-1:] or ''}"}
+                continue
+            d = json.loads(lines[-1])
+            out[name] = {k: d[k] for k in keep[name] if k in d}
+            if name in ("mixed", "precision") and isinstance(out[name].get("chosen"), dict):
+                out[name]["chosen"] = {k: v for k, v in out[name]["chosen"].items() if k not in ("tuning",)}
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": f"did not finish within {timeout_s} s"}
+    return out
 
 
 def run_serve(args):
