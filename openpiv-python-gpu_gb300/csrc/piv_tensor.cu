@@ -570,55 +570,75 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
     cur_sl = sl;
     cur_g0 = g0;
 
-    // ---- Staging: thread (half, t = (w, y)) takes row y of window w of its frames.
+    // ---- Staging: thread (half, t = (w, y)) takes row y of window w of its
+    // frames (both with one thread per TMEM lane: their reduction chains run
+    // side by side, each frame's arithmetic as for a frame alone).
     {
+      constexpr int NF = 2 / TPL;
       const int w = t / SS, y = t % SS;
       const bool ok = win_valid[sl][w] != 0;
+      float r[NF][SS];
 #pragma unroll
-      for (int fi = 0; fi < 2 / TPL; ++fi) {
+      for (int fi = 0; fi < NF; ++fi) {
         const int f = TPL == 2 ? half : fi;
-        float r[SS];
         if (ASYNC) {
           const unsigned char* row = sm + L::STG + (f * 128 + t) * SS * 4;
 #pragma unroll
           for (int c = 0; c < CH; ++c) {
             const float4 q4 = *reinterpret_cast<const float4*>(row + 16 * stg_chunk<CH>(t, c));
-            r[4 * c] = q4.x;
-            r[4 * c + 1] = q4.y;
-            r[4 * c + 2] = q4.z;
-            r[4 * c + 3] = q4.w;
+            r[fi][4 * c] = q4.x;
+            r[fi][4 * c + 1] = q4.y;
+            r[fi][4 * c + 2] = q4.z;
+            r[fi][4 * c + 3] = q4.w;
           }
         } else {
           const CorrSeg& q = seg_s[win_seg[sl][w]];
-          load_row(f == 0 ? q.frame_a : q.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * q.width, ok, r);
+          load_row(f == 0 ? q.frame_a : q.frame_b, a.pixel_type, win_base[sl][w] + (long long)y * q.width, ok,
+                   r[fi]);
         }
-        float sum = 0.f;
+      }
+      float sum[NF], mean[NF], l[NF];
 #pragma unroll
-        for (int x = 0; x < SS; ++x) sum += r[x];
-        // Window sums over its SS rows (a window's lanes are contiguous, SS | 32).
+      for (int fi = 0; fi < NF; ++fi) {
+        sum[fi] = 0.f;
 #pragma unroll
-        for (int o = 1; o < SS; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        const float mean = sum / (float)(SS * SS);
-        float l = 0.f;
+        for (int x = 0; x < SS; ++x) sum[fi] += r[fi][x];
+      }
+      // Window sums over its SS rows (a window's lanes are contiguous, SS | 32).
+#pragma unroll
+      for (int o = 1; o < SS; o <<= 1)
+#pragma unroll
+        for (int fi = 0; fi < NF; ++fi) sum[fi] += __shfl_xor_sync(0xffffffffu, sum[fi], o);
+#pragma unroll
+      for (int fi = 0; fi < NF; ++fi) {
+        mean[fi] = sum[fi] / (float)(SS * SS);
+        l[fi] = 0.f;
 #pragma unroll
         for (int x = 0; x < SS; ++x) {
-          r[x] -= mean;
-          l += fabsf(r[x]);
+          r[fi][x] -= mean[fi];
+          l[fi] += fabsf(r[fi][x]);
         }
+      }
 #pragma unroll
-        for (int o = 1; o < SS; o <<= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+      for (int o = 1; o < SS; o <<= 1)
+#pragma unroll
+        for (int fi = 0; fi < NF; ++fi) l[fi] += __shfl_xor_sync(0xffffffffu, l[fi], o);
+#pragma unroll
+      for (int fi = 0; fi < NF; ++fi) {
+        const int f = TPL == 2 ? half : fi;
         int e = 0;
-        if (l > 0.f) e = min(120, max(-120, L::SCALE_BITS - exp2_floor(l)));
+        if (l[fi] > 0.f) e = min(120, max(-120, L::SCALE_BITS - exp2_floor(l[fi])));
         const float s = pow2i(e);
 #pragma unroll
-        for (int x = 0; x < SS; ++x) r[x] *= s;
+        for (int x = 0; x < SS; ++x) r[fi][x] *= s;
         if (y == 0) {
           sc_e[sl][f][w] = e;
           const CorrSeg& sq = seg_s[win_seg[sl][w]];
-          if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean;
+          if (sq.win_means && ok) sq.win_means[2 * win_loc[sl][w] + f] = mean[fi];
         }
 #pragma unroll
-        for (int x = 0; x < SS; x += 8) st8s<SPLIT>(sm + L::OP + f * L::A1_BYTES, L::NOP, off_k(t, x, SS), r + x);
+        for (int x = 0; x < SS; x += 8)
+          st8s<SPLIT>(sm + L::OP + f * L::A1_BYTES, L::NOP, off_k(t, x, SS), r[fi] + x);
       }
     }
     if (!sync_for_mma()) break;
