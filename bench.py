@@ -230,15 +230,24 @@ class ClockSampler:
         self.proc = None
         self.path = None
 
-    def start(self):
+    def start(self, first_sample_s=3.0):
+        """Start sampling every 200 ms and wait (at most `first_sample_s`) for
+        the first sample, so that a timed region of a fraction of a second
+        is not over before nvidia-smi has started."""
         fd, self.path = tempfile.mkstemp(suffix=".csv")
-        os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
-                                          "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=fd,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            os.unlink(self.path)
+            return
+        finally:
+            os.close(fd)
+        deadline = time.monotonic() + first_sample_s
+        while time.monotonic() < deadline and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
