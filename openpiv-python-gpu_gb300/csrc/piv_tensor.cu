@@ -7,8 +7,9 @@
 // n_fft = 2, centred pad), the N real numbers
 //   R[0] = Re X(0), R[1] = Re X(N/2), R[2f] = Re X(f), R[2f+1] = Im X(f), 0 < f < N/2
 // hold the whole spectrum X (X(N-f) = conj X(f)); F is the N x ss matrix that
-// maps g to R. A CTA of 128 threads (one per TMEM lane) owns W = 128/ss
-// window pairs per tile:
+// maps g to R. A tile is W = 128/ss window pairs, one 128-row TMEM
+// accumulator (one or two threads per TMEM lane for ss 16 / 32, four for the
+// warp-specialised 64-px engine further down):
 //   stage 1  T = a F^T   rows (w, y),          K = x,  cols packed f_c       (per frame)
 //   stage 2  X = T^T F^T rows (tile e|o, w, c), K = y,  cols packed f_r       (per frame)
 //            tile e holds the rows k = 2c of T^T (Re T, or the DC column),
@@ -1013,7 +1014,7 @@ __global__ void __launch_bounds__(TcLayout<SS, SPLIT>::NT, TcLayout<SS, SPLIT>::
 // go from the peak search straight on to the next tile.
 //   TMEM: stage 1 -> columns [256, 512); stage 2 half 0 -> [0, 256), half 1
 //   -> [256, 512); stages 3 and 4 -> [0, 256).
-//   Shared memory (211 KB): constants F (16 KB), C / -S / S (48 KB) and E'
+//   Shared memory (216,064 bytes): constants F (16 KB), C / -S / S (48 KB) and E'
 //   (32 KB); the stage-1 operands (32 KB, then the first half of the stage-3
 //   operand); a 64 KB region for the stage-2 operands, then the second half
 //   of the stage-3 operand and the stage-4 operands; the next tile's 8-bit
