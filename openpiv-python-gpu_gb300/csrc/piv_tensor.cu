@@ -1373,7 +1373,8 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
     uint32_t ph[kNDone] = {0u, 0u, 0u, 0u, 0u};
     uint32_t ph_empty = 0u;
     // Every thread waits for the product itself; a wait that gives up sets
-    // abort_s, which all threads read after the tile's last barrier.
+    // abort_s, which the compute warps read through the barrier reduction
+    // after the peak search.
     auto done = [&](int k) {
       const bool ok = tc::mbar_wait_bounded(&done_bar[k], ph[k], kMaxPolls);
       ph[k] ^= 1u;
@@ -1639,7 +1640,7 @@ __global__ void __maxnreg__(96) k_corr_tc64(CorrArgs a, int* status) {
         }
         const bool mine = (ties && i == pi_) ||
                           (pi_ > 0 && pi_ < N - 1 && pj > 0 && pj < N - 1 && i >= pi_ - 1 && i <= pi_ + 1);
-        // The MMA warp has run the fits of the previous tile (it read the rows).
+        // The fit warp has run the fits of the previous tile (it has read the rows).
         if (it > 0) {
           const bool ok = tc::mbar_wait_bounded(&nbr_empty, ph_empty, kMaxPolls);
           ph_empty ^= 1u;
