@@ -319,7 +319,12 @@ int piv_field_geometry(int height, int width, int window_size, int search_size, 
  * get_s2n_ratio (gpu_process.py:1312-1347).
  *   frames_*: device [n_pairs][H][W] of pixel_type; masked windows (win_mask[k]
  *   nonzero, may be NULL) produce NaN displacement and zero s2n.
- *   u, v, s2n: device [n_pairs][m][n] of dtype; peak_i/peak_j may be NULL. */
+ *   u, v, s2n: device [n_pairs][m][n] of dtype; peak_i/peak_j may be NULL.
+ * Every search window of `geom` must lie inside the frame: a geometry whose
+ * last window passes the frame's edge (piv_field_geometry's centred grid with
+ * an odd search size and no spare pixel) gives PIV_E_UNSUPPORTED, inconsistent
+ * sizes or a negative n_pairs PIV_E_ARG (also piv_correlate_maps; plans refuse
+ * such passes at creation). */
 int piv_correlate(const piv_geometry* geom, int n_pairs, const void* frames_a, const void* frames_b,
                   int pixel_type, int dtype, int fft_size, int normalize, int subpixel_method,
                   const uint8_t* win_mask, void* u, void* v, int* peak_i, int* peak_j,

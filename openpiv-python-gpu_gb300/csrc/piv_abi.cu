@@ -217,6 +217,27 @@ static int plan_alloc_t(piv_plan* p, Ptr** ptr, size_t count) {
 
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
+// A geometry the correlation reads windows with: positive sizes and every
+// search window inside the frame. The kernels read window rows without
+// per-pixel frame checks. PIVFieldGPU's centred grid puts the last window
+// one pixel past the frame's edge for an odd search size that leaves no
+// spare pixel (gpu_process.py:932-933; the reference then stacks pixels it
+// never wrote, gpu_process.py:1127,1443-1447); such a geometry is refused.
+static int check_corr_geometry(const piv_geometry& g, int n_pairs) {
+  if (n_pairs < 0) return set_error(PIV_E_ARG, "n_pairs %d is negative", n_pairs);
+  if (g.height <= 0 || g.width <= 0 || g.search_size <= 0 || g.window_size <= 0 ||
+      g.window_size > g.search_size || g.spacing <= 0 || g.m <= 0 || g.n <= 0)
+    return set_error(PIV_E_ARG, "invalid geometry (frame %dx%d, search %d, window %d, spacing %d, field %dx%d)",
+                     g.height, g.width, g.search_size, g.window_size, g.spacing, g.m, g.n);
+  const long long y_end = (long long)(g.m - 1) * g.spacing + g.y_offset + g.search_size;
+  const long long x_end = (long long)(g.n - 1) * g.spacing + g.x_offset + g.search_size;
+  if (g.y_offset < 0 || g.x_offset < 0 || y_end > g.height || x_end > g.width)
+    return set_error(PIV_E_UNSUPPORTED,
+                     "windows outside the %dx%d frame (search %d, offset %d,%d, field %dx%d, spacing %d)", g.height,
+                     g.width, g.search_size, g.y_offset, g.x_offset, g.m, g.n, g.spacing);
+  return PIV_OK;
+}
+
 // The correlation engine of a pass and its launch variants.
 static int run_corr(int dft_mode, const CorrArgs& c, int variant, cudaStream_t s) {
   if (correlate_tensor_supported(c, dft_mode)) return correlate_tensor(c, dft_mode, variant, s);
@@ -344,6 +365,7 @@ int piv_plan_create(const piv_config* cfg, piv_plan** out) {
     IterState& s = p->st[k];
     s.it = it;
     rc = field_geometry(H, W, it.window_size, it.search_size, it.overlap_ratio, cfg->center, &s.g);
+    if (rc == PIV_OK) rc = check_corr_geometry(s.g, 0);
     if (rc) break;
     if (!is_pow2(it.fft_size) || it.fft_size < it.search_size || it.fft_size > 256) {
       rc = set_error(PIV_E_UNSUPPORTED, "fft_size %d (search size %d) is not supported", it.fft_size,
@@ -796,6 +818,7 @@ int piv_correlate(const piv_geometry* g, int n_pairs, const void* frames_a, cons
                   void* v, int* peak_i, int* peak_j, int s2n_method, int s2n_size, void* s2n, int dft_mode,
                   void* stream) {
   if (!g || !frames_a || !frames_b || !u || !v) return set_error(PIV_E_ARG, "NULL argument");
+  PIV_TRY(check_corr_geometry(*g, n_pairs));
   if (!is_pow2(fft_size) || fft_size < g->search_size || fft_size > 256)
     return set_error(PIV_E_UNSUPPORTED, "fft_size %d is not supported", fft_size);
   CorrArgs c{};
@@ -862,6 +885,7 @@ int piv_correlate_maps(const piv_geometry* g, int n_pairs, const void* frames_a,
                        int pixel_type, int dtype, int fft_size, int normalize, const uint8_t* win_mask, void* maps,
                        int dft_mode, void* stream) {
   if (!g || !frames_a || !frames_b || !maps) return set_error(PIV_E_ARG, "NULL argument");
+  PIV_TRY(check_corr_geometry(*g, n_pairs));
   if (!is_pow2(fft_size) || fft_size < g->search_size || fft_size > 256)
     return set_error(PIV_E_UNSUPPORTED, "fft_size %d is not supported", fft_size);
   cudaStream_t s = (cudaStream_t)stream;

@@ -48,6 +48,55 @@ def test_geometry_rejects_bad_args(lib):
     assert lib.piv_field_geometry(64, 64, 16, 16, 1.0, 1, ctypes.byref(g)) == _lib.PIV_E_ARG
 
 
+def _correlate_args(geom, n_pairs):
+    # Device pointers are never dereferenced: the geometry check returns first.
+    dev = ctypes.c_void_p(256)
+    return (ctypes.byref(geom), n_pairs, dev, dev, _lib.PIXEL["f32"], _lib.DTYPE["float32"], 16, 1,
+            _lib.SUBPIXEL["gaussian"], None, dev, dev, None, None, 0, 2, None, _lib.DFT["fft"], None)
+
+
+def test_correlation_refuses_windows_outside_the_frame(lib):
+    """The correlation kernels read window rows without per-pixel frame
+    checks, so the ABI refuses, before anything runs, a geometry whose search
+    windows pass the frame's edge: the centred grid of an odd search size with
+    no spare pixel (the reference would stack pixels it never wrote),
+    hand-made fields larger than the frame, and negative pair counts."""
+    g = _lib.PivGeometry()
+    _lib.check(lib.piv_field_geometry(63, 63, 9, 9, 0.0, 1, ctypes.byref(g)))
+    # Seven windows 9 px apart from column 1: the last one covers columns 55..63.
+    assert (g.n, g.spacing, g.x_offset) == (7, 9, 1)
+    assert lib.piv_correlate(*_correlate_args(g, 1)) == _lib.PIV_E_UNSUPPORTED
+    assert "outside" in _lib.last_error()
+    dev = ctypes.c_void_p(256)
+    assert lib.piv_correlate_maps(ctypes.byref(g), 1, dev, dev, _lib.PIXEL["f32"], _lib.DTYPE["float32"], 16, 1,
+                                  None, dev, _lib.DFT["fft"], None) == _lib.PIV_E_UNSUPPORTED
+
+    ok = _lib.PivGeometry()
+    _lib.check(lib.piv_field_geometry(64, 64, 16, 16, 0.5, 1, ctypes.byref(ok)))
+    big = _lib.PivGeometry.from_buffer_copy(ok)
+    big.m += 1
+    assert lib.piv_correlate(*_correlate_args(big, 1)) == _lib.PIV_E_UNSUPPORTED
+    bad = _lib.PivGeometry.from_buffer_copy(ok)
+    bad.spacing = 0
+    assert lib.piv_correlate(*_correlate_args(bad, 1)) == _lib.PIV_E_ARG
+    assert lib.piv_correlate(*_correlate_args(ok, -1)) == _lib.PIV_E_ARG
+    assert "negative" in _lib.last_error()
+
+
+def test_plan_refuses_windows_outside_the_frame(lib):
+    it = _lib.PivIteration(search_size=9, window_size=9, overlap_ratio=0.0, fft_size=16, deforming_order=1,
+                           deforming_par=0.5, normalize=1, subpixel_method=_lib.SUBPIXEL["gaussian"],
+                           validation_size=1, median_tol=2.0, num_replacing_iters=2, replacing_size=1,
+                           smoothing_par=0.5)
+    its = (_lib.PivIteration * 1)(it)
+    cfg = _lib.PivConfig(height=63, width=63, n_iters=1, iters=its, center=1, dt=1.0, scaling_par=1.0,
+                         dtype=_lib.DTYPE["float32"], pixel_type=_lib.PIXEL["f32"], max_pairs=1,
+                         dft_mode=_lib.DFT["fft"])
+    plan = ctypes.c_void_p()
+    assert lib.piv_plan_create(ctypes.byref(cfg), ctypes.byref(plan)) == _lib.PIV_E_UNSUPPORTED
+    assert "outside" in _lib.last_error() and not plan.value
+
+
 @pytest.mark.parametrize("kw", [
     dict(search_size_iters=(1, 2, 2), overlap_ratio=(0.5, 0.5, 0.75), n_fft=(2, 1, 3)),
     dict(search_size_iters=(2, 1), deforming_order=(1, 3), median_tol=(2, None), smoothing_par=0.5),
