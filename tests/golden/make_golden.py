@@ -2,7 +2,9 @@
 
 Run from the repository root on a machine that has the reference source:
 
-    python tests/golden/make_golden.py /path/to/openpiv-python-gpu
+    python tests/golden/make_golden.py /path/to/openpiv-python-gpu [case ...]
+
+(with case names, only those fixtures are written).
 
 The reference package is imported unmodified; ``cupy_shim`` maps CuPy to
 NumPy/SciPy and restates its four RawModule kernels. Stage outputs are
@@ -67,6 +69,14 @@ def cases():
          True),
         ("masked64", 2, (192, 192), 18, {"deforming_order": 1, "dtype_f": "float64", "mask": "disc"}, True),
         ("blank_region", 1, (128, 128), 19, {"median_tol": 2, "blank": True}, True),
+        ("validation5x5", 2, small, 20, {"deforming_order": 1, "validation_size": 2, "median_tol": 1.2,
+                                         "replacing_method": "median", "replacing_size": 2,
+                                         "num_replacing_iters": 2, "revalidate": True}, True),
+        ("overlap_per_pass", 2, (160, 160), 21, {"deforming_order": 1, "search_size_iters": (1, 1),
+                                                 "overlap_ratio": (0.5, 0.75)}, True),
+        ("nfft_real", 2, (160, 160), 22, {"deforming_order": 1, "search_size_iters": (1, 1),
+                                          "n_fft": (1.5, 3)}, True),
+        ("uint16", 2, small, 23, {"deforming_order": 1, "u16": True}, True),
     ]
 
 
@@ -86,13 +96,16 @@ def build_case(syn, cfg, shape, pair_index, overrides):
         b = b.copy()
         a[:48, :64] = 7
         b[:48, :64] = 7
+    if ov.pop("u16", False):  # 16-bit frames over the full range (x 257 maps 255 to 65535)
+        a = a.astype(np.uint16) * np.uint16(257)
+        b = b.astype(np.uint16) * np.uint16(257)
     piv.update(ov)
     if piv.get("mask") == "disc":
         piv["mask"] = _disc_mask(a.shape)
     return a, b, field, piv
 
 
-def run_reference(ref_root):
+def run_reference(ref_root, only=()):
     sys.path.insert(0, HERE)
     import cupy_shim
 
@@ -147,6 +160,8 @@ def run_reference(ref_root):
     gp.SmoothnGPU = gs.SmoothnGPU
 
     for name, cfg, shape, pair_index, overrides, store in cases():
+        if only and name not in only:
+            continue
         a, b, field, piv = build_case(syn, cfg, shape, pair_index, overrides)
         mss = piv.pop("min_search_size")
         stages.clear()
@@ -174,6 +189,6 @@ def run_reference(ref_root):
 
 
 if __name__ == "__main__":
-    if len(sys.argv) != 2:
-        sys.exit("usage: python tests/golden/make_golden.py <path of the openpiv-python-gpu source tree>")
-    run_reference(sys.argv[1])
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the openpiv-python-gpu source tree> [case ...]")
+    run_reference(sys.argv[1], tuple(sys.argv[2:]))
