@@ -690,8 +690,8 @@ def other_modes(timeout_s=300):
     """The mixed-size submission, serving and precision workloads, each run
     once by this script in a process of its own (after the timed steps
     above), summarised for the default line; a mode that fails or runs out
-    of time reports why instead (each takes well under a minute on a
-    GB300; the limit bounds the default run if one stalls)."""
+    of time reports why instead (the three together take under two minutes
+    on a GB300; the limit bounds the default run if one stalls)."""
     runs = {"mixed": ["--mixed", "--steps", "5", "--warmup", "3"], "serve": ["--serve"],
             "precision": ["--precision", "--steps", "5", "--warmup", "3"]}
     keep = {"mixed": ("metric", "value", "unit", "form", "chosen", "plain_form", "chosen_over_plain", "config"),
